@@ -1,0 +1,391 @@
+#!/usr/bin/env python3
+"""Benchmark: cell-timesteps/s of the mHM cell chain + mRM routing (FP64).
+
+Default workload (the single large domain): L1 1000 x 1000 cells, 6 soil
+horizons, hourly steps, L11 = 4 x 4 L1 cells (62,500 routing nodes, fractal
+DEM with a folded main valley: 1478 topological levels).  One benchmark step
+advances the whole basin by one chunk of 240 hourly time steps (10 days):
+forcing for the chunk (precipitation from a Gaussian random field with a
+20-cell length scale, 70 % dry hours, Gamma(0.6, 2 mm/h) amounts; temperature
+8 + 10 sin + N(0, 3) degC; Hargreaves PET) is resident in HBM and the cell
+chain, the L1->L11 accumulation and the Muskingum routing all run.  Steps
+continue the same simulation (states carry over); the forcing window repeats
+every step.  Inputs (3 x 1.92 GB of forcing per step) exceed the 129 MB L2,
+so no extra L2 flush is needed.
+
+`value` is device-timed throughput with inputs in HBM; `e2e` is the same run
+through the C ABI with the forcing in pinned host memory, copied to the
+device inside the timed region (overlapped with compute by the library) and
+the gauge discharge copied back every step.
+
+--impl reference times the CPU restatement of the reference (the oracle,
+libm build = the C library's exp/log/pow as gfortran calls them, OpenMP over
+cells as the reference's own loop, serial routing) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-timesteps/s (mHM+mRM, FP64)"
+UNIT = "cell-timesteps/s"
+CONFIGS = {
+    # name: (nrows, ncols, H, l11_factor, chunk_steps, dem kwargs)
+    "large": (1000, 1000, 6, 4, 240, dict(dem_kind="fractal", fractal_beta=3.0, tilt=0.0005, ridges=6)),
+    "small": (96, 96, 3, 4, 240, dict(dem_kind="plane")),
+}
+ALG_BYTES_PER_CELL_STEP = 32  # 24 B forcing read + 8 B total runoff write
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[4:8]):
+                if v.strip().lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except json.JSONDecodeError:
+            pass
+    return {}
+
+
+def traffic_from_profiles(name: str):
+    """DRAM bytes per cell-step of the cell-chain kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_cell_step:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def build_workload(cfg_name: str, seed: int = 1):
+    from mhm_gb300 import synth
+    nr, nc, H, f11, chunk, demkw = CONFIGS[cfg_name]
+    dom = synth.make_domain(nr, nc, H, f11, seed=seed, **demkw)
+    params = synth.make_eff_params(dom, seed=3)
+    return dom, params, chunk
+
+
+def device_forcing(dom, n_steps: int, seed: int, device):
+    """Forcing window [n_steps, N] generated on the GPU (torch as plumbing):
+    GRF-correlated precipitation occurrence (20-cell length scale, 70 % dry),
+    Gamma(0.6, 2) amounts, seasonal temperature + noise, Hargreaves PET."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    nr, nc = dom.nrows, dom.ncols
+    ky = torch.fft.fftfreq(nr, device=device)[:, None]
+    kx = torch.fft.rfftfreq(nc, device=device)[None, :]
+    filt = torch.exp(-2.0 * (torch.pi * 20.0) ** 2 * (kx * kx + ky * ky))
+    pre = torch.empty((n_steps, dom.n_cells), dtype=torch.float64, device=device)
+    gam = torch.distributions.Gamma(torch.tensor(0.6, dtype=torch.float64, device=device),
+                                    torch.tensor(0.5, dtype=torch.float64, device=device))
+    torch.manual_seed(seed)
+    for t in range(n_steps):
+        w = torch.randn((nr, nc), generator=g, device=device, dtype=torch.float64)
+        field = torch.fft.irfft2(torch.fft.rfft2(w) * filt, s=(nr, nc))
+        thr = torch.quantile(field.flatten()[:: max(1, nr * nc // 100000)], 0.7)
+        amt = gam.sample((nr, nc))
+        p2d = torch.where(field > thr, amt, torch.zeros_like(amt))
+        pre[t] = p2d.T.reshape(-1)  # column-major pack
+    hours = torch.arange(n_steps, device=device, dtype=torch.float64)
+    doy = (hours // 24) % 365 + 1
+    seas = 8.0 + 10.0 * torch.sin(2 * torch.pi * (doy - 81) / 365.0)
+    temp = seas[:, None] + 3.0 * torch.randn((n_steps, dom.n_cells), generator=g, device=device, dtype=torch.float64)
+    lat = torch.deg2rad(torch.from_numpy(dom.latitude).to(device))
+    dr = 1 + 0.033 * torch.cos(2 * torch.pi * doy / 365.0)
+    dec = 0.409 * torch.sin(2 * torch.pi * doy / 365.0 - 1.39)
+    ws = torch.arccos(torch.clamp(-torch.tan(lat)[None, :] * torch.tan(dec)[:, None], -1, 1))
+    ra = 24 * 60 / torch.pi * 0.082 * dr[:, None] * (ws * torch.sin(lat)[None, :] * torch.sin(dec)[:, None] +
+                                                      torch.cos(lat)[None, :] * torch.cos(dec)[:, None] * torch.sin(ws))
+    pet = torch.clamp(0.0023 * ra * 0.408 * (seas[:, None] + 17.8) * (10.0 ** 0.5), min=0.0) / 24.0
+    return pre.contiguous(), temp.contiguous(), pet.contiguous()
+
+
+def run_gpu(args) -> dict:
+    import torch
+    from mhm_gb300 import synth
+    from mhm_gb300._lib import load
+    from mhm_gb300.model import MhmGpu
+
+    rank, world, local = _env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(device)
+    lib = load()
+    dom, params, chunk = build_workload(args.config)
+    N = dom.n_cells
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, device=device.index)
+    g.prepare(params, synth.ROUTING_PARAMS_DEFAULT)
+    pre, temp, pet = device_forcing(dom, chunk, seed=2 + rank, device=device)
+    stream = torch.cuda.ExternalStream(g.stream, device=device)
+
+    def step(s: int, on_device=True, host=None):
+        tt0 = 1 + s * chunk
+        if on_device:
+            g.set_meteo(tt0, pre, temp, pet, on_device=True)
+        else:
+            g.set_meteo(tt0, *host)
+        return g.run(tt0, chunk)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # FP64 issue-rate peak on this GPU (roofline denominator for the FP64 pipe)
+    import ctypes as C
+    fl = C.c_double()
+    fp64_peak = None
+    if lib.mhm_probe_fp64(20000, C.byref(fl)) == 0:
+        fp64_peak = fl.value
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+    g.set_timing(True)
+    launches0 = lib.mhm_kernel_launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(device.index) as clk:
+        ev0.record(stream)
+        for s in range(args.warmup, args.warmup + args.steps):
+            step(s)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = lib.mhm_kernel_launch_count() - launches0
+    n_cell, t_cell = g.get_timing(0)
+    n_acc, t_acc = g.get_timing(1)
+    n_rt, t_rt = g.get_timing(2)
+    g.set_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    units = float(N) * chunk * args.steps * world
+    value = units / (ms * 1e-3)
+
+    # ---- e2e: host forcing (pinned), H2D + compute + D2H of the gauge series per step ----
+    host = [torch.empty((chunk, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    for h, d in zip(host, (pre, temp, pet)):
+        h.copy_(d)
+    hnp = [h.numpy() for h in host]
+    e2e_steps = max(1, min(args.steps, 3))
+    step(args.warmup + args.steps, on_device=False, host=hnp)  # warm the staging buffers
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(e2e_steps):
+        step(args.warmup + args.steps + 1 + s, on_device=False, host=hnp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    e2e_ms = max(e2e_ms, wall_ms)  # host copies happen inside mhm_run; count whichever is longer
+    if world > 1:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = float(N) * chunk * e2e_steps * world / (e2e_ms * 1e-3)
+
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    per_launch_s = (t_cell / max(n_cell, 1)) * 1e-3
+    alg_bytes = ALG_BYTES_PER_CELL_STEP * N * chunk
+    achieved = alg_bytes / per_launch_s / 1e9
+    tb = traffic_from_profiles("cell_chain_large.md")
+    fp64_line = None
+    ops = traffic_from_profiles_ops()
+    if fp64_peak and ops:
+        flops = ops * N * chunk / per_launch_s
+        fp64_line = {"achieved": flops / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": flops / fp64_peak, "peak_source": "measured live (DFMA probe)",
+                     "flop_per_cell_step": ops}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"single large domain: L1 {dom.nrows}x{dom.ncols} ({N} cells), "
+                               f"{dom.n_horizons} soil horizons, hourly, L11 {dom.n_nodes} nodes "
+                               f"({dom.depth_stats()[0]} routing levels); step = {chunk} time steps",
+                   "cells": N, "horizons": dom.n_horizons, "l11_nodes": dom.n_nodes,
+                   "routing_levels": dom.depth_stats()[0], "steps_per_bench_step": chunk,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (forcing 3 x %.2f GB per step)" % (chunk * N * 8 / 1e9)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * chunk * N * 8,
+                "d2h_bytes_per_step": chunk * len(dom.gauge_node) * 8, "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": (tb * N * chunk) if tb else None,
+                     "kernel": "cell_chain_kernel<6>", "alg_bytes_per_launch": alg_bytes,
+                     "launch_ms": per_launch_s * 1e3, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
+                     if peaks else "of fallback"},
+        "roofline_fp64": fp64_line,
+        "kernel_time_ms": {"cell_chain": t_cell, "runoff_acc": t_acc, "routing": t_rt,
+                           "timed_region": ms},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(dom, params, args)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def traffic_from_profiles_ops():
+    f = ROOT / "profiles" / "cell_chain_large.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("fp64_flop_per_cell_step:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(dom, params, args, target_s: float = 15.0) -> dict:
+    """The oracle (libm build, OpenMP over cells, serial routing) on a bounded
+    sample of the same workload: the same basin, consecutive 24-step blocks
+    (one 24-step forcing block, repeated as the GPU run repeats its window)
+    until ~target_s seconds have been spent."""
+    from mhm_gb300 import synth
+    from oracle.oracle import OracleRun
+    threads = os.cpu_count() or 1
+    r = OracleRun(dom, params, synth.ROUTING_PARAMS_DEFAULT, kind="libm")
+    blk = 24
+    f = synth.make_forcing(dom, blk, seed=5)
+    r.run(f, 1, 1, blk, nthreads=threads)  # first block: SM initialisation and warm-up, untimed
+    done = 0
+    t0 = time.perf_counter()
+    tt = blk + 1
+    while time.perf_counter() - t0 < target_s:
+        r.run(f, tt, tt, blk, nthreads=threads)
+        tt += blk
+        done += blk
+    dt = time.perf_counter() - t0
+    return {"value": dom.n_cells * done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{dom.n_cells} cells x {done} hourly steps in {dt:.1f} s (oracle libm build, "
+                      f"OpenMP {threads} threads over cells, serial routing)"}
+
+
+def run_reference(args) -> dict | None:
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return None
+    from oracle import oracle
+    oracle.build()
+    dom, params, chunk = build_workload(args.config)
+    base = cpu_baseline(dom, params, args, target_s=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
+    v = base["value"]
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dom.n_cells * chunk / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"single large domain: L1 {dom.nrows}x{dom.ncols}, {dom.n_horizons} horizons, "
+                                   f"hourly, {dom.n_nodes} L11 nodes; step = {chunk} time steps"},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    out = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * mhm_gpu.h -- C ABI of the GB300 implementation of mHM's per-cell water
+ * balance and mRM's Muskingum routing (libmhm_gpu.so).
+ *
+ * The reference has no C interface: its hot path is a set of Fortran module
+ * procedures.  Each entry point below replaces one of them, with the same
+ * argument meaning, and is what an iso_c_binding interface module on the
+ * Fortran side binds (the binding is shown in INTEGRATION.md).
+ *
+ * Conventions
+ *   - Every function returns an int status: MHM_OK (0) or a negative MHM_ERR_*
+ *     code; mhm_last_error() gives a message.  Arguments are validated on the
+ *     host before anything is launched.
+ *   - Arrays follow the reference's layout: L1 cells are packed column-major
+ *     over the mask (src/common/mo_grid.f90:145-150), 2-D (cell, horizon) and
+ *     (cell, month) arrays are column-major, i.e. element (k, h) is at
+ *     [h * n_cells + k]; index VALUES (L1_L11_Id, netPerm, fromN, toN, gauge
+ *     nodes) are 1-based as in Fortran.
+ *   - Host pointers are borrowed for the duration of the call only, except
+ *     the forcing set by mhm_set_forcing, which is read by the following
+ *     mhm_run calls.
+ *   - A context is used by one host thread at a time (the reference is not
+ *     reentrant either); separate contexts may run concurrently.
+ *   - A context owns all its device memory.  Several parameter sets
+ *     ("members", e.g. a calibration ensemble) can share one domain and one
+ *     forcing: member m has its own effective parameters, states and outputs.
+ *   - All state arithmetic is IEEE FP64.
+ */
+#ifndef MHM_GPU_H
+#define MHM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MHM_OK 0
+#define MHM_ERR_INVALID (-1)     /* bad argument or shape */
+#define MHM_ERR_CUDA (-2)        /* CUDA runtime error or no device */
+#define MHM_ERR_OOM (-3)         /* device allocation failed */
+#define MHM_ERR_TIMEOUT (-4)     /* a bounded device wait ran out */
+#define MHM_ERR_NAN (-5)         /* non-finite state or forcing detected */
+#define MHM_ERR_UNSUPPORTED (-6) /* process option not implemented */
+
+/* forcing kinds for mhm_set_forcing (the reference's L1_pre, L1_temp, L1_pet,
+ * L1_tmin, L1_tmax of src/meteo/mo_meteo_handler.f90) */
+#define MHM_FORC_PRE 0
+#define MHM_FORC_TEMP 1
+#define MHM_FORC_PET 2
+#define MHM_FORC_TMIN 3
+#define MHM_FORC_TMAX 4
+
+typedef struct mhm_ctx mhm_ctx;
+
+/* One basin: what mHM's initialisation (mhm_interface_init, mrm_init) hands
+ * to the time loop.  Replaces the module globals read by do_time_step
+ * (src/mHM/mo_mhm_interface_run.f90:341-638) and mRM_routing
+ * (src/mRM/mo_mrm_routing.f90:104-110). */
+typedef struct {
+    int32_t n_cells;             /* level1%nCells                              */
+    int32_t n_horizons;          /* nSoilHorizons_mHM (1..8)                   */
+    int32_t n_nodes;             /* level11%nCells                             */
+    int32_t n_outlets;           /* L11_nOutlets                               */
+    int32_t timestep;            /* model time step [h] (mhm.nml timestep)     */
+    int32_t proc_soilmoist;      /* processMatrix(3,1): 1..4                   */
+    int32_t proc_pet;            /* processMatrix(5,1): -1, 0 or 1             */
+    int32_t proc_routing;        /* processMatrix(8,1): 0 or 1                 */
+    int32_t n_tstep_forcing_day; /* 24 (hourly forcing) or 1 (daily forcing)   */
+    int32_t jul_start;           /* simPer%julStart (Julian day number)        */
+    int32_t map_flag;            /* routing resolution >= hydrology resolution */
+    int32_t n_gauges;            /* domain_mrm%nGauges                         */
+    int32_t n_members;           /* parameter sets run together (>= 1)         */
+    int32_t read_states;         /* 1: states come from a restart (no SM reset
+                                    at tt == 1, C1/C2 not regenerated)         */
+    const double *evap_coeff;    /* [12] mhm.nml &panEvapo                      */
+    const double *fday_prec, *fnight_prec; /* [12] &nightDayRatio             */
+    const double *fday_pet, *fnight_pet;   /* [12]                            */
+    const double *fday_temp, *fnight_temp; /* [12]                            */
+    const double *l1_area_km2;   /* [n_cells] level1%CellArea * 1e-6           */
+    const int32_t *l1_l11_id;    /* [n_cells] L1_L11_Id                        */
+    const double *l11_area_km2;  /* [n_nodes] level11%CellArea * 1e-6          */
+    const int32_t *l11_l1_id;    /* [n_nodes] L11_L1_Id (used if !map_flag)    */
+    const int32_t *net_perm;     /* [n_nodes] L11_netPerm (1..nLinks valid)    */
+    const int32_t *from_n;       /* [n_nodes] L11_fromN                        */
+    const int32_t *to_n;         /* [n_nodes] L11_toN                          */
+    const double *length;        /* [nLinks] L11_length [m]                    */
+    const double *slope;         /* [nLinks] L11_slope                         */
+    const double *ffp_imp;       /* [nLinks] L11_nLinkFracFPimp                */
+    const int32_t *gauge_node;   /* [n_gauges] gaugeNodeList                   */
+    const double *latitude;      /* [n_cells] level1%y (only for proc_pet = 1) */
+} mhm_domain_desc;
+
+/* L1 effective parameters of one member: the L1_* arrays of
+ * src/MPR/mo_mpr_global_variables.f90 that mHM() reads
+ * (src/mHM/mo_mhm_interface_run.f90:405-451), for one land-cover scene. */
+typedef struct {
+    const double *fSealed, *alpha, *degDayInc, *degDayMax, *degDayNoPre;
+    const double *fAsp, *HarSamCoeff;
+    const double *karstLoss, *kFastFlow, *kSlowFlow, *kBaseFlow, *kPerco;
+    const double *jarvis_thresh_c1, *tempThresh, *unsatThresh, *sealedThresh;
+    const double *maxInter;        /* [12 * n_cells] (cell, LAI month)          */
+    const double *petLAIcorFactor; /* [12 * n_cells] or NULL (proc_pet = -1)    */
+    const double *fRoots, *soilMoistSat, *soilMoistFC, *wiltingPoint, *soilMoistExp; /* [H * n_cells] */
+} mhm_eff_params;
+
+/* Restart state of one member: the fields of src/mHM/mo_restart.f90:146-258
+ * (L1_Inter, L1_snowPack, L1_sealSTW, L1_soilMoist, L1_unsatSTW, L1_satSTW)
+ * and src/mRM/mo_mrm_restart.f90:231-272 (L11_qOUT, L11_qTIN, L11_qTR,
+ * L11_Qmod, L11_C1, L11_C2), packed as in the reference's memory. */
+typedef struct {
+    double *interc, *snowpack, *sealSTW, *unsatSTW, *satSTW; /* [n_cells]        */
+    double *soilMoist;                                       /* [H * n_cells]    */
+    double *qOUT, *Qmod;                                     /* [n_nodes]        */
+    double *qTIN, *qTR;            /* [2 * n_nodes]: column 1 = previous step     */
+    double *C1, *C2;                                         /* [n_nodes]        */
+} mhm_restart;
+
+/* Context lifetime.  Replaces mhm_interface_init's domain set-up
+ * (src/mHM/mo_mhm_interface.F90:37-228): validates the network (netPerm must
+ * be a topological order of the links) and builds the device-side routing
+ * levels.  Selects device `device` (-1: current). */
+int mhm_ctx_create(const mhm_domain_desc *desc, int32_t device, mhm_ctx **out);
+int mhm_ctx_destroy(mhm_ctx *ctx);
+const char *mhm_last_error(const mhm_ctx *ctx);
+/* cudaStream_t of the context (work of all calls is ordered on it). */
+void *mhm_ctx_stream(mhm_ctx *ctx);
+
+/* Effective parameters of `member` (the restart path of
+ * mhm_interface_run_prepare, src/mHM/mo_mhm_interface_run.f90:221-231). */
+int mhm_set_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
+
+/* Muskingum coefficients C1/C2 of `member` from the five routing parameters
+ * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device). */
+int mhm_set_routing_params(mhm_ctx *ctx, int32_t member, const double *rout_param5);
+
+/* Default initial states (fluxes_states_default_init,
+ * src/mHM/mo_init_states.f90:258-345, and fluxes_states_default_init_routing,
+ * src/mRM/mo_mrm_init.f90:453-499).  horizon_depth[n_horizons] in mm. */
+int mhm_init_states(mhm_ctx *ctx, int32_t member, const double *horizon_depth);
+
+/* Forcing rows row0 .. row0+n_rows-1 (1-based forcing step index iMeteoTS of
+ * src/meteo/mo_meteo_handler.f90:575-620), layout [n_rows][n_cells].
+ * on_device = 0: host memory, copied to the device inside mhm_run (pinned
+ * memory from mhm_host_alloc overlaps the copies with compute);
+ * on_device = 1: device memory that stays valid until the next
+ * mhm_set_forcing of that kind. */
+int mhm_set_forcing(mhm_ctx *ctx, int32_t kind, int32_t row0, int32_t n_rows, const double *data,
+                    int32_t on_device);
+
+/* Advance all members by time steps tt0 .. tt0+n_steps-1 (1-based as the
+ * reference's tt): n_steps x do_time_step (src/mHM/mo_mhm_interface_run.f90:
+ * 341-638) without file output, i.e. meteo for the step, the mHM() cell chain
+ * (src/mHM/mo_mhm.f90:229-521) and mRM_routing (src/mRM/mo_mrm_routing.f90:
+ * 104-303).  q_gauge (host, may be NULL): gauge discharge [m3 s-1],
+ * laid out [member][gauge][step] (per member the column-major
+ * mRM_runoff(step, gauge) of the reference).  Blocks until done. */
+int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
+
+/* Per-step L1 total runoff [mm TS-1] and L11 discharge of the last mhm_run:
+ * optional outputs enabled before the run (adds HBM traffic). */
+int mhm_enable_outputs(mhm_ctx *ctx, int32_t total_runoff, int32_t qmod);
+/* total_runoff [n_steps][member][n_cells]; qmod [member][n_steps][n_nodes] */
+int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod);
+
+/* Restart state of one member (host buffers). */
+int mhm_get_state(mhm_ctx *ctx, int32_t member, const mhm_restart *st);
+int mhm_set_state(mhm_ctx *ctx, int32_t member, const mhm_restart *st);
+
+/* One state or flux variable by the reference's pybind name
+ * (pybind/src/wrapper.f90:569-777): "L1_INTER", "L1_SNOWPACK", "L1_SEALSTW",
+ * "L1_SOILMOIST", "L1_UNSATSTW", "L1_SATSTW", "L11_QMOD", "L11_QOUT". */
+int mhm_get_var(mhm_ctx *ctx, int32_t member, const char *name, double *out);
+
+/* Per-kernel device time of the calls since the last reset, measured with
+ * CUDA events on the context's stream.  kind: 0 cell chain, 1 L1->L11
+ * accumulation, 2 routing, 3 everything between the first and last launch of
+ * an mhm_run.  Timing is off unless enabled (it adds event records). */
+int mhm_set_timing(mhm_ctx *ctx, int32_t on);
+int mhm_get_timing(mhm_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
+
+/* Routing order of an L11 network (host computation, no device needed):
+ * replaces L11_routing_order (src/mRM/mo_mrm_net_startup.f90:728-886) with an
+ * O(nLinks x sweeps) algorithm giving the same ranks.  Inputs fromN/toN
+ * [n_nodes] (1-based, links 1..n_nodes-n_outlets valid); outputs net_perm and
+ * r_order [n_nodes] (entries past nLinks set to -9999 as in the reference). */
+int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n, const int32_t *to_n,
+                      int32_t *net_perm, int32_t *r_order);
+
+/* Calendar of model steps tt0 .. tt0+n-1 of a run starting at Julian day
+ * number jul_start (host computation): month (1-12), hour (0-23) and day of
+ * year, as do_time_step obtains them from dec2date(newTime - 0.5)
+ * (src/mHM/mo_mhm_interface_run.f90:355-363, src/common/
+ * mo_common_datetime_type.f90:71-125).  Any output pointer may be NULL. */
+int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t n, int32_t *month,
+                      int32_t *hour, int32_t *doy);
+
+/* Pinned host memory for forcing and outputs. */
+int mhm_host_alloc(size_t bytes, void **ptr);
+int mhm_host_free(void *ptr);
+
+/* Build information: sm arch, number of kernels launched so far. */
+int mhm_version(int32_t *major, int32_t *minor);
+int64_t mhm_kernel_launch_count(void);
+
+/* Elementary-function check: evaluates hmath log/exp/pow of n inputs on the
+ * device (where == 1) or the host (where == 0): op 0 log(x), 1 exp(x),
+ * 2 pow(x, y).  Used by the tests to show host and device bit-equality. */
+int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const double *y, double *out);
+
+/* FP64 issue-rate probe: dependent DFMA chains on every SM for `iters`
+ * iterations; returns achieved FP64 FLOP/s (2 per DFMA) in *flops. */
+int mhm_probe_fp64(int64_t iters, double *flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

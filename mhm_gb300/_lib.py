@@ -1,0 +1,119 @@
+"""ctypes binding of libmhm_gpu.so (the C ABI of include/mhm_gpu.h).
+
+The library is built in-tree by mhm_gb300.build; loading fails loudly when it
+is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import build as _build
+
+MHM_OK = 0
+MHM_ERR_INVALID = -1
+MHM_ERR_CUDA = -2
+MHM_ERR_OOM = -3
+MHM_ERR_TIMEOUT = -4
+MHM_ERR_NAN = -5
+MHM_ERR_UNSUPPORTED = -6
+
+FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX = range(5)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class DomainDesc(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int32), ("n_horizons", C.c_int32), ("n_nodes", C.c_int32),
+        ("n_outlets", C.c_int32), ("timestep", C.c_int32), ("proc_soilmoist", C.c_int32),
+        ("proc_pet", C.c_int32), ("proc_routing", C.c_int32), ("n_tstep_forcing_day", C.c_int32),
+        ("jul_start", C.c_int32), ("map_flag", C.c_int32), ("n_gauges", C.c_int32),
+        ("n_members", C.c_int32), ("read_states", C.c_int32),
+        ("evap_coeff", _dp), ("fday_prec", _dp), ("fnight_prec", _dp), ("fday_pet", _dp),
+        ("fnight_pet", _dp), ("fday_temp", _dp), ("fnight_temp", _dp),
+        ("l1_area_km2", _dp), ("l1_l11_id", _ip), ("l11_area_km2", _dp), ("l11_l1_id", _ip),
+        ("net_perm", _ip), ("from_n", _ip), ("to_n", _ip),
+        ("length", _dp), ("slope", _dp), ("ffp_imp", _dp), ("gauge_node", _ip), ("latitude", _dp),
+    ]
+
+
+EFF_PARAM_FIELDS = [
+    "fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "HarSamCoeff",
+    "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco",
+    "jarvis_thresh_c1", "tempThresh", "unsatThresh", "sealedThresh",
+    "maxInter", "petLAIcorFactor",
+    "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp",
+]
+
+
+class EffParams(C.Structure):
+    _fields_ = [(n, _dp) for n in EFF_PARAM_FIELDS]
+
+
+RESTART_FIELDS = ["interc", "snowpack", "sealSTW", "unsatSTW", "satSTW", "soilMoist",
+                  "qOUT", "Qmod", "qTIN", "qTR", "C1", "C2"]
+
+
+class Restart(C.Structure):
+    _fields_ = [(n, _dp) for n in RESTART_FIELDS]
+
+
+EXPORTS = [
+    "mhm_ctx_create", "mhm_ctx_destroy", "mhm_last_error", "mhm_ctx_stream", "mhm_set_eff_params",
+    "mhm_set_routing_params", "mhm_init_states", "mhm_set_forcing", "mhm_run", "mhm_enable_outputs",
+    "mhm_get_outputs", "mhm_get_state", "mhm_set_state", "mhm_get_var", "mhm_set_timing",
+    "mhm_get_timing", "mhm_host_alloc", "mhm_host_free", "mhm_version", "mhm_kernel_launch_count",
+    "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar",
+]
+
+_LIB = None
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load libmhm_gpu.so (building it first if needed); raises if unavailable."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build_if_missing and (not path.exists() or _build._stale()):
+        _build.build()
+    if not path.exists():
+        raise RuntimeError(f"libmhm_gpu.so not found at {path}: run mhm_gb300.build.build()")
+    L = C.CDLL(str(path), mode=os.RTLD_NOW | getattr(os, "RTLD_GLOBAL", 0))
+    vp = C.c_void_p
+    L.mhm_ctx_create.argtypes = [C.POINTER(DomainDesc), C.c_int32, C.POINTER(vp)]
+    L.mhm_ctx_destroy.argtypes = [vp]
+    L.mhm_last_error.argtypes = [vp]
+    L.mhm_last_error.restype = C.c_char_p
+    L.mhm_ctx_stream.argtypes = [vp]
+    L.mhm_ctx_stream.restype = vp
+    L.mhm_set_eff_params.argtypes = [vp, C.c_int32, C.POINTER(EffParams)]
+    L.mhm_set_routing_params.argtypes = [vp, C.c_int32, _dp]
+    L.mhm_init_states.argtypes = [vp, C.c_int32, _dp]
+    L.mhm_set_forcing.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
+    L.mhm_run.argtypes = [vp, C.c_int32, C.c_int32, _dp]
+    L.mhm_enable_outputs.argtypes = [vp, C.c_int32, C.c_int32]
+    L.mhm_get_outputs.argtypes = [vp, _dp, _dp]
+    L.mhm_get_state.argtypes = [vp, C.c_int32, C.POINTER(Restart)]
+    L.mhm_set_state.argtypes = [vp, C.c_int32, C.POINTER(Restart)]
+    L.mhm_get_var.argtypes = [vp, C.c_int32, C.c_char_p, _dp]
+    L.mhm_set_timing.argtypes = [vp, C.c_int32]
+    L.mhm_get_timing.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.mhm_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+    L.mhm_host_free.argtypes = [vp]
+    L.mhm_version.argtypes = [_ip, _ip]
+    L.mhm_kernel_launch_count.argtypes = []
+    L.mhm_kernel_launch_count.restype = C.c_int64
+    L.mhm_hmath_eval.argtypes = [C.c_int32, C.c_int32, C.c_int64, _dp, _dp, _dp]
+    L.mhm_probe_fp64.argtypes = [C.c_int64, C.POINTER(C.c_double)]
+    L.mhm_routing_order.argtypes = [C.c_int32, C.c_int32, _ip, _ip, _ip, _ip]
+    L.mhm_step_calendar.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip, _ip, _ip]
+    _LIB = L
+    return L

@@ -1,0 +1,362 @@
+// cell_chain.cu -- the mHM L1 cell chain as one time-looping kernel.
+//
+// One thread advances one (member, cell) through a chunk of time steps with
+// all states and effective parameters in registers; forcing is read once per
+// step as coalesced [step][cell] rows and the step's total runoff is written
+// as a coalesced [step][member][cell] row.  The arithmetic of every step is
+// the reference's, in the reference's order (compiled with --fmad=false;
+// log/exp/pow from hmath.h), so a step here equals a step of
+//   mHM() cell loop              src/mHM/mo_mhm.f90:458-517
+//   get_corrected_pet/temp/prec  src/meteo/mo_meteo_handler.f90:915-1285
+// bit for bit.  Expressions that depend on parameters only (c2TSTu/k, the
+// degree-day threshold, FC-PW, ...) are evaluated once per chunk: the same
+// operands give the same bits as the reference's per-step evaluation.
+#include <cfloat>
+#include <cmath>
+
+#include "hmath.h"
+#include "mhm_kernels.cuh"
+
+namespace mhm {
+
+namespace {
+
+constexpr double kEps = DBL_EPSILON; // src/common/mo_common_constants.f90:25
+constexpr double kTwoThird = 2.0 / 3.0;
+constexpr double kPiD = 3.141592653589793238462643383279502884197;
+constexpr double kTwoPiD = 6.283185307179586476925286766559005768394;
+constexpr double kDaySecs = 86400.0, kYearDays = 365.0, kSolarConst = 1367.0, kSpecHeatET = 2.45e06;
+constexpr double kDeg2Rad = 3.141592653589793238462643383279502884197 / 180.0;
+constexpr double kHarSamConst = 17.800;
+
+// src/mHM/mo_pet.f90:314-355 (CUDA's sin/cos/tan/acos; only the daily-forcing
+// Hargreaves variant uses it)
+__device__ double extraterr_rad_approx(int doy, double latitude)
+{
+    double dr = 1.0 + 0.0330 * cos(kTwoPiD * doy / kYearDays);
+    double delta = 0.4090 * sin(kTwoPiD * doy / kYearDays - 1.3900);
+    double arg = -tan(latitude) * tan(delta);
+    if (arg < -1.0) arg = -1.0;
+    if (arg > 1.0) arg = 1.0;
+    double omega = acos(arg);
+    return kDaySecs / kPiD / kSpecHeatET * kSolarConst * dr *
+           (omega * sin(latitude) * sin(delta) + cos(latitude) * cos(delta) * sin(omega));
+}
+
+// FORCES mo_utils LE (in-tree copy pre-proc/mtCLIM/mo_utils.f90 lesserequal_dp)
+__device__ __forceinline__ bool le_dp(double a, double b)
+{
+    return !(((kEps * fabs(b) - fabs(a - b)) < 0.0) && (a > b));
+}
+
+// src/mHM/mo_pet.f90:73-116
+__device__ double pet_hargreaves(double coeff, double tavg, double tmax, double tmin, double rad)
+{
+    double delta_temp = tmax - tmin;
+    if (le_dp(delta_temp, 0.0) || le_dp(tavg, -kHarSamConst)) return 0.0;
+    return coeff * rad * (tavg + kHarSamConst) * sqrt(delta_temp);
+}
+
+template <int H>
+struct CellRegs {
+    // states
+    double interc, snow, seal, unsat, sat, sm[H];
+    // parameters (and parameter-only derived values)
+    double fsealed, one_minus_fsealed_unused;
+    double ddinc, ddmax_s, ddnopre_s, dd_thr;
+    double tthresh, sthresh, uthresh, karst, alpha1;
+    double k0s, k1s, k2s, kps; // c2TSTu / k
+    double jarvis;
+    double fasp, harsam, lat_rad;
+    double sms[H], froots[H], fc[H], pw[H], beta[H], fc_pw[H], sat_pw[H];
+};
+
+} // namespace
+
+template <int H>
+__global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = a.n_cells;
+    if (gid >= N * a.n_members) return;
+    const int m = (int)(gid / N);
+    const int k = (int)(gid - (int64_t)m * N);
+    const int np = n_param_planes(H);
+    const int ns = n_state_planes(H);
+    const double *P = a.params + (size_t)m * np * N + k;
+    double *S = a.states + (size_t)m * ns * N + k;
+    auto par = [&](int plane) { return __ldg(P + (size_t)plane * N); };
+
+    CellRegs<H> c;
+    const double c2 = a.c2TSTu;
+    c.fsealed = par(P_FSEALED);
+    c.ddinc = par(P_DDINC);
+    c.ddmax_s = par(P_DDMAX) * c2;   // mo_mhm.f90:463
+    c.ddnopre_s = par(P_DDNOPRE) * c2; // mo_mhm.f90:464
+    c.dd_thr = (c.ddmax_s - c.ddnopre_s) / c.ddinc; // mo_snow_accum_melt.f90:137
+    c.tthresh = par(P_TTHRESH);
+    c.sthresh = par(P_STHRESH);
+    c.uthresh = par(P_UTHRESH);
+    c.karst = par(P_KARST);
+    c.alpha1 = 1.0 + par(P_ALPHA); // mo_runoff.f90:139
+    c.k1s = c2 / par(P_K1);        // mo_mhm.f90:484
+    c.kps = c2 / par(P_KP);
+    c.k0s = c2 / par(P_K0);
+    c.k2s = c2 / par(P_K2);        // mo_mhm.f90:488
+    c.jarvis = par(P_JARVIS);
+    c.fasp = par(P_FASP);
+    c.harsam = par(P_HARSAM);
+    c.lat_rad = (a.proc_pet == 1) ? kDeg2Rad * __ldg(a.latitude + k) : 0.0;
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+        c.froots[h] = par(P_HORIZON + h);
+        c.sms[h] = par(P_HORIZON + H + h);
+        c.fc[h] = par(P_HORIZON + 2 * H + h);
+        c.pw[h] = par(P_HORIZON + 3 * H + h);
+        c.beta[h] = par(P_HORIZON + 4 * H + h);
+        c.fc_pw[h] = c.fc[h] - c.pw[h];   // feddes denominator, mo_soil_moisture.f90:358
+        c.sat_pw[h] = c.sms[h] - c.pw[h]; // jarvis denominator, mo_soil_moisture.f90:435
+    }
+    c.interc = S[(size_t)S_INTERC * N];
+    c.snow = S[(size_t)S_SNOW * N];
+    c.seal = S[(size_t)S_SEAL * N];
+    c.unsat = S[(size_t)S_UNSAT * N];
+    c.sat = S[(size_t)S_SAT * N];
+#pragma unroll
+    for (int h = 0; h < H; ++h) c.sm[h] = a.reset_sm ? 0.5 * c.fc[h] : S[(size_t)(S_SM + h) * N];
+
+    const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
+    int cur_month = -1;
+    double imax = 0.0, petlai = 0.0;
+    int cur_doy = -1;
+    double rad = 0.0;
+    const size_t out_stride = (size_t)a.n_members * N;
+    double *tro = a.tro + (size_t)m * N + k;
+
+    for (int t = 0; t < a.n_steps; ++t) {
+        const StepInfo si = a.steps[t];
+        const int month = si.month;
+        if (month != cur_month) { // iLAI = month (LUT-based LAI)
+            cur_month = month;
+            imax = par(P_MAXINTER + month - 1);
+            if (a.proc_pet == -1) petlai = par(P_PETLAI + month - 1);
+        }
+        const size_t f = (size_t)(si.row - a.row_base) * N + k;
+        // ---- meteo for the step (mo_meteo_handler.f90:915-1285) ----
+        double pv;
+        if (a.proc_pet == 0) {
+            pv = c.fasp * __ldg(a.pet + f);
+        } else if (a.proc_pet == -1) {
+            pv = petlai * __ldg(a.pet + f);
+        } else {
+            if (si.doy != cur_doy) {
+                cur_doy = si.doy;
+                rad = extraterr_rad_approx(cur_doy, c.lat_rad);
+            }
+            pv = c.fasp * pet_hargreaves(c.harsam, __ldg(a.temp + f), __ldg(a.tmax + f), __ldg(a.tmin + f), rad);
+        }
+        double pet, temp, prec;
+        if (a.is_hourly) {
+            pet = pv;
+            temp = __ldg(a.temp + f);
+            prec = __ldg(a.pre + f);
+        } else { // temporal_disagg_*_daynight, mo_meteo_temporal_tools.f90:66-161
+            const int mi = month - 1;
+            const double nd = a.nTstepDay;
+            if (nd > 1.0) {
+                pet = 2.0 * pv * (si.isday ? a.tab.fday_pet[mi] : a.tab.fnight_pet[mi]) / nd;
+                temp = __ldg(a.temp + f) + (si.isday ? a.tab.fday_temp[mi] : a.tab.fnight_temp[mi]);
+                prec = 2.0 * __ldg(a.pre + f) * (si.isday ? a.tab.fday_prec[mi] : a.tab.fnight_prec[mi]) / nd;
+            } else {
+                pet = pv;
+                temp = __ldg(a.temp + f);
+                prec = __ldg(a.pre + f);
+            }
+        }
+
+        // ---- canopy_interc, mo_canopy_interc.f90:75-133 ----
+        double throughfall, aet_can;
+        {
+            double aux = c.interc + prec;
+            if (aux >= imax) {
+                throughfall = aux - imax;
+                c.interc = imax;
+            } else {
+                throughfall = 0.0;
+                c.interc = aux;
+            }
+            aet_can = (imax > kEps) ? pet * hm_pow(c.interc / imax, kTwoThird) : 0.0;
+            if (aet_can < 0.0) aet_can = 0.0;
+            if (c.interc > aet_can) {
+                c.interc = c.interc - aet_can;
+            } else {
+                aet_can = c.interc;
+                c.interc = 0.0;
+            }
+        }
+        // ---- snow_accum_melt, mo_snow_accum_melt.f90:70-158 ----
+        double prec_effect;
+        {
+            const bool warm = temp > c.tthresh;
+            double rain = warm ? throughfall : 0.0;
+            double snowf = warm ? 0.0 : throughfall;
+            double dd = (prec <= c.dd_thr) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
+            double melt;
+            if (warm) {
+                if (c.snow > 0.0) {
+                    double aux = dd * (temp - c.tthresh);
+                    if (aux > c.snow) {
+                        melt = c.snow;
+                        c.snow = 0.0;
+                    } else {
+                        melt = aux;
+                        c.snow = c.snow - aux;
+                    }
+                } else {
+                    melt = 0.0;
+                    c.snow = 0.0;
+                }
+            } else {
+                melt = 0.0;
+                c.snow = c.snow + snowf;
+            }
+            prec_effect = melt + rain;
+        }
+        // ---- soil_moisture, mo_soil_moisture.f90:176-286 ----
+        double runoff_sealed = 0.0;
+        double infil_last;
+        {
+            if (c.fsealed > 0.0) {
+                double tmp = c.seal + prec_effect;
+                if (tmp > c.sthresh) {
+                    runoff_sealed = tmp - c.sthresh;
+                    c.seal = c.sthresh;
+                } else {
+                    runoff_sealed = 0.0;
+                    c.seal = tmp;
+                }
+                double aet_sealed;
+                if (c.sthresh > kEps) {
+                    aet_sealed = (pet / a.tab.evap[month - 1] - aet_can) * (c.seal / c.sthresh);
+                    if (aet_sealed < 0.0) aet_sealed = 0.0;
+                } else {
+                    aet_sealed = DBL_MAX;
+                }
+                if (c.seal > aet_sealed) {
+                    c.seal = c.seal - aet_sealed;
+                } else {
+                    c.seal = 0.0;
+                }
+            }
+            double infil = prec_effect; // prec_effec_soil of horizon 1
+            double aet_above = 0.0;     // masked running sum of positive aet above
+            const double demand = pet - aet_can;
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+                const double pin = infil;
+                double smh = c.sm[h];
+                if (smh > c.sms[h]) {
+                    infil = pin;
+                } else {
+                    double frac_runoff = (smh > kEps) ? hm_exp(c.beta[h] * hm_log(smh / c.sms[h])) : 0.0;
+                    double tmp = pin * (1.0 - frac_runoff);
+                    if ((smh + tmp) > c.sms[h]) {
+                        infil = pin + (smh - c.sms[h]);
+                        smh = c.sms[h];
+                    } else {
+                        infil = pin - tmp;
+                        smh = smh + tmp;
+                    }
+                }
+                double aet = demand;
+                if (h != 0) aet = aet - aet_above;
+                double stress;
+                if (feddes) {
+                    if (smh >= c.fc[h]) stress = c.froots[h];
+                    else if (smh > c.pw[h]) stress = c.froots[h] * (smh - c.pw[h]) / c.fc_pw[h];
+                    else stress = 0.0;
+                } else {
+                    double th = (smh - c.pw[h]) / c.sat_pw[h];
+                    if (th < 0.0) th = 0.0;
+                    if (th > 1.0) th = 1.0;
+                    if (th >= c.jarvis) stress = c.froots[h];
+                    else if (th < c.jarvis) stress = c.froots[h] * (th / c.jarvis);
+                    else stress = 0.0;
+                }
+                aet = aet * stress;
+                if (aet < 0.0) aet = 0.0;
+                if (smh > aet) {
+                    smh = smh - aet;
+                } else {
+                    aet = smh - kEps;
+                    smh = kEps;
+                }
+                if (smh < kEps) smh = kEps;
+                c.sm[h] = smh;
+                if (aet > 0.0) aet_above = aet_above + aet;
+            }
+            infil_last = infil;
+        }
+        // ---- runoff_unsat_zone, mo_runoff.f90:74-154 ----
+        double fast = 0.0, slow = 0.0, base;
+        {
+            c.unsat = c.unsat + infil_last;
+            if (c.unsat > c.uthresh) {
+                double x = c.k0s * (c.unsat - c.uthresh);
+                double y = c.unsat - kEps;
+                fast = (x < y) ? x : y;
+            }
+            c.unsat = c.unsat - fast;
+            if (c.unsat > kEps) {
+                double x = c.k1s * hm_pow(c.unsat, c.alpha1);
+                double y = c.unsat - kEps;
+                slow = (x < y) ? x : y;
+            }
+            c.unsat = c.unsat - slow;
+            double perc = c.kps * c.unsat;
+            if (c.unsat > perc) {
+                c.unsat = c.unsat - perc;
+                c.sat = c.sat + perc * c.karst;
+            } else {
+                c.sat = c.sat + c.unsat * c.karst;
+                c.unsat = 0.0;
+            }
+        }
+        // ---- runoff_sat_zone, mo_runoff.f90:191-212 ----
+        if (c.sat > 0.0) {
+            base = c.k2s * c.sat;
+            c.sat = c.sat - base;
+        } else {
+            base = 0.0;
+            c.sat = 0.0;
+        }
+        // ---- L1_total_runoff, mo_runoff.f90:248-274 ----
+        tro[(size_t)t * out_stride] = ((base + slow + fast) * (1.0 - c.fsealed)) + (runoff_sealed * c.fsealed);
+    }
+
+    S[(size_t)S_INTERC * N] = c.interc;
+    S[(size_t)S_SNOW * N] = c.snow;
+    S[(size_t)S_SEAL * N] = c.seal;
+    S[(size_t)S_UNSAT * N] = c.unsat;
+    S[(size_t)S_SAT * N] = c.sat;
+#pragma unroll
+    for (int h = 0; h < H; ++h) S[(size_t)(S_SM + h) * N] = c.sm[h];
+}
+
+// Host-side launcher: H is a template parameter so the horizon arrays stay in registers.
+cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_cells * a.n_members;
+    const int block = 128;
+    const unsigned grid = (unsigned)((n + block - 1) / block);
+    switch (H) {
+#define MHM_CASE(HH) \
+    case HH: cell_chain_kernel<HH><<<grid, block, 0, s>>>(a); break;
+        MHM_CASE(1) MHM_CASE(2) MHM_CASE(3) MHM_CASE(4) MHM_CASE(5) MHM_CASE(6) MHM_CASE(7) MHM_CASE(8)
+#undef MHM_CASE
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+} // namespace mhm

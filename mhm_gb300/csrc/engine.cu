@@ -1,0 +1,954 @@
+// engine.cu -- the C ABI of include/mhm_gpu.h: context, device memory, the
+// chunked time loop (cell chain -> L1->L11 accumulation -> level routing) and
+// state/variable access.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hmath.h"
+#include "mhm_gpu.h"
+#include "mhm_kernels.cuh"
+#include "network.h"
+
+namespace mhm {
+cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s);
+cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
+cudaError_t launch_route_level(const RouteArgs &a, cudaStream_t s);
+cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
+cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double TS, const double *length,
+                            const double *slope, const double *ffp, const int32_t *link_pos, double *C1,
+                            double *C2, cudaStream_t s);
+cudaError_t launch_hmath_eval(int op, int64_t n, const double *x, const double *y, double *out, cudaStream_t s);
+cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *sink, cudaStream_t s);
+} // namespace mhm
+
+using namespace mhm;
+
+namespace {
+
+std::atomic<int64_t> g_launches{0};
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t ensure(size_t count)
+    {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        n = count;
+        return cudaSuccess;
+    }
+};
+
+struct TimedLaunch {
+    int kind;
+    cudaEvent_t a, b;
+};
+
+struct ForcingSrc {
+    const double *ptr = nullptr;
+    int32_t row0 = 0, n_rows = 0, on_device = 0;
+    bool set = false;
+};
+
+} // namespace
+
+struct mhm_ctx {
+    // domain
+    int32_t N = 0, H = 0, L = 0, n_out = 0, n_links = 0, M = 1, G = 0;
+    int32_t timestep = 1, proc_sm = 1, proc_pet = 0, proc_rout = 1, ntfd = 24, jul_start = 0, map_flag = 1;
+    int32_t read_states = 0;
+    int device = 0;
+    MonthTables tab{};
+    double ss_max = 0.0;
+    LevelNetwork net;
+    std::vector<int32_t> gauge_pos;
+    // device: static
+    DevBuf<double> params, states, latitude, l1_area, pos_area, length, slope, ffp, rout_p5;
+    DevBuf<double> C1, C2, qtin1, qtr1, qout_last, qmod_last;
+    DevBuf<int32_t> node_cell_ptr, node_cells, pos_l11_l1, up_ptr, up_pos, link_pos, gauge_pos_d;
+    DevBuf<int8_t> pos_flags;
+    // device: per run / chunk
+    DevBuf<StepInfo> steps;
+    DevBuf<double> tro, qout, qtr, qmod, q_gauge;
+    DevBuf<double> stage[5][2];
+    // forcing
+    ForcingSrc forc[5];
+    // outputs
+    int32_t out_tro = 0, out_qmod = 0;
+    std::vector<double> host_tro, host_qmod;
+    int32_t last_steps = 0;
+    // execution
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
+    bool timing = false;
+    std::vector<TimedLaunch> pending;
+    int64_t t_launches[4] = {0, 0, 0, 0};
+    double t_ms[4] = {0, 0, 0, 0};
+    size_t chunk_bytes = (size_t)8 << 30;
+    std::string err;
+};
+
+namespace {
+
+int fail(mhm_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(mhm_ctx *c, cudaError_t e, const char *what)
+{
+    int code = (e == cudaErrorMemoryAllocation) ? MHM_ERR_OOM : MHM_ERR_CUDA;
+    return fail(c, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                                                                             \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what);                                                    \
+    } while (0)
+
+template <class T>
+cudaError_t upload(DevBuf<T> &b, const T *host, size_t n, cudaStream_t s)
+{
+    cudaError_t e = b.ensure(n);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    return cudaMemcpyAsync(b.p, host, n * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+// Timed launch bracket: events recorded on the launching stream.
+struct Bracket {
+    mhm_ctx *c;
+    int kind;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Bracket(mhm_ctx *cc, int k) : c(cc), kind(k)
+    {
+        if (c->timing) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    void done()
+    {
+        if (c->timing) {
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({kind, a, b});
+        }
+    }
+};
+
+void harvest_timing(mhm_ctx *c)
+{
+    for (auto &t : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+            c->t_ms[t.kind] += ms;
+            c->t_launches[t.kind] += 1;
+        }
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    c->pending.clear();
+}
+
+} // namespace
+
+extern "C" {
+
+int mhm_version(int32_t *major, int32_t *minor)
+{
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+    return MHM_OK;
+}
+
+int64_t mhm_kernel_launch_count(void) { return g_launches.load(); }
+
+const char *mhm_last_error(const mhm_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void *mhm_ctx_stream(mhm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
+{
+    if (!d || !out) return MHM_ERR_INVALID;
+    *out = nullptr;
+    mhm_ctx *ctx = new mhm_ctx();
+    auto bad = [&](const std::string &m) {
+        std::string msg = m;
+        delete ctx;
+        std::fprintf(stderr, "mhm_ctx_create: %s\n", msg.c_str());
+        return MHM_ERR_INVALID;
+    };
+    if (d->n_cells < 1) return bad("n_cells < 1");
+    if (d->n_horizons < 1 || d->n_horizons > kMaxHorizons) return bad("n_horizons must be 1..8");
+    if (d->n_members < 1) return bad("n_members < 1");
+    if (d->timestep < 1 || 24 % d->timestep != 0) return bad("timestep must divide 24 hours");
+    if (d->proc_soilmoist < 1 || d->proc_soilmoist > 4) return bad("proc_soilmoist must be 1..4");
+    if (d->proc_pet < -1 || d->proc_pet > 1) return bad("proc_pet must be -1, 0 or 1 (2, 3 unsupported)");
+    if (d->proc_routing != 0 && d->proc_routing != 1) return bad("proc_routing must be 0 or 1");
+    if (d->n_tstep_forcing_day != 24 && d->n_tstep_forcing_day != 1)
+        return bad("n_tstep_forcing_day must be 24 or 1");
+    if (d->jul_start < 2299161) return bad("jul_start before the Gregorian reform is not supported");
+    if (!d->evap_coeff) return bad("evap_coeff missing");
+    if (d->n_tstep_forcing_day == 1 && (!d->fday_prec || !d->fnight_prec || !d->fday_pet || !d->fnight_pet ||
+                                        !d->fday_temp || !d->fnight_temp))
+        return bad("day/night ratios missing for daily forcing");
+    if (d->proc_pet == 1 && !d->latitude) return bad("latitude missing for Hargreaves PET");
+    ctx->N = d->n_cells;
+    ctx->H = d->n_horizons;
+    ctx->M = d->n_members;
+    ctx->timestep = d->timestep;
+    ctx->proc_sm = d->proc_soilmoist;
+    ctx->proc_pet = d->proc_pet;
+    ctx->proc_rout = d->proc_routing;
+    ctx->ntfd = d->n_tstep_forcing_day;
+    ctx->jul_start = d->jul_start;
+    ctx->map_flag = d->map_flag;
+    ctx->read_states = d->read_states;
+    for (int i = 0; i < 12; ++i) {
+        ctx->tab.evap[i] = d->evap_coeff[i];
+        if (d->n_tstep_forcing_day == 1) {
+            ctx->tab.fday_prec[i] = d->fday_prec[i];
+            ctx->tab.fnight_prec[i] = d->fnight_prec[i];
+            ctx->tab.fday_pet[i] = d->fday_pet[i];
+            ctx->tab.fnight_pet[i] = d->fnight_pet[i];
+            ctx->tab.fday_temp[i] = d->fday_temp[i];
+            ctx->tab.fnight_temp[i] = d->fnight_temp[i];
+        }
+    }
+    if (ctx->proc_rout == 1) {
+        if (d->n_nodes < 1 || !d->l1_l11_id || !d->net_perm || !d->from_n || !d->to_n)
+            return bad("routing arrays missing");
+        if (!d->map_flag && (!d->l11_l1_id || !d->l11_area_km2)) return bad("L11_L1_Id/areas missing");
+        if (d->map_flag && !d->l1_area_km2) return bad("L1 cell areas missing");
+        ctx->L = d->n_nodes;
+        ctx->n_out = d->n_outlets;
+        std::string err;
+        if (ctx->L > 1) {
+            if (!build_level_network(d->n_nodes, d->n_outlets, d->net_perm, d->from_n, d->to_n, ctx->net, err))
+                return bad(err);
+        } else {
+            ctx->net = LevelNetwork{};
+            ctx->net.n_nodes = 1;
+            ctx->net.n_levels = 1;
+            ctx->net.level_ptr = {0, 1};
+            ctx->net.pos_of_node = {0};
+            ctx->net.node_of_pos = {0};
+            ctx->net.up_ptr = {0, 0};
+            ctx->net.pos_flags = {2}; // Qmod = qOUT for a single node
+        }
+        ctx->n_links = ctx->net.n_links;
+        if (ctx->n_links > 0 && (!d->length || !d->slope || !d->ffp_imp)) return bad("link length/slope/fFPimp missing");
+        ctx->G = d->n_gauges;
+        if (ctx->G < 0 || (ctx->G > 0 && !d->gauge_node)) return bad("gauges");
+        for (int g = 0; g < ctx->G; ++g) {
+            int v = d->gauge_node[g] - 1;
+            if (v < 0 || v >= ctx->L) return bad("gauge node out of range");
+            ctx->gauge_pos.push_back(ctx->net.pos_of_node[v]);
+        }
+        for (int k = 0; k < ctx->N; ++k)
+            if (d->l1_l11_id[k] < 1 || d->l1_l11_id[k] > ctx->L) return bad("L1_L11_Id out of range");
+        if (!d->map_flag)
+            for (int i = 0; i < ctx->L; ++i)
+                if (d->l11_l1_id[i] < 1 || d->l11_l1_id[i] > ctx->N) return bad("L11_L1_Id out of range");
+    }
+    // device
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        delete ctx;
+        std::fprintf(stderr, "mhm_ctx_create: no CUDA device (%s)\n", cudaGetErrorString(e));
+        return MHM_ERR_CUDA;
+    }
+    if (device >= 0) {
+        if (device >= ndev) return bad("device index out of range");
+        cudaSetDevice(device);
+    }
+    cudaGetDevice(&ctx->device);
+    auto ck = [&](cudaError_t ee, const char *w) {
+        if (ee != cudaSuccess) {
+            std::fprintf(stderr, "mhm_ctx_create: %s: %s\n", w, cudaGetErrorString(ee));
+            return false;
+        }
+        return true;
+    };
+    if (!ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream") ||
+        !ck(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream")) {
+        mhm_ctx_destroy(ctx);
+        return MHM_ERR_CUDA;
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaEventCreateWithFlags(&ctx->ev_copied[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ctx->ev_consumed[i], cudaEventDisableTiming);
+    }
+    const size_t N = ctx->N, M = ctx->M, H = ctx->H, L = ctx->L;
+    bool ok = true;
+    ok = ok && ck(ctx->params.ensure(M * n_param_planes((int)H) * N), "params");
+    ok = ok && ck(ctx->states.ensure(M * n_state_planes((int)H) * N), "states");
+    if (ok) {
+        cudaMemsetAsync(ctx->params.p, 0, ctx->params.n * sizeof(double), ctx->stream);
+        cudaMemsetAsync(ctx->states.p, 0, ctx->states.n * sizeof(double), ctx->stream);
+    }
+    if (ok && ctx->proc_pet == 1) ok = ck(upload(ctx->latitude, d->latitude, N, ctx->stream), "latitude");
+    if (ok && ctx->proc_rout == 1) {
+        const LevelNetwork &net = ctx->net;
+        // L1 cells of each node in ascending cell order, by position
+        std::vector<int32_t> cnt(L + 1, 0), cells(N);
+        for (size_t k = 0; k < N; ++k) cnt[net.pos_of_node[d->l1_l11_id[k] - 1] + 1]++;
+        for (size_t p = 0; p < L; ++p) cnt[p + 1] += cnt[p];
+        std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+        for (size_t k = 0; k < N; ++k) cells[fill[net.pos_of_node[d->l1_l11_id[k] - 1]]++] = (int32_t)k;
+        std::vector<int32_t> pl1(L, 0);
+        std::vector<double> parea(L, 0.0);
+        for (size_t p = 0; p < L; ++p) {
+            int v = net.node_of_pos[p];
+            if (!d->map_flag) pl1[p] = d->l11_l1_id[v] - 1;
+            parea[p] = d->l11_area_km2 ? d->l11_area_km2[v] : 0.0;
+        }
+        ok = ok && ck(upload(ctx->node_cell_ptr, cnt.data(), L + 1, ctx->stream), "cell ptr");
+        ok = ok && ck(upload(ctx->node_cells, cells.data(), N, ctx->stream), "cells");
+        ok = ok && ck(upload(ctx->pos_l11_l1, pl1.data(), L, ctx->stream), "l11_l1");
+        ok = ok && ck(upload(ctx->pos_area, parea.data(), L, ctx->stream), "l11 area");
+        if (d->map_flag) ok = ok && ck(upload(ctx->l1_area, d->l1_area_km2, N, ctx->stream), "l1 area");
+        ok = ok && ck(upload(ctx->up_ptr, net.up_ptr.data(), L + 1, ctx->stream), "up ptr");
+        ok = ok && ck(upload(ctx->up_pos, net.up_pos.data(), net.up_pos.size(), ctx->stream), "up pos");
+        ok = ok && ck(upload(ctx->pos_flags, net.pos_flags.data(), L, ctx->stream), "flags");
+        ok = ok && ck(upload(ctx->link_pos, net.link_pos.data(), net.link_pos.size(), ctx->stream), "link pos");
+        ok = ok && ck(upload(ctx->gauge_pos_d, ctx->gauge_pos.data(), ctx->gauge_pos.size(), ctx->stream), "gauges");
+        if (ctx->n_links > 0) {
+            ok = ok && ck(upload(ctx->length, d->length, ctx->n_links, ctx->stream), "length");
+            ok = ok && ck(upload(ctx->slope, d->slope, ctx->n_links, ctx->stream), "slope");
+            ok = ok && ck(upload(ctx->ffp, d->ffp_imp, ctx->n_links, ctx->stream), "ffp");
+            double mx = -HUGE_VAL;
+            for (int i = 0; i < ctx->n_links; ++i) mx = std::max(mx, d->slope[i]);
+            ctx->ss_max = mx;
+        }
+        ok = ok && ck(ctx->rout_p5.ensure(5 * M), "p5");
+        for (auto *b : {&ctx->C1, &ctx->C2, &ctx->qtin1, &ctx->qtr1, &ctx->qout_last, &ctx->qmod_last}) {
+            ok = ok && ck(b->ensure(M * L), "routing state");
+            if (ok) cudaMemsetAsync(b->p, 0, M * L * sizeof(double), ctx->stream);
+        }
+    }
+    if (ok) ok = ck(cudaStreamSynchronize(ctx->stream), "init sync");
+    if (!ok) {
+        mhm_ctx_destroy(ctx);
+        return MHM_ERR_OOM;
+    }
+    if (const char *s = std::getenv("MHM_CHUNK_BYTES")) ctx->chunk_bytes = (size_t)std::atoll(s);
+    *out = ctx;
+    return MHM_OK;
+}
+
+int mhm_ctx_destroy(mhm_ctx *ctx)
+{
+    if (!ctx) return MHM_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    harvest_timing(ctx);
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->ev_copied[i]) cudaEventDestroy(ctx->ev_copied[i]);
+        if (ctx->ev_consumed[i]) cudaEventDestroy(ctx->ev_consumed[i]);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    delete ctx;
+    return MHM_OK;
+}
+
+int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
+{
+    if (!ctx || !p) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const size_t N = ctx->N;
+    const int H = ctx->H, np = n_param_planes(H);
+    const double *scalars[16] = {p->fSealed,   p->alpha,     p->degDayInc, p->degDayMax,   p->degDayNoPre,
+                                 p->fAsp,      p->HarSamCoeff, p->karstLoss, p->kFastFlow, p->kSlowFlow,
+                                 p->kBaseFlow, p->kPerco,    p->jarvis_thresh_c1, p->tempThresh, p->unsatThresh,
+                                 p->sealedThresh};
+    double *base = ctx->params.p + (size_t)m * np * N;
+    for (int i = 0; i < 16; ++i) {
+        if (!scalars[i]) {
+            if (i == P_HARSAM && ctx->proc_pet != 1) continue;
+            if (i == P_FASP && ctx->proc_pet == -1) continue;
+            if (i == P_JARVIS && (ctx->proc_sm == 1 || ctx->proc_sm == 4)) continue;
+            return fail(ctx, MHM_ERR_INVALID, "effective parameter " + std::to_string(i) + " missing");
+        }
+        CK(cudaMemcpyAsync(base + (size_t)i * N, scalars[i], N * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "params");
+    }
+    if (!p->maxInter) return fail(ctx, MHM_ERR_INVALID, "maxInter missing");
+    CK(cudaMemcpyAsync(base + (size_t)P_MAXINTER * N, p->maxInter, 12 * N * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->stream),
+       "maxInter");
+    if (ctx->proc_pet == -1) {
+        if (!p->petLAIcorFactor) return fail(ctx, MHM_ERR_INVALID, "petLAIcorFactor missing");
+        CK(cudaMemcpyAsync(base + (size_t)P_PETLAI * N, p->petLAIcorFactor, 12 * N * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "petLAI");
+    }
+    const double *hz[5] = {p->fRoots, p->soilMoistSat, p->soilMoistFC, p->wiltingPoint, p->soilMoistExp};
+    for (int g = 0; g < 5; ++g) {
+        if (!hz[g]) return fail(ctx, MHM_ERR_INVALID, "horizon parameter missing");
+        CK(cudaMemcpyAsync(base + (size_t)(P_HORIZON + g * H) * N, hz[g], (size_t)H * N * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "horizon params");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "params sync");
+    return MHM_OK;
+}
+
+int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
+{
+    if (!ctx || !p5) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
+    if (ctx->n_links == 0) return MHM_OK;
+    const size_t L = ctx->L;
+    CK(cudaMemcpyAsync(ctx->rout_p5.p + 5 * m, p5, 5 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "p5");
+    Bracket br(ctx, 2);
+    CK(launch_reg_rout(ctx->n_links, ctx->rout_p5.p + 5 * m, ctx->ss_max, (double)ctx->timestep, ctx->length.p,
+                       ctx->slope.p, ctx->ffp.p, ctx->link_pos.p, ctx->C1.p + m * L, ctx->C2.p + m * L,
+                       ctx->stream),
+       "reg_rout");
+    br.done();
+    g_launches++;
+    CK(cudaStreamSynchronize(ctx->stream), "reg_rout sync");
+    return MHM_OK;
+}
+
+int mhm_init_states(mhm_ctx *ctx, int32_t m, const double *hd)
+{
+    if (!ctx || !hd) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const size_t N = ctx->N;
+    const int H = ctx->H, ns = n_state_planes(H);
+    // mo_init_states.f90:258-345: interc 0, snow 15, sealed 0, unsat 10, sat 75,
+    // SM(h) = (depth(h) - depth(h-1)) * 0.25, last horizon to 1500 mm
+    std::vector<double> s((size_t)ns * N);
+    auto plane = [&](int pl, double v) { std::fill(s.begin() + (size_t)pl * N, s.begin() + (size_t)(pl + 1) * N, v); };
+    plane(S_INTERC, 0.0);
+    plane(S_SNOW, 15.0);
+    plane(S_SEAL, 0.0);
+    plane(S_UNSAT, 10.0);
+    plane(S_SAT, 75.0);
+    for (int h = 0; h < H - 1; ++h) plane(S_SM + h, (h == 0 ? hd[0] : hd[h] - hd[h - 1]) * 0.25);
+    plane(S_SM + H - 1, (1500.0 - (H >= 2 ? hd[H - 2] : 0.0)) * 0.25);
+    CK(cudaMemcpyAsync(ctx->states.p + (size_t)m * ns * N, s.data(), s.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->stream),
+       "states");
+    if (ctx->proc_rout == 1) {
+        const size_t L = ctx->L;
+        for (auto *b : {&ctx->qtin1, &ctx->qtr1, &ctx->qout_last, &ctx->qmod_last})
+            CK(cudaMemsetAsync(b->p + m * L, 0, L * sizeof(double), ctx->stream), "routing states");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "states sync");
+    return MHM_OK;
+}
+
+int mhm_set_forcing(mhm_ctx *ctx, int32_t kind, int32_t row0, int32_t n_rows, const double *data, int32_t on_device)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (kind < 0 || kind > 4) return fail(ctx, MHM_ERR_INVALID, "forcing kind");
+    if (row0 < 1 || n_rows < 1 || !data) return fail(ctx, MHM_ERR_INVALID, "forcing rows");
+    ForcingSrc &f = ctx->forc[kind];
+    f.ptr = data;
+    f.row0 = row0;
+    f.n_rows = n_rows;
+    f.on_device = on_device ? 1 : 0;
+    f.set = true;
+    return MHM_OK;
+}
+
+int mhm_enable_outputs(mhm_ctx *ctx, int32_t total_runoff, int32_t qmod)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    ctx->out_tro = total_runoff ? 1 : 0;
+    ctx->out_qmod = qmod ? 1 : 0;
+    return MHM_OK;
+}
+
+int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (total_runoff) {
+        if (!ctx->out_tro) return fail(ctx, MHM_ERR_INVALID, "total_runoff output not enabled");
+        std::memcpy(total_runoff, ctx->host_tro.data(), ctx->host_tro.size() * sizeof(double));
+    }
+    if (qmod) {
+        if (!ctx->out_qmod) return fail(ctx, MHM_ERR_INVALID, "qmod output not enabled");
+        std::memcpy(qmod, ctx->host_qmod.data(), ctx->host_qmod.size() * sizeof(double));
+    }
+    return MHM_OK;
+}
+
+int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
+    const size_t N = ctx->N, M = ctx->M, L = ctx->L;
+    const int H = ctx->H;
+    CK(cudaSetDevice(ctx->device), "set device");
+    // which forcing kinds the configuration reads
+    bool need[5] = {true, true, ctx->proc_pet != 1, ctx->proc_pet == 1, ctx->proc_pet == 1};
+    const int32_t stride = (int32_t)std::lround(24.0 / (double)ctx->ntfd);
+    const int32_t first_row = (tt0 + stride - 1) / stride;
+    const int32_t last_row = (tt0 + n_steps - 1 + stride - 1) / stride;
+    int on_device = -1;
+    int32_t row0_all = 0;
+    for (int k = 0; k < 5; ++k) {
+        if (!need[k]) continue;
+        const ForcingSrc &f = ctx->forc[k];
+        if (!f.set) return fail(ctx, MHM_ERR_INVALID, "forcing kind " + std::to_string(k) + " not set");
+        if (first_row < f.row0 || last_row > f.row0 + f.n_rows - 1)
+            return fail(ctx, MHM_ERR_INVALID, "forcing rows do not cover the requested steps");
+        if (on_device < 0) {
+            on_device = f.on_device;
+            row0_all = f.row0;
+        }
+        if (on_device != f.on_device) return fail(ctx, MHM_ERR_INVALID, "mixed host/device forcing");
+        if (on_device && f.row0 != row0_all)
+            return fail(ctx, MHM_ERR_INVALID, "device forcing kinds must share row0");
+    }
+    // chunk length from the total-runoff budget
+    size_t per_step = M * N * sizeof(double);
+    int32_t Tc = (int32_t)std::max<size_t>(1, std::min<size_t>((size_t)n_steps, ctx->chunk_bytes / per_step));
+    if (!on_device) Tc = std::max<int32_t>(stride, Tc / stride * stride); // whole forcing rows per chunk
+    // calendar for the whole run (absolute forcing row in StepInfo::row)
+    std::vector<StepInfo> si(n_steps);
+    for (int32_t i = 0; i < n_steps; ++i) {
+        const int64_t tt = (int64_t)tt0 + i;
+        StepDate sd = step_date(ctx->jul_start, ctx->timestep, tt);
+        si[i].row = (int32_t)((tt + stride - 1) / stride);
+        si[i].month = (int8_t)sd.month;
+        si[i].isday = (int8_t)(sd.hour > 6 && sd.hour <= 18); // mo_meteo_handler.f90:1048
+        si[i].doy = (int16_t)sd.doy;
+    }
+    CK(upload(ctx->steps, si.data(), si.size(), ctx->stream), "steps");
+    CK(ctx->tro.ensure((size_t)Tc * M * N), "total runoff chunk");
+    if (ctx->proc_rout == 1) {
+        CK(ctx->qout.ensure(M * (size_t)Tc * L), "qout chunk");
+        CK(ctx->qtr.ensure(M * (size_t)Tc * L), "qtr chunk");
+        CK(ctx->qmod.ensure(M * (size_t)Tc * L), "qmod chunk");
+        if (ctx->G > 0) CK(ctx->q_gauge.ensure(M * (size_t)ctx->G * n_steps), "q_gauge");
+    }
+    if (ctx->out_tro) ctx->host_tro.assign((size_t)n_steps * M * N, 0.0);
+    if (ctx->out_qmod) ctx->host_qmod.assign(M * (size_t)n_steps * L, 0.0);
+    const int32_t max_rows = (Tc + stride - 1) / stride + 1;
+    if (!on_device)
+        for (int k = 0; k < 5; ++k)
+            if (need[k])
+                for (int s = 0; s < 2; ++s) CK(ctx->stage[k][s].ensure((size_t)max_rows * N), "forcing staging");
+
+    const int nchunks = (n_steps + Tc - 1) / Tc;
+    auto chunk_rows = [&](int c, int32_t &r0, int32_t &r1) {
+        const int32_t s0 = c * Tc, s1 = std::min(n_steps, s0 + Tc) - 1;
+        r0 = si[s0].row;
+        r1 = si[s1].row;
+    };
+    auto issue_copy = [&](int c) -> int {
+        if (on_device || c >= nchunks) return MHM_OK;
+        const int slot = c & 1;
+        int32_t r0, r1;
+        chunk_rows(c, r0, r1);
+        if (c >= 2) CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_consumed[slot], 0), "wait slot");
+        for (int k = 0; k < 5; ++k) {
+            if (!need[k]) continue;
+            const ForcingSrc &f = ctx->forc[k];
+            CK(cudaMemcpyAsync(ctx->stage[k][slot].p, f.ptr + (size_t)(r0 - f.row0) * N,
+                               (size_t)(r1 - r0 + 1) * N * sizeof(double), cudaMemcpyHostToDevice, ctx->copy_stream),
+               "forcing H2D");
+        }
+        CK(cudaEventRecord(ctx->ev_copied[slot], ctx->copy_stream), "record copied");
+        return MHM_OK;
+    };
+    cudaEvent_t run_a = nullptr, run_b = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&run_a);
+        cudaEventCreate(&run_b);
+        cudaEventRecord(run_a, ctx->stream);
+    }
+    // the stream must not start reading staging slots before the copies are issued
+    if (int rc = issue_copy(0)) return rc;
+    for (int c = 0; c < nchunks; ++c) {
+        if (int rc = issue_copy(c + 1)) return rc;
+        const int32_t s0 = c * Tc;
+        const int32_t nT = std::min(n_steps, s0 + Tc) - s0;
+        const int slot = c & 1;
+        CellArgs a{};
+        a.n_cells = ctx->N;
+        a.n_members = ctx->M;
+        a.n_steps = nT;
+        a.proc_sm = ctx->proc_sm;
+        a.proc_pet = ctx->proc_pet;
+        a.is_hourly = ctx->ntfd == 24;
+        a.reset_sm = (tt0 + s0 == 1) && !ctx->read_states;
+        a.c2TSTu = (double)ctx->timestep / 24.0;
+        a.nTstepDay = 24.0 / (double)ctx->timestep;
+        const double *fp[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        if (on_device) {
+            a.row_base = row0_all;
+            for (int k = 0; k < 5; ++k)
+                if (need[k]) fp[k] = ctx->forc[k].ptr;
+        } else {
+            int32_t r0, r1;
+            chunk_rows(c, r0, r1);
+            a.row_base = r0;
+            for (int k = 0; k < 5; ++k)
+                if (need[k]) fp[k] = ctx->stage[k][slot].p;
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[slot], 0), "wait copied");
+        }
+        a.pre = fp[0];
+        a.temp = fp[1];
+        a.pet = fp[2];
+        a.tmin = fp[3];
+        a.tmax = fp[4];
+        a.steps = ctx->steps.p + s0;
+        a.params = ctx->params.p;
+        a.states = ctx->states.p;
+        a.tro = ctx->tro.p;
+        a.latitude = ctx->latitude.p;
+        a.tab = ctx->tab;
+        {
+            Bracket br(ctx, 0);
+            CK(launch_cell_chain(a, H, ctx->stream), "cell chain launch");
+            br.done();
+            g_launches++;
+        }
+        if (!on_device) CK(cudaEventRecord(ctx->ev_consumed[slot], ctx->stream), "record consumed");
+        if (ctx->out_tro)
+            CK(cudaMemcpyAsync(ctx->host_tro.data() + (size_t)s0 * M * N, ctx->tro.p, (size_t)nT * M * N * sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->stream),
+               "tro D2H");
+        if (ctx->proc_rout != 1) continue;
+        AccArgs acc{};
+        acc.n_cells = ctx->N;
+        acc.n_nodes = ctx->L;
+        acc.n_members = ctx->M;
+        acc.n_steps = nT;
+        acc.map_flag = ctx->map_flag;
+        acc.TST = 3600.0 * ctx->timestep;
+        acc.tro = ctx->tro.p;
+        acc.l1_area = ctx->l1_area.p;
+        acc.node_cell_ptr = ctx->node_cell_ptr.p;
+        acc.node_cells = ctx->node_cells.p;
+        acc.pos_l11_l1 = ctx->pos_l11_l1.p;
+        acc.pos_area = ctx->pos_area.p;
+        acc.qout = ctx->qout.p;
+        {
+            Bracket br(ctx, 1);
+            CK(launch_runoff_acc(acc, ctx->stream), "runoff acc launch");
+            br.done();
+            g_launches++;
+        }
+        RouteArgs r{};
+        r.n_nodes = ctx->L;
+        r.n_members = ctx->M;
+        r.n_steps = nT;
+        r.write_qmod = 1;
+        r.up_ptr = ctx->up_ptr.p;
+        r.up_pos = ctx->up_pos.p;
+        r.pos_flags = ctx->pos_flags.p;
+        r.C1 = ctx->C1.p;
+        r.C2 = ctx->C2.p;
+        r.qout = ctx->qout.p;
+        r.qtr = ctx->qtr.p;
+        r.qmod = ctx->qmod.p;
+        r.qtin1 = ctx->qtin1.p;
+        r.qtr1 = ctx->qtr1.p;
+        {
+            Bracket br(ctx, 2);
+            for (int l = 0; l < ctx->net.n_levels; ++l) {
+                r.lvl_begin = ctx->net.level_ptr[l];
+                r.lvl_end = ctx->net.level_ptr[l + 1];
+                CK(launch_route_level(r, ctx->stream), "route launch");
+                g_launches++;
+            }
+            br.done();
+        }
+        if (ctx->G > 0) {
+            GaugeArgs g{};
+            g.n_members = ctx->M;
+            g.n_steps = nT;
+            g.n_nodes = ctx->L;
+            g.n_gauges = ctx->G;
+            g.step_offset = s0;
+            g.total_steps = n_steps;
+            g.gauge_pos = ctx->gauge_pos_d.p;
+            g.qmod = ctx->qmod.p;
+            g.q_gauge = ctx->q_gauge.p;
+            CK(launch_gauge_gather(g, ctx->stream), "gauge launch");
+            g_launches++;
+        }
+        if (ctx->out_qmod)
+            for (size_t m = 0; m < M; ++m)
+                CK(cudaMemcpyAsync(ctx->host_qmod.data() + (m * n_steps + s0) * L, ctx->qmod.p + m * (size_t)nT * L,
+                                   (size_t)nT * L * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+                   "qmod D2H");
+        if (c == nchunks - 1) {
+            // qOUT and Qmod of the last step (restart fields)
+            for (size_t m = 0; m < M; ++m) {
+                CK(cudaMemcpyAsync(ctx->qout_last.p + m * L, ctx->qout.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, ctx->stream),
+                   "qout last");
+                CK(cudaMemcpyAsync(ctx->qmod_last.p + m * L, ctx->qmod.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, ctx->stream),
+                   "qmod last");
+            }
+        }
+    }
+    if (ctx->timing) {
+        cudaEventRecord(run_b, ctx->stream);
+        ctx->pending.push_back({3, run_a, run_b});
+    }
+    if (q_gauge && ctx->proc_rout == 1 && ctx->G > 0)
+        CK(cudaMemcpyAsync(q_gauge, ctx->q_gauge.p, M * (size_t)ctx->G * n_steps * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream),
+           "q_gauge D2H");
+    CK(cudaStreamSynchronize(ctx->stream), "run sync");
+    ctx->last_steps = n_steps;
+    harvest_timing(ctx);
+    return MHM_OK;
+}
+
+int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
+{
+    if (!ctx || !st) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const size_t N = ctx->N, L = ctx->L;
+    const int H = ctx->H, ns = n_state_planes(H);
+    const double *S = ctx->states.p + (size_t)m * ns * N;
+    double *dst[5] = {st->interc, st->snowpack, st->sealSTW, st->unsatSTW, st->satSTW};
+    const int pl[5] = {S_INTERC, S_SNOW, S_SEAL, S_UNSAT, S_SAT};
+    for (int i = 0; i < 5; ++i)
+        if (dst[i]) CK(cudaMemcpy(dst[i], S + (size_t)pl[i] * N, N * sizeof(double), cudaMemcpyDeviceToHost), "state");
+    if (st->soilMoist)
+        CK(cudaMemcpy(st->soilMoist, S + (size_t)S_SM * N, (size_t)H * N * sizeof(double), cudaMemcpyDeviceToHost),
+           "SM");
+    if (ctx->proc_rout == 1) {
+        std::vector<double> buf(L);
+        auto by_node = [&](const double *dev, double *out, size_t off) -> int {
+            CK(cudaMemcpy(buf.data(), dev + m * L, L * sizeof(double), cudaMemcpyDeviceToHost), "routing state");
+            for (size_t v = 0; v < L; ++v) out[off + v] = buf[ctx->net.pos_of_node[v]];
+            return MHM_OK;
+        };
+        int rc;
+        if (st->qOUT && (rc = by_node(ctx->qout_last.p, st->qOUT, 0))) return rc;
+        if (st->Qmod && (rc = by_node(ctx->qmod_last.p, st->Qmod, 0))) return rc;
+        if (st->qTIN) {
+            if ((rc = by_node(ctx->qtin1.p, st->qTIN, 0))) return rc;
+            std::memcpy(st->qTIN + L, st->qTIN, L * sizeof(double));
+        }
+        if (st->qTR) {
+            if ((rc = by_node(ctx->qtr1.p, st->qTR, 0))) return rc;
+            std::memcpy(st->qTR + L, st->qTR, L * sizeof(double));
+        }
+        // L11_C1 / L11_C2 are per link (1..nLinks), the tail stays at its initial 0
+        auto by_link = [&](const double *dev, double *out) -> int {
+            CK(cudaMemcpy(buf.data(), dev + m * L, L * sizeof(double), cudaMemcpyDeviceToHost), "routing coeffs");
+            for (size_t i = 0; i < L; ++i) out[i] = 0.0;
+            for (int i = 0; i < ctx->n_links; ++i) out[i] = buf[ctx->net.link_pos[i]];
+            return MHM_OK;
+        };
+        if (st->C1 && (rc = by_link(ctx->C1.p, st->C1))) return rc;
+        if (st->C2 && (rc = by_link(ctx->C2.p, st->C2))) return rc;
+    }
+    return MHM_OK;
+}
+
+int mhm_set_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
+{
+    if (!ctx || !st) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const size_t N = ctx->N, L = ctx->L;
+    const int H = ctx->H, ns = n_state_planes(H);
+    double *S = ctx->states.p + (size_t)m * ns * N;
+    const double *src[5] = {st->interc, st->snowpack, st->sealSTW, st->unsatSTW, st->satSTW};
+    const int pl[5] = {S_INTERC, S_SNOW, S_SEAL, S_UNSAT, S_SAT};
+    for (int i = 0; i < 5; ++i)
+        if (src[i]) CK(cudaMemcpy(S + (size_t)pl[i] * N, src[i], N * sizeof(double), cudaMemcpyHostToDevice), "state");
+    if (st->soilMoist)
+        CK(cudaMemcpy(S + (size_t)S_SM * N, st->soilMoist, (size_t)H * N * sizeof(double), cudaMemcpyHostToDevice),
+           "SM");
+    if (ctx->proc_rout == 1) {
+        std::vector<double> buf(L);
+        auto to_pos = [&](const double *in, double *dev) -> int {
+            for (size_t v = 0; v < L; ++v) buf[ctx->net.pos_of_node[v]] = in[v];
+            CK(cudaMemcpy(dev + m * L, buf.data(), L * sizeof(double), cudaMemcpyHostToDevice), "routing state");
+            return MHM_OK;
+        };
+        int rc;
+        if (st->qOUT && (rc = to_pos(st->qOUT, ctx->qout_last.p))) return rc;
+        if (st->Qmod && (rc = to_pos(st->Qmod, ctx->qmod_last.p))) return rc;
+        if (st->qTIN && (rc = to_pos(st->qTIN, ctx->qtin1.p))) return rc;
+        if (st->qTR && (rc = to_pos(st->qTR, ctx->qtr1.p))) return rc;
+        auto link_to_pos = [&](const double *in, double *dev) -> int {
+            std::fill(buf.begin(), buf.end(), 0.0);
+            for (int i = 0; i < ctx->n_links; ++i) buf[ctx->net.link_pos[i]] = in[i];
+            CK(cudaMemcpy(dev + m * L, buf.data(), L * sizeof(double), cudaMemcpyHostToDevice), "routing coeffs");
+            return MHM_OK;
+        };
+        if (st->C1 && (rc = link_to_pos(st->C1, ctx->C1.p))) return rc;
+        if (st->C2 && (rc = link_to_pos(st->C2, ctx->C2.p))) return rc;
+    }
+    return MHM_OK;
+}
+
+int mhm_get_var(mhm_ctx *ctx, int32_t m, const char *name, double *out)
+{
+    if (!ctx || !name || !out) return MHM_ERR_INVALID;
+    mhm_restart st{};
+    const std::string n(name);
+    if (n == "L1_INTER") st.interc = out;
+    else if (n == "L1_SNOWPACK") st.snowpack = out;
+    else if (n == "L1_SEALSTW") st.sealSTW = out;
+    else if (n == "L1_SOILMOIST") st.soilMoist = out;
+    else if (n == "L1_UNSATSTW") st.unsatSTW = out;
+    else if (n == "L1_SATSTW") st.satSTW = out;
+    else if (n == "L11_QMOD") st.Qmod = out;
+    else if (n == "L11_QOUT") st.qOUT = out;
+    else return fail(ctx, MHM_ERR_INVALID, "unknown variable " + n);
+    if ((st.Qmod || st.qOUT) && ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
+    return mhm_get_state(ctx, m, &st);
+}
+
+int mhm_set_timing(mhm_ctx *ctx, int32_t on)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    ctx->timing = on != 0;
+    for (int i = 0; i < 4; ++i) {
+        ctx->t_launches[i] = 0;
+        ctx->t_ms[i] = 0.0;
+    }
+    return MHM_OK;
+}
+
+int mhm_get_timing(mhm_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms)
+{
+    if (!ctx || kind < 0 || kind > 3) return MHM_ERR_INVALID;
+    if (launches) *launches = ctx->t_launches[kind];
+    if (total_ms) *total_ms = ctx->t_ms[kind];
+    return MHM_OK;
+}
+
+int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n, const int32_t *to_n,
+                      int32_t *net_perm, int32_t *r_order)
+{
+    if (n_nodes < 1 || n_outlets < 0 || n_outlets > n_nodes || !from_n || !to_n || !net_perm || !r_order)
+        return MHM_ERR_INVALID;
+    std::string err;
+    if (!routing_order(n_nodes, n_outlets, from_n, to_n, net_perm, r_order, err)) {
+        std::fprintf(stderr, "mhm_routing_order: %s\n", err.c_str());
+        return MHM_ERR_INVALID;
+    }
+    return MHM_OK;
+}
+
+int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t n, int32_t *month,
+                      int32_t *hour, int32_t *doy)
+{
+    if (jul_start < 2299161 || timestep < 1 || 24 % timestep != 0 || tt0 < 1 || n < 0) return MHM_ERR_INVALID;
+    for (int32_t i = 0; i < n; ++i) {
+        StepDate sd = step_date(jul_start, timestep, (int64_t)tt0 + i);
+        if (month) month[i] = sd.month;
+        if (hour) hour[i] = sd.hour;
+        if (doy) doy[i] = sd.doy;
+    }
+    return MHM_OK;
+}
+
+int mhm_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr) return MHM_ERR_INVALID;
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+    return e == cudaSuccess ? MHM_OK : (e == cudaErrorMemoryAllocation ? MHM_ERR_OOM : MHM_ERR_CUDA);
+}
+
+int mhm_host_free(void *ptr)
+{
+    return cudaFreeHost(ptr) == cudaSuccess ? MHM_OK : MHM_ERR_CUDA;
+}
+
+int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const double *y, double *out)
+{
+    if (op < 0 || op > 2 || n < 0 || !x || !out || (op == 2 && !y)) return MHM_ERR_INVALID;
+    if (where == 0) {
+        for (int64_t i = 0; i < n; ++i)
+            out[i] = op == 0 ? hm_log(x[i]) : op == 1 ? hm_exp(x[i]) : hm_pow(x[i], y[i]);
+        return MHM_OK;
+    }
+    double *dx = nullptr, *dy = nullptr, *dout = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dx);
+        cudaFree(dy);
+        cudaFree(dout);
+    };
+    size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMalloc(&dx, bytes) != cudaSuccess || cudaMalloc(&dout, bytes) != cudaSuccess ||
+        (op == 2 && cudaMalloc(&dy, bytes) != cudaSuccess)) {
+        cleanup();
+        return MHM_ERR_OOM;
+    }
+    cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice);
+    if (op == 2) cudaMemcpy(dy, y, bytes, cudaMemcpyHostToDevice);
+    cudaError_t e = launch_hmath_eval(op, n, dx, dy, dout, 0);
+    g_launches++;
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cleanup();
+    return e == cudaSuccess ? MHM_OK : MHM_ERR_CUDA;
+}
+
+int mhm_probe_fp64(int64_t iters, double *flops)
+{
+    if (iters < 1 || !flops) return MHM_ERR_INVALID;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MHM_ERR_CUDA;
+    const int threads = 256, blocks = sms * 8;
+    double *sink = nullptr;
+    if (cudaMalloc(&sink, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return MHM_ERR_OOM;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    launch_fp64_probe(iters / 10 + 1, blocks, threads, sink, 0); // warm-up
+    cudaEventRecord(a, 0);
+    cudaError_t e = launch_fp64_probe(iters, blocks, threads, sink, 0);
+    cudaEventRecord(b, 0);
+    g_launches += 2;
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    if (e != cudaSuccess || ms <= 0.f) return MHM_ERR_CUDA;
+    // 8 independent chains per thread, 1 DFMA (2 FLOP) each per iteration
+    *flops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3);
+    return MHM_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,106 @@
+// mhm_kernels.cuh -- shared declarations of the device kernels and their
+// argument blocks (device layout of a context).
+#pragma once
+#include <cstdint>
+
+namespace mhm {
+
+constexpr int kMaxHorizons = 8;
+
+// Per-member effective-parameter planes, each [n_cells] contiguous:
+// params[(m * n_planes + plane) * n_cells + k].
+enum ParamPlane : int {
+    P_FSEALED = 0,
+    P_ALPHA,
+    P_DDINC,
+    P_DDMAX,
+    P_DDNOPRE,
+    P_FASP,
+    P_HARSAM,
+    P_KARST,
+    P_K0, // kFastFlow
+    P_K1, // kSlowFlow
+    P_K2, // kBaseFlow
+    P_KP, // kPerco
+    P_JARVIS,
+    P_TTHRESH,
+    P_UTHRESH,
+    P_STHRESH,
+    P_MAXINTER,             // 12 planes (LAI month)
+    P_PETLAI = P_MAXINTER + 12, // 12 planes
+    P_HORIZON = P_PETLAI + 12,  // then 5 groups of H planes: fRoots, SMs, FC, PW, beta
+};
+__host__ __device__ constexpr int n_param_planes(int H) { return P_HORIZON + 5 * H; }
+
+// Per-member state planes: states[(m * n_planes + plane) * n_cells + k]
+enum StatePlane : int { S_INTERC = 0, S_SNOW, S_SEAL, S_UNSAT, S_SAT, S_SM };
+__host__ __device__ constexpr int n_state_planes(int H) { return S_SM + H; }
+
+// One model step: forcing row (0-based within the device forcing window),
+// calendar month (1..12), day flag and day of year.
+struct StepInfo {
+    int32_t row;
+    int8_t month;
+    int8_t isday;
+    int16_t doy;
+};
+
+struct MonthTables {
+    double evap[12];
+    double fday_prec[12], fnight_prec[12];
+    double fday_pet[12], fnight_pet[12];
+    double fday_temp[12], fnight_temp[12];
+};
+
+struct CellArgs {
+    int32_t n_cells, n_members, n_steps;
+    int32_t proc_sm, proc_pet, is_hourly;
+    int32_t reset_sm;   // tt == 1 && !read_states: SM = 0.5 * FC before the first step
+    int32_t row_base;   // forcing row (1-based iMeteoTS) stored first in the buffers
+    double c2TSTu;      // timestep / 24
+    double nTstepDay;   // 24 / timestep
+    const double *pre, *temp, *pet, *tmin, *tmax; // [rows][n_cells] from row_base
+    const StepInfo *steps;                        // [n_steps]
+    const double *params;                         // [M][planes][n_cells]
+    double *states;                               // [M][planes][n_cells]
+    double *tro;                                  // [n_steps][M][n_cells]
+    const double *latitude;                       // [n_cells]
+    MonthTables tab;
+};
+
+struct AccArgs {
+    int32_t n_cells, n_nodes, n_members, n_steps;
+    int32_t map_flag, pad_;
+    double TST;                  // HourSecs * timestep
+    const double *tro;           // [n_steps][M][n_cells]
+    const double *l1_area;       // [n_cells]
+    const int32_t *node_cell_ptr; // [n_nodes+1] by level position
+    const int32_t *node_cells;    // ascending L1 index per node
+    const int32_t *pos_l11_l1;    // [n_nodes] 0-based L1 cell of the node (!map_flag)
+    const double *pos_area;       // [n_nodes] L11 area by position
+    double *qout;                 // [M][n_steps][n_nodes] by level position
+};
+
+struct RouteArgs {
+    int32_t n_nodes, n_members, n_steps;
+    int32_t lvl_begin, lvl_end; // positions of this level
+    int32_t write_qmod;
+    const int32_t *up_ptr;      // [n_nodes+1]
+    const int32_t *up_pos;      // upstream positions in rank order
+    const int8_t *pos_flags;    // bit0: is link (has C1/C2), bit1: add qOUT
+    const double *C1, *C2;      // [M][n_nodes] by position
+    const double *qout;         // [M][n_steps][n_nodes]
+    double *qtr;                // [M][n_steps][n_nodes] routed outflow series
+    double *qmod;               // [M][n_steps][n_nodes] (if write_qmod)
+    double *qtin1, *qtr1;       // [M][n_nodes] state (previous step)
+};
+
+struct GaugeArgs {
+    int32_t n_members, n_steps, n_nodes, n_gauges;
+    int32_t step_offset, total_steps;
+    const int32_t *gauge_pos;
+    const double *qmod;    // [M][n_steps][n_nodes]
+    double *q_gauge;       // [M][n_gauges][total_steps]
+};
+
+} // namespace mhm

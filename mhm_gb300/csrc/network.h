@@ -1,0 +1,50 @@
+// network.h -- host-side preparation of an L11 routing network for the
+// level-synchronous device routing, and the model-step calendar.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mhm {
+
+// Routing network laid out by topological level (positions 0..n_nodes-1).
+struct LevelNetwork {
+    int32_t n_nodes = 0, n_links = 0, n_levels = 0;
+    std::vector<int32_t> level_ptr;  // [n_levels + 1] position ranges
+    std::vector<int32_t> pos_of_node; // [n_nodes] 0-based node -> position
+    std::vector<int32_t> node_of_pos; // [n_nodes]
+    std::vector<int32_t> up_ptr;      // [n_nodes + 1] by position
+    std::vector<int32_t> up_pos;      // upstream positions, netPerm rank order
+    std::vector<int8_t> pos_flags;    // bit0 is link, bit1 adds its own qOUT
+    std::vector<int32_t> link_pos;    // [n_links] 1-based link i-1 -> position of fromN(i)
+    int32_t max_width = 0;
+};
+
+// Builds the level layout from L11_netPerm / L11_fromN / L11_toN (1-based, as
+// produced by L11_set_network_topology and L11_routing_order,
+// src/mRM/mo_mrm_net_startup.f90:630-886).  Fails (returns false, message in
+// err) unless netPerm is a permutation of the links in which every link comes
+// after all links that drain into its source node -- the order the reference
+// routes in (src/mRM/mo_mrm_routing.f90:435-459).
+bool build_level_network(int32_t n_nodes, int32_t n_outlets, const int32_t *net_perm, const int32_t *from_n,
+                         const int32_t *to_n, LevelNetwork &out, std::string &err);
+
+// Routing order of L11_routing_order (src/mRM/mo_mrm_net_startup.f90:728-886)
+// computed with per-link counts of unranked upstream links instead of the
+// reference's all-pairs scan: O(n_links x sweeps).  Same ranks, same netPerm.
+bool routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n, const int32_t *to_n,
+                   int32_t *net_perm, int32_t *r_order, std::string &err);
+
+// Calendar of model step tt (1-based) for a run starting at Julian day number
+// jul_start with `timestep` hours per step: integer Gregorian arithmetic
+// (E. G. Richards' JDN <-> date algorithms), equal to the reference's
+// dec2date(newTime - 0.5) (src/common/mo_common_datetime_type.f90:71-125,
+// src/mHM/mo_mhm_interface_run.f90:360).
+struct StepDate {
+    int32_t year, month, day, hour, doy;
+};
+StepDate step_date(int32_t jul_start, int32_t timestep, int64_t tt);
+int64_t gregorian_to_jdn(int32_t y, int32_t m, int32_t d);
+void jdn_to_gregorian(int64_t jdn, int32_t *y, int32_t *m, int32_t *d);
+
+} // namespace mhm

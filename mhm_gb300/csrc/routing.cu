@@ -1,0 +1,153 @@
+// routing.cu -- mRM L1->L11 runoff accumulation and Muskingum link routing,
+// time-chunked and level-synchronous.
+//
+// The reference advances every link one step at a time in netPerm order
+// (L11_routing, src/mRM/mo_mrm_routing.f90:380-481).  The per-link recurrence
+// only reads the link's own previous step and the same-step outflow of its
+// upstream links, so a whole chunk of steps of one link can run as soon as the
+// chunk of every upstream link is done: links are grouped into topological
+// levels and each level advances its links through the full chunk.  Inflow
+// sums at confluences keep the reference's order (upstream links in netPerm
+// rank order, then the node's own qOUT), so results are bit-identical.
+#include <cstdint>
+
+#include "mhm_kernels.cuh"
+
+namespace mhm {
+
+// L11_runoff_acc, src/mRM/mo_mrm_pre_routing.f90:77-143: per (step, member,
+// node) the area-weighted sum of its L1 cells in ascending cell order, then
+// *1000/TST.  Output indexed by routing-level position.
+__global__ void __launch_bounds__(256) runoff_acc_kernel(const AccArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t L = a.n_nodes;
+    const int64_t total = (int64_t)a.n_steps * a.n_members * L;
+    if (gid >= total) return;
+    const int pos = (int)(gid % L);
+    const int64_t tm = gid / L; // t * M + m
+    const int m = (int)(tm % a.n_members);
+    const int t = (int)(tm / a.n_members);
+    const double *row = a.tro + (size_t)tm * a.n_cells;
+    double q;
+    if (a.map_flag) {
+        double acc = 0.0;
+        const int b = __ldg(a.node_cell_ptr + pos), e = __ldg(a.node_cell_ptr + pos + 1);
+        for (int j = b; j < e; ++j) {
+            const int k = __ldg(a.node_cells + j);
+            acc = acc + __ldg(row + k) * __ldg(a.l1_area + k);
+        }
+        q = acc * 1000.0 / a.TST;
+    } else {
+        q = __ldg(row + __ldg(a.pos_l11_l1 + pos)) * __ldg(a.pos_area + pos) * 1000.0 / a.TST;
+    }
+    a.qout[((size_t)m * a.n_steps + t) * L + pos] = q;
+}
+
+// One topological level: each (member, node) of the level advances through
+// the chunk.  L11_routing body, src/mRM/mo_mrm_routing.f90:435-478.
+__global__ void __launch_bounds__(128) route_level_kernel(const RouteArgs a)
+{
+    const int width = a.lvl_end - a.lvl_begin;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)width * a.n_members) return;
+    const int m = (int)(gid / width);
+    const int pos = a.lvl_begin + (int)(gid - (int64_t)m * width);
+    const int64_t L = a.n_nodes;
+    const size_t ms = (size_t)m * L;
+    const size_t series = (size_t)m * a.n_steps * L;
+    const int ub = __ldg(a.up_ptr + pos), ue = __ldg(a.up_ptr + pos + 1);
+    const int flags = __ldg(a.pos_flags + pos);
+    const bool is_link = flags & 1;
+    const bool add_qout = flags & 2;
+    const double c1 = is_link ? __ldg(a.C1 + ms + pos) : 0.0;
+    const double c2 = is_link ? __ldg(a.C2 + ms + pos) : 0.0;
+    double qtin1 = a.qtin1[ms + pos];
+    double qtr1 = a.qtr1[ms + pos];
+    for (int t = 0; t < a.n_steps; ++t) {
+        const size_t row = series + (size_t)t * L;
+        double qtin = 0.0; // netNode_qTIN(:, IT) = 0
+        for (int j = ub; j < ue; ++j) qtin = qtin + a.qtr[row + __ldg(a.up_pos + j)];
+        if (add_qout) qtin = qtin + __ldg(a.qout + row + pos);
+        if (is_link) {
+            double qtr = qtr1 + c1 * (qtin1 - qtr1) + c2 * (qtin - qtin1);
+            a.qtr[row + pos] = qtr;
+            qtr1 = qtr;
+        }
+        qtin1 = qtin;
+        a.qmod[row + pos] = 0.0 + qtin; // L11_qMod = (0 + Qmod) / real(rout_loop = 1)
+    }
+    a.qtin1[ms + pos] = qtin1;
+    a.qtr1[ms + pos] = qtr1;
+}
+
+// GaugeDischarge(gaugeIndexList) = L11_Qmod(gaugeNodeList), mo_mrm_routing.f90:299-301
+__global__ void gauge_gather_kernel(const GaugeArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)a.n_members * a.n_gauges * a.n_steps;
+    if (gid >= total) return;
+    const int t = (int)(gid % a.n_steps);
+    const int64_t mg = gid / a.n_steps;
+    const int g = (int)(mg % a.n_gauges);
+    const int m = (int)(mg / a.n_gauges);
+    const double v = a.qmod[((size_t)m * a.n_steps + t) * a.n_nodes + __ldg(a.gauge_pos + g)];
+    a.q_gauge[((size_t)m * a.n_gauges + g) * a.total_steps + a.step_offset + t] = v;
+}
+
+// reg_rout, src/mRM/mo_mrm_mpr.f90:61-119, one thread per link; ss_max is the
+// basin's max slope (parameter independent, computed on the host once).
+__global__ void reg_rout_kernel(int n_links, const double *p5, double ss_max, double TS,
+                                const double *length, const double *slope, const double *ffp,
+                                const int32_t *link_pos, double *C1, double *C2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_links) return;
+    const double p0 = p5[0], p1 = p5[1], p2 = p5[2], p3 = p5[3], p4 = p5[4];
+    double K = p0 + p1 * (length[i] * 0.001) + p2 * slope[i] + p3 * ffp[i];
+    double xi = p4 * (1.0 + slope[i] / ss_max);
+    if (xi > 0.5) xi = 0.5;
+    if (xi < 0.005) xi = 0.005;
+    if (K > 0.5 * TS / xi) K = 0.5 * TS / xi;
+    if (K < 0.5 * TS / (1.0 - xi)) K = 0.5 * TS / (1.0 - xi);
+    const double c1 = TS / (K * (1.0 - xi) + 0.5 * TS);
+    const int pos = link_pos[i];
+    C1[pos] = c1;
+    C2[pos] = 1.0 - c1 * K / TS;
+}
+
+cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_steps * a.n_members * a.n_nodes;
+    if (n == 0) return cudaSuccess;
+    runoff_acc_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_route_level(const RouteArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)(a.lvl_end - a.lvl_begin) * a.n_members;
+    if (n == 0) return cudaSuccess;
+    route_level_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_members * a.n_gauges * a.n_steps;
+    if (n == 0) return cudaSuccess;
+    gauge_gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double TS, const double *length,
+                            const double *slope, const double *ffp, const int32_t *link_pos, double *C1,
+                            double *C2, cudaStream_t s)
+{
+    if (n_links <= 0) return cudaSuccess;
+    reg_rout_kernel<<<(n_links + 127) / 128, 128, 0, s>>>(n_links, p5, ss_max, TS, length, slope, ffp, link_pos,
+                                                          C1, C2);
+    return cudaGetLastError();
+}
+
+} // namespace mhm

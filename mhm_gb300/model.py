@@ -1,0 +1,228 @@
+"""Host-side interface over the C ABI, shaped like the reference's run API.
+
+The reference drives one basin with mhm_interface_run_prepare /
+prepare_domain / do_time_step (src/mHM/mo_mhm_interface_run.f90:160-638) and
+exposes them to Python as ``mhm.run.*`` (pybind/src/wrapper.f90:176-233).
+``MhmGpu`` keeps that vocabulary: ``prepare`` loads effective parameters and
+default states (the restart path of mhm_interface_run_prepare), ``set_meteo``
+hands over forcing, ``run`` advances time steps (do_time_step x n) and
+``get_variable`` / ``get_runoff`` read results back.  Everything executes in
+libmhm_gpu.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .synth import Domain
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def _d(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+class MhmError(RuntimeError):
+    pass
+
+
+class MhmGpu:
+    """One basin (optionally with n_members parameter sets) on one GPU."""
+
+    def __init__(self, dom: Domain, proc_soilmoist: int = 1, proc_pet: int = 0, proc_routing: int = 1,
+                 hourly: bool = True, n_members: int = 1, read_states: bool = False, device: int = -1):
+        self.L = _lib.load()
+        self.dom = dom
+        self.n_members = n_members
+        self._keep: list = []
+
+        def keep(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dt)
+            self._keep.append(a)
+            return a
+
+        d = _lib.DomainDesc()
+        d.n_cells = dom.n_cells
+        d.n_horizons = dom.n_horizons
+        d.n_nodes = dom.n_nodes
+        d.n_outlets = dom.n_outlets
+        d.timestep = dom.timestep
+        d.proc_soilmoist = proc_soilmoist
+        d.proc_pet = proc_pet
+        d.proc_routing = proc_routing
+        d.n_tstep_forcing_day = 24 if hourly else 1
+        d.jul_start = dom.jul_start
+        d.map_flag = 1
+        d.n_gauges = len(dom.gauge_node)
+        d.n_members = n_members
+        d.read_states = 1 if read_states else 0
+        d.evap_coeff = _d(keep(dom.evap_coeff))
+        d.fday_prec = _d(keep(dom.fday_prec))
+        d.fnight_prec = _d(keep(dom.fnight_prec))
+        d.fday_pet = _d(keep(dom.fday_pet))
+        d.fnight_pet = _d(keep(dom.fnight_pet))
+        d.fday_temp = _d(keep(dom.fday_temp))
+        d.fnight_temp = _d(keep(dom.fnight_temp))
+        d.l1_area_km2 = _d(keep(dom.l1_area_km2))
+        d.l1_l11_id = _i(keep(dom.l1_l11_id, np.int32))
+        d.l11_area_km2 = _d(keep(dom.l11_area_km2))
+        d.l11_l1_id = _i(keep(dom.l11_l1_id, np.int32))
+        d.net_perm = _i(keep(dom.net_perm, np.int32))
+        d.from_n = _i(keep(dom.from_n, np.int32))
+        d.to_n = _i(keep(dom.to_n, np.int32))
+        d.length = _d(keep(dom.length))
+        d.slope = _d(keep(dom.slope))
+        d.ffp_imp = _d(keep(dom.ffp_imp))
+        d.gauge_node = _i(keep(dom.gauge_node, np.int32))
+        d.latitude = _d(keep(dom.latitude))
+        self._desc = d
+        ctx = C.c_void_p()
+        rc = self.L.mhm_ctx_create(C.byref(d), device, C.byref(ctx))
+        if rc != 0:
+            raise MhmError(f"mhm_ctx_create failed ({rc})")
+        self.ctx = ctx
+        self._forcing_keep: dict[int, object] = {}
+
+    # ---- lifetime ----
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.mhm_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.L.mhm_last_error(self.ctx).decode(errors="replace")
+            raise MhmError(f"{what} failed ({rc}): {msg}")
+
+    # ---- set-up (mhm_interface_run_prepare) ----
+    def set_eff_params(self, p: dict[str, np.ndarray], member: int = 0):
+        ep = _lib.EffParams()
+        hold = []
+        for name in _lib.EFF_PARAM_FIELDS:
+            a = p.get(name)
+            if a is not None:
+                a = np.ascontiguousarray(a, np.float64)
+                hold.append(a)
+                setattr(ep, name, _d(a))
+        self._check(self.L.mhm_set_eff_params(self.ctx, member, C.byref(ep)), "mhm_set_eff_params")
+
+    def set_routing_params(self, p5, member: int = 0):
+        a = np.ascontiguousarray(p5, np.float64)
+        self._check(self.L.mhm_set_routing_params(self.ctx, member, _d(a)), "mhm_set_routing_params")
+
+    def init_states(self, member: int = 0):
+        hd = np.ascontiguousarray(self.dom.horizon_depth, np.float64)
+        self._check(self.L.mhm_init_states(self.ctx, member, _d(hd)), "mhm_init_states")
+
+    def prepare(self, params: dict[str, np.ndarray] | list, routing_params=None):
+        """Effective parameters (one dict, or one per member), default states
+        and Muskingum coefficients for every member."""
+        plist = params if isinstance(params, list) else [params] * self.n_members
+        rlist = routing_params if (routing_params is not None and np.ndim(routing_params) == 2) else \
+            [routing_params] * self.n_members
+        for m in range(self.n_members):
+            self.set_eff_params(plist[m], m)
+            self.init_states(m)
+            if rlist[m] is not None:
+                self.set_routing_params(rlist[m], m)
+
+    # ---- forcing (set_meteo) ----
+    def set_forcing(self, kind: int, row0: int, data, on_device: bool = False):
+        """data: numpy [rows, N] (host) or an object with data_ptr() (device)."""
+        if on_device:
+            ptr = C.c_void_p(data.data_ptr())
+            n_rows = int(data.shape[0])
+        else:
+            data = np.ascontiguousarray(data, np.float64)
+            ptr = data.ctypes.data_as(C.c_void_p)
+            n_rows = data.shape[0]
+        self._forcing_keep[kind] = data
+        self._check(self.L.mhm_set_forcing(self.ctx, kind, row0, n_rows, ptr, 1 if on_device else 0),
+                    "mhm_set_forcing")
+
+    def set_meteo(self, row0: int, pre, temp, pet=None, tmin=None, tmax=None, on_device: bool = False):
+        self.set_forcing(_lib.FORC_PRE, row0, pre, on_device)
+        self.set_forcing(_lib.FORC_TEMP, row0, temp, on_device)
+        if pet is not None:
+            self.set_forcing(_lib.FORC_PET, row0, pet, on_device)
+        if tmin is not None:
+            self.set_forcing(_lib.FORC_TMIN, row0, tmin, on_device)
+        if tmax is not None:
+            self.set_forcing(_lib.FORC_TMAX, row0, tmax, on_device)
+
+    # ---- time stepping (do_time_step x n) ----
+    def enable_outputs(self, total_runoff: bool = False, qmod: bool = False):
+        self._check(self.L.mhm_enable_outputs(self.ctx, int(total_runoff), int(qmod)), "mhm_enable_outputs")
+        self._out = (total_runoff, qmod)
+
+    def run(self, tt0: int, n_steps: int) -> np.ndarray:
+        """Advance steps tt0..tt0+n_steps-1; returns gauge discharge
+        [member, gauge, step] in m3 s-1."""
+        G = len(self.dom.gauge_node)
+        q = np.zeros((self.n_members, G, n_steps), np.float64)
+        self._check(self.L.mhm_run(self.ctx, tt0, n_steps, _d(q) if G else None), "mhm_run")
+        self._last_steps = n_steps
+        return q
+
+    def get_outputs(self):
+        n = self._last_steps
+        tro = np.zeros((n, self.n_members, self.dom.n_cells)) if self._out[0] else None
+        qm = np.zeros((self.n_members, n, self.dom.n_nodes)) if self._out[1] else None
+        self._check(self.L.mhm_get_outputs(self.ctx, _d(tro), _d(qm)), "mhm_get_outputs")
+        return tro, qm
+
+    # ---- state access (restart fields, get_variable) ----
+    def get_state(self, member: int = 0) -> dict[str, np.ndarray]:
+        N, H, L = self.dom.n_cells, self.dom.n_horizons, self.dom.n_nodes
+        shapes = {"interc": N, "snowpack": N, "sealSTW": N, "unsatSTW": N, "satSTW": N,
+                  "soilMoist": H * N, "qOUT": L, "Qmod": L, "qTIN": 2 * L, "qTR": 2 * L, "C1": L, "C2": L}
+        out = {k: np.zeros(v) for k, v in shapes.items()}
+        st = _lib.Restart(**{k: _d(v) for k, v in out.items()})
+        self._check(self.L.mhm_get_state(self.ctx, member, C.byref(st)), "mhm_get_state")
+        return out
+
+    def set_state(self, state: dict[str, np.ndarray], member: int = 0):
+        arrs = {k: np.ascontiguousarray(v, np.float64) for k, v in state.items()}
+        st = _lib.Restart(**{k: _d(v) for k, v in arrs.items()})
+        self._check(self.L.mhm_set_state(self.ctx, member, C.byref(st)), "mhm_set_state")
+
+    def get_variable(self, name: str, member: int = 0) -> np.ndarray:
+        n = {"L1_SOILMOIST": self.dom.n_horizons * self.dom.n_cells, "L11_QMOD": self.dom.n_nodes,
+             "L11_QOUT": self.dom.n_nodes}.get(name, self.dom.n_cells)
+        out = np.zeros(n)
+        self._check(self.L.mhm_get_var(self.ctx, member, name.encode(), _d(out)), "mhm_get_var")
+        return out
+
+    # ---- timing ----
+    def set_timing(self, on: bool):
+        self._check(self.L.mhm_set_timing(self.ctx, int(on)), "mhm_set_timing")
+
+    def get_timing(self, kind: int) -> tuple[int, float]:
+        n = C.c_int64()
+        ms = C.c_double()
+        self._check(self.L.mhm_get_timing(self.ctx, kind, C.byref(n), C.byref(ms)), "mhm_get_timing")
+        return n.value, ms.value
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.mhm_ctx_stream(self.ctx) or 0)

@@ -1,0 +1,169 @@
+/*
+ * mhm_oracle.h -- CPU restatement of the mHM / mRM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
+ * implementation in mhm_gb300/: only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py may load it.  Nothing in the product links or
+ * calls it.
+ *
+ * Each function restates one reference routine (cited at its definition in
+ * mhm_oracle.c), keeping the reference's evaluation order, branch conditions,
+ * eps_dp = epsilon(1d0) and Fortran real**real semantics.  The reference is
+ * compiled by gfortran without FMA contraction, so this file is compiled with
+ * -ffp-contract=off.  Two builds exist:
+ *   liboracle_hmath.so -- exp/log/pow from mhm_gb300/csrc/hmath.h (the same
+ *                         elementary functions the GPU uses: bitwise parity);
+ *   liboracle_libm.so  -- exp/log/pow from the C library (glibc), i.e. the
+ *                         functions gfortran calls: the reference-semantics
+ *                         build, compared at 1e-9 relative.
+ * Arrays: 0-based C pointers; index values stored in them (L1_L11_Id,
+ * netPerm, fromN, toN, gauge nodes) are 1-based as in Fortran.  2-D arrays
+ * (cells, horizons) are column-major as in the reference: element (k, h) is at
+ * [h * nCells + k].
+ */
+#ifndef MHM_ORACLE_H
+#define MHM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- process routines (scalar, as in the reference) ---- */
+void ora_canopy_interc(double pet, double interc_max, double precip, double *interc,
+                       double *throughfall, double *evap_canopy);
+void ora_snow_accum_melt(double deg_day_incr, double deg_day_max, double deg_day_noprec,
+                         double prec, double temperature, double temperature_thresh,
+                         double thrfall, double *snow_pack, double *deg_day, double *melt,
+                         double *prec_effect, double *rain, double *snow);
+double ora_feddes_et_reduction(double sm, double fc, double pw, double froots);
+double ora_jarvis_et_reduction(double sm, double sat, double pw, double froots, double c1);
+void ora_soil_moisture(int processCase, int nH, double frac_sealed, double water_thresh_sealed,
+                       double pet, double evap_coeff, const double *sm_sat, const double *frac_roots,
+                       const double *sm_fc, const double *wilting_point, const double *sm_exponen,
+                       double jarvis_thresh_c1, double aet_canopy, double prec_effec,
+                       double *runoff_sealed, double *storage_sealed, double *infiltration,
+                       double *soil_moist, double *aet, double *aet_sealed);
+void ora_runoff_unsat_zone(double k1, double kp, double k0, double alpha, double karst_loss,
+                           double pefec_soil, double unsat_thresh, double *sat_storage,
+                           double *unsat_storage, double *slow_interflow, double *fast_interflow,
+                           double *perc);
+void ora_runoff_sat_zone(double k2, double *sat_storage, double *baseflow);
+double ora_L1_total_runoff(double fsealed, double fast, double slow, double base, double direct);
+
+double ora_extraterr_rad_approx(int doy, double latitude_rad);
+double ora_pet_hargreaves(double HarSamCoeff, double HarSamConst, double tavg, double tmax,
+                          double tmin, double latitude_deg, int doy);
+double ora_sat_vap_pressure(double tavg);
+double ora_slope_satpressure(double tavg);
+double ora_pet_priestly(double alpha, double rn, double tavg);
+double ora_pet_penman(double net_rad, double tavg, double act_vap_pressure, double aerodyn_resistance,
+                      double bulksurface_resistance, double a_s, double a_sh);
+
+double ora_disagg_meteo_weights(double day_val, double weight, double correction);
+double ora_disagg_flux_daynight(int isday, double ntimesteps_day, double day_val, double fday,
+                                double fnight);
+double ora_disagg_state_daynight(int isday, double ntimesteps_day, double day_val, double fday,
+                                 double fnight, int add_correction);
+
+/* ---- calendar (mo_julian restated) ---- */
+int32_t ora_julday(int32_t dd, int32_t mm, int32_t yy);
+void ora_caldat(int32_t julian, int32_t *dd, int32_t *mm, int32_t *yy);
+void ora_dec2date(double julian, int32_t *dd, int32_t *mm, int32_t *yy, int32_t *hh,
+                  int32_t *nn, int32_t *ss);
+/* Per-step calendar of a run, emulating datetimeinfo (init/increment) and the
+ * dec2date(newTime - 0.5) calls of do_time_step.  For steps tt = 1..nSteps:
+ * month[tt-1], hour, doy, day, year. */
+void ora_step_calendar(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
+                       int32_t *hour, int32_t *doy, int32_t *day, int32_t *year);
+
+/* ---- routing ---- */
+void ora_reg_rout(const double *param5, const double *length, const double *slope,
+                  const double *fFPimp, int nLinks, double TS, double *C1, double *C2);
+void ora_L11_runoff_acc(int nCells, int nNodes, const double *qAll, const double *efecArea,
+                        const int32_t *L1_L11_Id, const double *L11_areaCell,
+                        const int32_t *L11_L1_Id, int TS, int map_flag, double *qAcc);
+/* qTIN, qTR: column-major (nNodes, 2), column IT1=0 holds the previous step. */
+void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN,
+                     const int32_t *toN, const double *C1, const double *C2, const double *qOUT,
+                     double *qTIN, double *qTR, double *Qmod);
+/* L11_set_network_topology: links from the L11 D8 directions (mRM codes). fDir11 and
+ * the returned ids use the L11 grid packed column-major over the mask (cells 1..nCells),
+ * cellCoor[k] = (row, col) 1-based.  Returns nLinks; fromN/toN sized nCells. */
+int ora_L11_set_network_topology(int nrows, int ncols, const int32_t *id2d /*[ncols][nrows]*/,
+                                 int nCells, const int32_t *cellRow, const int32_t *cellCol,
+                                 const int32_t *fDir11, int32_t *fromN, int32_t *toN);
+/* L11_routing_order, literal O(nLinks^2) sweep.  Outputs sized nNodes:
+ * netPerm (1-based link ids in routing order), rOrder (rank of each link). */
+void ora_L11_routing_order(int nNodes, int nOutlets, const int32_t *fromN, const int32_t *toN,
+                           int32_t *netPerm, int32_t *rOrder);
+
+/* ---- whole-domain run (the mhm_eval time loop for one domain) ---- */
+typedef struct {
+    int32_t nCells, nH, nNodes, nOutlets, timestep;
+    int32_t proc_sm;      /* processMatrix(3,1): 1..4 */
+    int32_t proc_pet;     /* processMatrix(5,1): -1, 0, 1 */
+    int32_t proc_rout;    /* processMatrix(8,1): 0 or 1 */
+    int32_t nTstepForcingDay; /* 24 (hourly) or 1 (daily) */
+    int32_t read_states;  /* 1: states (and C1/C2) come from a restart */
+    int32_t jul_start;    /* simPer%julStart */
+    int32_t map_flag;     /* routing resolution >= hydrology resolution */
+    int32_t nGauges;
+    int32_t pad_;
+    const double *evap_coeff;                 /* [12] */
+    const double *fday_prec, *fnight_prec;    /* [12] */
+    const double *fday_pet, *fnight_pet;      /* [12] */
+    const double *fday_temp, *fnight_temp;    /* [12] */
+    const double *l1_area_km2;                /* [nCells] CellArea * 1e-6 */
+    const int32_t *l1_l11_id;                 /* [nCells] */
+    const double *l11_area_km2;               /* [nNodes] */
+    const int32_t *l11_l1_id;                 /* [nNodes] */
+    const int32_t *net_perm, *from_n, *to_n;  /* [nNodes] (valid 1..nLinks) */
+    const double *length, *slope, *ffp_imp;   /* [nLinks] */
+    const double *rout_param;                 /* [5] */
+    const int32_t *gauge_node;                /* [nGauges] */
+    const double *latitude;                   /* [nCells] degrees */
+} ora_domain;
+
+typedef struct {
+    const double *fSealed, *alpha, *degDayInc, *degDayMax, *degDayNoPre, *fAsp, *HarSamCoeff;
+    const double *karstLoss, *kFastFlow, *kSlowFlow, *kBaseFlow, *kPerco;
+    const double *jarvis_c1, *tempThresh, *unsatThresh, *sealedThresh;
+    const double *maxInter;        /* [12][nCells] (column-major (nCells, 12)) */
+    const double *petLAIcorFactor; /* [12][nCells] or NULL */
+    const double *fRoots, *SMs, *FC, *PW, *beta; /* [nH][nCells] */
+} ora_params;
+
+typedef struct {
+    double *interc, *snowpack, *sealSTW, *SM /*[nH][nCells]*/, *unsat, *sat;
+    double *qTIN, *qTR;   /* [2][nNodes] column-major (nNodes, 2) */
+    double *qOUT, *Qmod;  /* [nNodes] */
+    double *C1, *C2;      /* [nNodes] (links 1..nLinks used) */
+} ora_state;
+
+/* Forcing rows: row r of pre/temp/pet/tmin/tmax is [r][nCells]; the row used at
+ * step tt is iMeteoTS(tt) - forc_row0 (iMeteoTS as in update_timestep, 1-based). */
+typedef struct {
+    const double *pre, *temp, *pet, *tmin, *tmax;
+    int32_t forc_row0;
+    int32_t n_rows;
+} ora_forcing;
+
+/* Run steps tt = tt0 .. tt0+nT-1 (1-based, tt0 >= 1).  Outputs (any may be NULL):
+ * q_gauge[nT][nGauges], total_runoff[nT][nCells], qmod[nT][nNodes].
+ * nthreads <= 0: OpenMP default.  Returns 0 on success. */
+int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
+            int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff, double *qmod,
+            int nthreads);
+
+/* Set the reference's default initial states (mo_init_states.f90:258-345,
+ * mo_mrm_init.f90:453-499).  horizon_depth[nH] in mm. */
+void ora_default_states(const ora_domain *d, const double *horizon_depth, ora_state *s);
+
+/* which elementary-function build this is: 0 = hmath, 1 = libm */
+int ora_math_kind(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,200 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loaded by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
+bench.py -- never by the mhm_gb300 package.  `build()` compiles both variants
+(hmath and libm elementary functions) with the Makefile next to this file.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def build() -> None:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+
+
+class OraDomain(C.Structure):
+    _fields_ = [
+        ("nCells", C.c_int32), ("nH", C.c_int32), ("nNodes", C.c_int32), ("nOutlets", C.c_int32),
+        ("timestep", C.c_int32), ("proc_sm", C.c_int32), ("proc_pet", C.c_int32), ("proc_rout", C.c_int32),
+        ("nTstepForcingDay", C.c_int32), ("read_states", C.c_int32), ("jul_start", C.c_int32),
+        ("map_flag", C.c_int32), ("nGauges", C.c_int32), ("pad_", C.c_int32),
+        ("evap_coeff", _dp), ("fday_prec", _dp), ("fnight_prec", _dp), ("fday_pet", _dp),
+        ("fnight_pet", _dp), ("fday_temp", _dp), ("fnight_temp", _dp),
+        ("l1_area_km2", _dp), ("l1_l11_id", _ip), ("l11_area_km2", _dp), ("l11_l1_id", _ip),
+        ("net_perm", _ip), ("from_n", _ip), ("to_n", _ip), ("length", _dp), ("slope", _dp),
+        ("ffp_imp", _dp), ("rout_param", _dp), ("gauge_node", _ip), ("latitude", _dp),
+    ]
+
+
+PARAM_FIELDS = ["fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "HarSamCoeff",
+                "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco", "jarvis_c1", "tempThresh",
+                "unsatThresh", "sealedThresh", "maxInter", "petLAIcorFactor", "fRoots", "SMs", "FC", "PW",
+                "beta"]
+# mhm_eff_params name -> oracle name
+PARAM_ALIAS = {"jarvis_thresh_c1": "jarvis_c1", "soilMoistSat": "SMs", "soilMoistFC": "FC",
+               "wiltingPoint": "PW", "soilMoistExp": "beta"}
+
+
+class OraParams(C.Structure):
+    _fields_ = [(n, _dp) for n in PARAM_FIELDS]
+
+
+STATE_FIELDS = ["interc", "snowpack", "sealSTW", "SM", "unsat", "sat", "qTIN", "qTR", "qOUT", "Qmod", "C1", "C2"]
+
+
+class OraState(C.Structure):
+    _fields_ = [(n, _dp) for n in STATE_FIELDS]
+
+
+class OraForcing(C.Structure):
+    _fields_ = [("pre", _dp), ("temp", _dp), ("pet", _dp), ("tmin", _dp), ("tmax", _dp),
+                ("forc_row0", C.c_int32), ("n_rows", C.c_int32)]
+
+
+_LIBS: dict[str, C.CDLL] = {}
+
+
+def load(kind: str = "hmath") -> C.CDLL:
+    """kind: 'hmath' (the GPU's elementary functions) or 'libm' (the C library's)."""
+    if kind in _LIBS:
+        return _LIBS[kind]
+    path = BUILD / f"liboracle_{kind}.so"
+    if not path.exists():
+        build()
+    L = C.CDLL(str(path))
+    d = C.c_double
+    L.ora_canopy_interc.argtypes = [d, d, d, _dp, _dp, _dp]
+    L.ora_snow_accum_melt.argtypes = [d, d, d, d, d, d, d, _dp, _dp, _dp, _dp, _dp, _dp]
+    L.ora_feddes_et_reduction.argtypes = [d, d, d, d]
+    L.ora_feddes_et_reduction.restype = d
+    L.ora_jarvis_et_reduction.argtypes = [d, d, d, d, d]
+    L.ora_jarvis_et_reduction.restype = d
+    L.ora_soil_moisture.argtypes = [C.c_int, C.c_int, d, d, d, d, _dp, _dp, _dp, _dp, _dp, d, d, d,
+                                    _dp, _dp, _dp, _dp, _dp, _dp]
+    L.ora_runoff_unsat_zone.argtypes = [d, d, d, d, d, d, d, _dp, _dp, _dp, _dp, _dp]
+    L.ora_runoff_sat_zone.argtypes = [d, _dp, _dp]
+    L.ora_L1_total_runoff.argtypes = [d, d, d, d, d]
+    L.ora_L1_total_runoff.restype = d
+    L.ora_extraterr_rad_approx.argtypes = [C.c_int, d]
+    L.ora_extraterr_rad_approx.restype = d
+    L.ora_pet_hargreaves.argtypes = [d, d, d, d, d, d, C.c_int]
+    L.ora_pet_hargreaves.restype = d
+    for f in ("ora_sat_vap_pressure", "ora_slope_satpressure"):
+        getattr(L, f).argtypes = [d]
+        getattr(L, f).restype = d
+    L.ora_pet_priestly.argtypes = [d, d, d]
+    L.ora_pet_priestly.restype = d
+    L.ora_pet_penman.argtypes = [d, d, d, d, d, d, d]
+    L.ora_pet_penman.restype = d
+    L.ora_disagg_meteo_weights.argtypes = [d, d, d]
+    L.ora_disagg_meteo_weights.restype = d
+    L.ora_disagg_flux_daynight.argtypes = [C.c_int, d, d, d, d]
+    L.ora_disagg_flux_daynight.restype = d
+    L.ora_disagg_state_daynight.argtypes = [C.c_int, d, d, d, d, C.c_int]
+    L.ora_disagg_state_daynight.restype = d
+    L.ora_julday.argtypes = [C.c_int32] * 3
+    L.ora_julday.restype = C.c_int32
+    L.ora_caldat.argtypes = [C.c_int32, _ip, _ip, _ip]
+    L.ora_dec2date.argtypes = [d, _ip, _ip, _ip, _ip, _ip, _ip]
+    L.ora_step_calendar.argtypes = [C.c_int32, C.c_int32, C.c_int32, _ip, _ip, _ip, _ip, _ip]
+    L.ora_reg_rout.argtypes = [_dp, _dp, _dp, _dp, C.c_int, d, _dp, _dp]
+    L.ora_L11_runoff_acc.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _dp, _ip, C.c_int, C.c_int, _dp]
+    L.ora_L11_routing.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp]
+    L.ora_L11_set_network_topology.argtypes = [C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, _ip]
+    L.ora_L11_set_network_topology.restype = C.c_int
+    L.ora_L11_routing_order.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.ora_run.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
+                          C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int]
+    L.ora_default_states.argtypes = [C.POINTER(OraDomain), _dp, C.POINTER(OraState)]
+    L.ora_math_kind.restype = C.c_int
+    _LIBS[kind] = L
+    return L
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+class OracleRun:
+    """The mhm_eval time loop of one basin on the CPU (oracle)."""
+
+    def __init__(self, dom, params: dict, rout_param=None, proc_sm=1, proc_pet=0, proc_rout=1,
+                 hourly=True, read_states=False, kind="hmath"):
+        self.L = load(kind)
+        self.dom = dom
+        self.keep = []
+
+        def k(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dt)
+            self.keep.append(a)
+            return a
+
+        d = OraDomain()
+        d.nCells, d.nH, d.nNodes, d.nOutlets = dom.n_cells, dom.n_horizons, dom.n_nodes, dom.n_outlets
+        d.timestep, d.proc_sm, d.proc_pet, d.proc_rout = dom.timestep, proc_sm, proc_pet, proc_rout
+        d.nTstepForcingDay = 24 if hourly else 1
+        d.read_states = int(read_states)
+        d.jul_start = dom.jul_start
+        d.map_flag = 1
+        d.nGauges = len(dom.gauge_node)
+        for n in ("evap_coeff", "fday_prec", "fnight_prec", "fday_pet", "fnight_pet", "fday_temp", "fnight_temp",
+                  "l11_area_km2", "length", "slope", "ffp_imp", "latitude", "l1_area_km2"):
+            setattr(d, n, _d(k(getattr(dom, n))))
+        for n in ("l1_l11_id", "l11_l1_id", "net_perm", "from_n", "to_n", "gauge_node"):
+            setattr(d, n, _i(k(getattr(dom, n), np.int32)))
+        rp = k(rout_param if rout_param is not None else np.zeros(5))
+        d.rout_param = _d(rp)
+        self.d = d
+        p = OraParams()
+        for name, arr in params.items():
+            oname = PARAM_ALIAS.get(name, name)
+            if oname in PARAM_FIELDS and arr is not None:
+                setattr(p, oname, _d(k(arr)))
+        self.p = p
+        N, H, Ln = dom.n_cells, dom.n_horizons, dom.n_nodes
+        self.state = {"interc": np.zeros(N), "snowpack": np.zeros(N), "sealSTW": np.zeros(N),
+                      "SM": np.zeros(H * N), "unsat": np.zeros(N), "sat": np.zeros(N),
+                      "qTIN": np.zeros(2 * Ln), "qTR": np.zeros(2 * Ln), "qOUT": np.zeros(Ln),
+                      "Qmod": np.zeros(Ln), "C1": np.zeros(Ln), "C2": np.zeros(Ln)}
+        self.s = OraState(**{n: _d(self.state[n]) for n in STATE_FIELDS})
+        hd = k(dom.horizon_depth)
+        self.L.ora_default_states(C.byref(self.d), _d(hd), C.byref(self.s))
+
+    def run(self, forcing: dict, row0: int, tt0: int, n_steps: int, nthreads: int = 0,
+            want_tro: bool = False, want_qmod: bool = False):
+        f = OraForcing()
+        keep = []
+        for n in ("pre", "temp", "pet", "tmin", "tmax"):
+            a = forcing.get(n)
+            if a is not None:
+                a = np.ascontiguousarray(a, np.float64)
+                keep.append(a)
+                setattr(f, n, _d(a))
+        f.forc_row0 = row0
+        f.n_rows = next(a.shape[0] for a in keep)
+        G = len(self.dom.gauge_node)
+        q = np.zeros((n_steps, G))
+        tro = np.zeros((n_steps, self.dom.n_cells)) if want_tro else None
+        qm = np.zeros((n_steps, self.dom.n_nodes)) if want_qmod else None
+        rc = self.L.ora_run(C.byref(self.d), C.byref(self.p), C.byref(self.s), C.byref(f), tt0, n_steps,
+                            _d(q), _d(tro), _d(qm), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"ora_run failed ({rc})")
+        return q, tro, qm
