@@ -20,7 +20,7 @@
 namespace mhm {
 cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
-cudaError_t launch_route_level(const RouteArgs &a, cudaStream_t s);
+cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
 cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
 cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double TS, const double *length,
                             const double *slope, const double *ffp, const int32_t *link_pos, double *C1,
@@ -87,7 +87,7 @@ struct mhm_ctx {
     // device: static
     DevBuf<double> params, states, latitude, l1_area, pos_area, length, slope, ffp, rout_p5;
     DevBuf<double> C1, C2, qtin1, qtr1, qout_last, qmod_last;
-    DevBuf<int32_t> node_cell_ptr, node_cells, pos_l11_l1, up_ptr, up_pos, link_pos, gauge_pos_d;
+    DevBuf<int32_t> node_cell_ptr, node_cells, pos_l11_l1, up_ptr, up_pos, link_pos, gauge_pos_d, pos_level;
     DevBuf<int8_t> pos_flags;
     // device: per run / chunk
     DevBuf<StepInfo> steps;
@@ -107,6 +107,7 @@ struct mhm_ctx {
     int64_t t_launches[4] = {0, 0, 0, 0};
     double t_ms[4] = {0, 0, 0, 0};
     size_t chunk_bytes = (size_t)8 << 30;
+    int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
     std::string err;
 };
 
@@ -334,6 +335,10 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         ok = ok && ck(upload(ctx->pos_l11_l1, pl1.data(), L, ctx->stream), "l11_l1");
         ok = ok && ck(upload(ctx->pos_area, parea.data(), L, ctx->stream), "l11 area");
         if (d->map_flag) ok = ok && ck(upload(ctx->l1_area, d->l1_area_km2, N, ctx->stream), "l1 area");
+        std::vector<int32_t> plev(L, 0);
+        for (int l = 0; l < net.n_levels; ++l)
+            for (int p = net.level_ptr[l]; p < net.level_ptr[l + 1]; ++p) plev[p] = l;
+        ok = ok && ck(upload(ctx->pos_level, plev.data(), L, ctx->stream), "levels");
         ok = ok && ck(upload(ctx->up_ptr, net.up_ptr.data(), L + 1, ctx->stream), "up ptr");
         ok = ok && ck(upload(ctx->up_pos, net.up_pos.data(), net.up_pos.size(), ctx->stream), "up pos");
         ok = ok && ck(upload(ctx->pos_flags, net.pos_flags.data(), L, ctx->stream), "flags");
@@ -359,6 +364,10 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         return MHM_ERR_OOM;
     }
     if (const char *s = std::getenv("MHM_CHUNK_BYTES")) ctx->chunk_bytes = (size_t)std::atoll(s);
+    if (const char *s = std::getenv("MHM_ROUTE_SUB")) {
+        int v = std::atoi(s);
+        if (v >= 1 && v <= 16) ctx->route_sub = v;
+    }
     *out = ctx;
     return MHM_OK;
 }
@@ -669,7 +678,8 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         r.n_nodes = ctx->L;
         r.n_members = ctx->M;
         r.n_steps = nT;
-        r.write_qmod = 1;
+        r.sub = std::min(ctx->route_sub, nT);
+        r.pos_level = ctx->pos_level.p;
         r.up_ptr = ctx->up_ptr.p;
         r.up_pos = ctx->up_pos.p;
         r.pos_flags = ctx->pos_flags.p;
@@ -682,10 +692,15 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         r.qtr1 = ctx->qtr1.p;
         {
             Bracket br(ctx, 2);
-            for (int l = 0; l < ctx->net.n_levels; ++l) {
-                r.lvl_begin = ctx->net.level_ptr[l];
-                r.lvl_end = ctx->net.level_ptr[l + 1];
-                CK(launch_route_level(r, ctx->stream), "route launch");
+            // wavefront: tick k advances sub-chunk k - l of level l
+            const int D = ctx->net.n_levels;
+            const int n_sub = (nT + r.sub - 1) / r.sub;
+            for (int k = 0; k < D + n_sub - 1; ++k) {
+                const int lo = std::max(0, k - n_sub + 1), hi = std::min(k, D - 1);
+                r.tick = k;
+                r.pos_begin = ctx->net.level_ptr[lo];
+                r.pos_end = ctx->net.level_ptr[hi + 1];
+                CK(launch_route_tick(r, ctx->stream), "route launch");
                 g_launches++;
             }
             br.done();
@@ -732,6 +747,14 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
     CK(cudaStreamSynchronize(ctx->stream), "run sync");
     ctx->last_steps = n_steps;
     harvest_timing(ctx);
+    if (ctx->out_qmod) { // routing-level positions -> node order
+        std::vector<double> row(L);
+        for (size_t r = 0; r < M * (size_t)n_steps; ++r) {
+            double *q = ctx->host_qmod.data() + r * L;
+            for (size_t v = 0; v < L; ++v) row[v] = q[ctx->net.pos_of_node[v]];
+            std::memcpy(q, row.data(), L * sizeof(double));
+        }
+    }
     return MHM_OK;
 }
 

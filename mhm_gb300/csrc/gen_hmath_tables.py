@@ -143,6 +143,60 @@ def main():
     for thi, tlo in et:
         print("  %s, %s, \\" % (hexd(thi), hexd(tlo)))
     print("}")
+    fixed_point_tables(lt)
+
+
+def q(v, frac_bits):
+    """Round v * 2^frac_bits to the nearest integer (mpmath)."""
+    return int(mp.nint(mp.mpf(v) * mp.mpf(2) ** frac_bits))
+
+
+def limbs128(n):
+    """Signed 128-bit integer -> (hi as int64 two's complement, lo as uint64)."""
+    n &= (1 << 128) - 1
+    return (n >> 64), n & ((1 << 64) - 1)
+
+
+def fixed_point_tables(lt):
+    """Integer-pipe variants: every quantity as a fixed-point integer.
+    Q116 = signed 128-bit integer scaled by 2^-116, Q64/Q63 = 64-bit."""
+    print("/* ---- fixed-point (integer pipe) log/exp ---- */")
+    ln2 = mp.log(2)
+    hi, lo = limbs128(q(ln2, 116))
+    print("#define HM_FX_LN2_Q116_HI 0x%016xULL" % hi)
+    print("#define HM_FX_LN2_Q116_LO 0x%016xULL" % lo)
+    hi, lo = limbs128(q(ln2 / 128, 116))
+    print("#define HM_FX_LN2N_Q116_HI 0x%016xULL" % hi)
+    print("#define HM_FX_LN2N_Q116_LO 0x%016xULL" % lo)
+    print("#define HM_FX_INVLN2N_Q54 0x%016xULL /* round(128/ln2 * 2^54) */" % q(128 / ln2, 54))
+    # log1p(r) = r * (1 + r * q(r)), q = -1/2 + r/3 - r^2/4 + r^3/5 - r^4/6 + r^5/7 (Q63)
+    for n in range(2, 8):
+        v = q(mp.mpf((-1) ** (n + 1)) / n, 63)
+        print("#define HM_FX_LOG_C%d ((int64_t)0x%016xULL)" % (n, v & ((1 << 64) - 1)))
+    # expm1(r) = r + r^2 * (1/2 + r/6 + r^2/24 + r^3/120 + r^4/720) (Q63)
+    for n in range(2, 7):
+        v = q(1 / mp.factorial(n), 63)
+        print("#define HM_FX_EXP_C%d ((int64_t)0x%016xULL)" % (n, v))
+    # log table: A (invc * 2^9 for z >= 1, invc * 2^8 for z < 1) and -log(invc) in Q116
+    one_idx = None
+    print("/* log: {A, logc Q116 hi, logc Q116 lo} x 256 */")
+    print("#define HM_FX_LOG_TABLE_INIT { \\")
+    for j, (invc, _, _) in enumerate(lt):
+        zlo_bits = OFF + (j << LOG_SHIFT)
+        scale = 9 if (zlo_bits >> 52) >= 0x3FF else 8
+        A = mp.mpf(invc) * mp.mpf(2) ** scale
+        assert A == mp.nint(A), (j, invc)
+        logc = -mp.log(mp.mpf(invc))
+        hi, lo = limbs128(q(logc, 116))
+        print("  0x%016xULL, 0x%016xULL, 0x%016xULL, \\" % (int(A), hi, lo))
+    print("}")
+    print("/* exp: 2^(j/128) in Q63, x 128 */")
+    print("#define HM_FX_EXP_TABLE_INIT { \\")
+    for j in range(128):
+        v = q(mp.mpf(2) ** (mp.mpf(j) / 128), 63)
+        assert v < (1 << 64)
+        print("  0x%016xULL, \\" % v)
+    print("}")
 
 
 if __name__ == "__main__":

@@ -218,8 +218,272 @@ HM_FN double hm_pow_t(double x, double y, const uint64_t *ltab, const uint64_t *
     return hm_exp_dd_t(eh, el, etab);
 }
 
+/* ======================================================================
+ * Integer-pipe variants.  On GB300 the FP64 pipe issues ~0.5 T thread-ops/s
+ * while the integer pipes are tens of times faster, so the same table-driven
+ * reductions are evaluated in 64/128-bit fixed point: log(x) as a Q116
+ * number (k*ln2 + logc exact to 2^-107, log1p of the exact reduced argument
+ * with relative error < 2^-61), exp from a Q64 argument (Taylor expm1 in
+ * Q64, 2^(j/128) in Q63), and one final round-to-nearest-even to double.
+ * No FP64 instruction is used on the main paths.  Accuracy (tests/
+ * test_hmath.py): < 0.51 ulp for log and exp, < 0.6 ulp for pow.
+ * ====================================================================== */
+typedef __int128 hm_i128;
+typedef unsigned __int128 hm_u128;
+
+static const uint64_t hm_fxlog_tab_h[3 * HM_LOG_N] = HM_FX_LOG_TABLE_INIT;
+static const uint64_t hm_fxexp_tab_h[128] = HM_FX_EXP_TABLE_INIT;
+#if defined(__CUDACC__)
+static __device__ const uint64_t hm_fxlog_tab_d[3 * HM_LOG_N] = HM_FX_LOG_TABLE_INIT;
+static __device__ const uint64_t hm_fxexp_tab_d[128] = HM_FX_EXP_TABLE_INIT;
+#endif
+#if defined(__CUDA_ARCH__)
+#define HM_FXLOG_TAB hm_fxlog_tab_d
+#define HM_FXEXP_TAB hm_fxexp_tab_d
+#else
+#define HM_FXLOG_TAB hm_fxlog_tab_h
+#define HM_FXEXP_TAB hm_fxexp_tab_h
+#endif
+
+HM_FN uint64_t hm_umulhi(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((hm_u128)a * b) >> 64);
+#endif
+}
+
+/* floor(a * b / 2^64) for signed a, b */
+HM_FN int64_t hm_smulhi(int64_t a, int64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __mul64hi(a, b);
+#else
+    return (int64_t)(((hm_i128)a * b) >> 64);
+#endif
+}
+
+HM_FN int hm_clz64(uint64_t x) /* x != 0 */
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+
+HM_FN int hm_clz128(hm_u128 x) /* x != 0 */
+{
+    uint64_t hi = (uint64_t)(x >> 64);
+    return hi ? hm_clz64(hi) : 64 + hm_clz64((uint64_t)x);
+}
+
+/* Round mant * 2^(e - 63) (mant in [2^63, 2^64), `sticky` = nonzero bits
+ * below mant) to the nearest double, ties to even; gradual underflow and
+ * overflow to infinity. */
+HM_FN double hm_make_double(int neg, uint64_t mant, int e, int sticky)
+{
+    const uint64_t sign = neg ? 0x8000000000000000ULL : 0;
+    int be = e + 1023;
+    if (be >= 2047)
+        return hm_b2d(sign | 0x7ff0000000000000ULL);
+    int sh = 11;
+    if (be <= 0) {
+        sh = 11 + 1 - be;
+        be = 0;
+        if (sh > 64)
+            return hm_b2d(sign); /* below half the smallest subnormal */
+    }
+    uint64_t m53, rem, half;
+    if (sh == 64) {
+        m53 = 0;
+        rem = mant;
+        half = 0x8000000000000000ULL;
+    } else {
+        m53 = mant >> sh;
+        rem = mant & ((1ULL << sh) - 1);
+        half = 1ULL << (sh - 1);
+    }
+    if (rem > half || (rem == half && (sticky || (m53 & 1))))
+        m53++;
+    const uint64_t bits = (be > 0 ? ((uint64_t)(be - 1) << 52) : 0) + m53;
+    return hm_b2d(sign | bits);
+}
+
+/* log(x) for positive normal-or-subnormal finite x as a Q116 fixed-point
+ * number; also returns log1p of the reduced argument as a floating value
+ * (neg, mant, e) and whether x lies in the two intervals around 1 where
+ * log(x) == log1p(r) (near1).  Caller handles zero / negative / inf / NaN. */
+HM_FN hm_i128 hm_log_fx(uint64_t u, int *near1, int *tneg, uint64_t *tmant, int *te)
+{
+    int64_t kadj = 0;
+    if ((u >> 52) == 0) {
+        /* subnormal u * 2^-1074: shift the leading 1 to bit 52, which reads
+         * as the normal number (u << lz) * 2^-1074 = x * 2^lz */
+        const int lz = hm_clz64(u) - 11;
+        u <<= lz;
+        kadj = -lz;
+    }
+    const uint64_t tmp = u - HM_LOG_OFF;
+    const int64_t k = ((int64_t)tmp >> 52) + kadj;
+    const uint32_t i = (uint32_t)(tmp >> (52 - HM_LOG_NBITS)) & (HM_LOG_N - 1);
+    const uint64_t iz = u - (tmp & 0xfff0000000000000ULL);
+    const uint64_t M = (iz & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t A = HM_FXLOG_TAB[3 * i];
+    const int64_t R = (int64_t)(M * A) - ((int64_t)1 << 61); /* r = z*invc - 1 = R * 2^-61, exact */
+    const hm_i128 logc = (hm_i128)(((hm_u128)HM_FXLOG_TAB[3 * i + 1] << 64) | HM_FXLOG_TAB[3 * i + 2]);
+    *near1 = (k == 0) && (logc == 0);
+    if (R == 0) {
+        *tmant = 0;
+        return (hm_i128)k * (hm_i128)(((hm_u128)HM_FX_LN2_Q116_HI << 64) | HM_FX_LN2_Q116_LO) + logc;
+    }
+    /* log1p(r) = r * (1 + r * q(r)), q in Q63, r in Q64 */
+    const int64_t rq = R * 8;
+    int64_t q = HM_FX_LOG_C7;
+    q = HM_FX_LOG_C6 + hm_smulhi(rq, q);
+    q = HM_FX_LOG_C5 + hm_smulhi(rq, q);
+    q = HM_FX_LOG_C4 + hm_smulhi(rq, q);
+    q = HM_FX_LOG_C3 + hm_smulhi(rq, q);
+    q = HM_FX_LOG_C2 + hm_smulhi(rq, q);
+    const int64_t rqq = hm_smulhi(rq, q);                        /* r*q(r), Q63 */
+    const uint64_t f = (uint64_t)(((int64_t)1 << 62) + (rqq >> 1)); /* 1 + r*q(r), Q62 */
+    const uint64_t aR = (uint64_t)(R < 0 ? -R : R);
+    const int lz = hm_clz64(aR);
+    uint64_t mant = hm_umulhi(aR << lz, f);
+    const int lz2 = hm_clz64(mant);
+    mant <<= lz2;
+    const int e = 4 - lz - lz2; /* |log1p(r)| = mant * 2^(e - 63) */
+    *tneg = R < 0;
+    *tmant = mant;
+    *te = e;
+    /* S = k*ln2 + logc + log1p(r) in Q116 */
+    const int sh = e + 53;
+    hm_i128 tau = sh >= 0 ? (hm_i128)((hm_u128)mant << sh) : (hm_i128)(mant >> (-sh < 64 ? -sh : 63));
+    if (R < 0)
+        tau = -tau;
+    return (hm_i128)k * (hm_i128)(((hm_u128)HM_FX_LN2_Q116_HI << 64) | HM_FX_LN2_Q116_LO) + logc + tau;
+}
+
+/* Q116 -> nearest double */
+HM_FN double hm_q116_to_double(hm_i128 S)
+{
+    if (S == 0)
+        return 0.0;
+    const int neg = S < 0;
+    const hm_u128 a = (hm_u128)(neg ? -S : S);
+    const int lz = hm_clz128(a);
+    const hm_u128 n = a << lz;
+    return hm_make_double(neg, (uint64_t)(n >> 64), 11 - lz, (uint64_t)n != 0);
+}
+
+HM_FN double hm_log_i(double x)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint32_t top = (uint32_t)(u >> 32);
+    if (top >= 0x7ff00000u) { /* +inf, NaN, or negative (sign bit set) */
+        if (u == 0x7ff0000000000000ULL)
+            return x;
+        if ((u << 1) == 0)
+            return -HUGE_VAL; /* -0 */
+        return hm_b2d(0x7ff8000000000000ULL);
+    }
+    if (u == 0)
+        return -HUGE_VAL;
+    int near1, tneg, te;
+    uint64_t tmant;
+    const hm_i128 S = hm_log_fx(u, &near1, &tneg, &tmant, &te);
+    if (near1)
+        return tmant ? hm_make_double(tneg, tmant, te, 0) : 0.0;
+    return hm_q116_to_double(S);
+}
+
+/* exp(X * 2^-64) for a signed Q64 argument */
+HM_FN double hm_exp_q64(hm_i128 X)
+{
+    if (X > ((hm_i128)710 << 64))
+        return HUGE_VAL;
+    if (X < -((hm_i128)746 << 64))
+        return 0.0;
+    const int64_t t = (int64_t)(X >> 12);                     /* Q52 */
+    const int64_t kq = hm_smulhi(t, (int64_t)HM_FX_INVLN2N_Q54); /* x*128/ln2 in Q42 */
+    const int64_t k = (kq + ((int64_t)1 << 41)) >> 42;
+    const hm_i128 ln2n = (hm_i128)(((hm_u128)HM_FX_LN2N_Q116_HI << 64) | HM_FX_LN2N_Q116_LO);
+    const int64_t r = (int64_t)(X - (((hm_i128)k * ln2n) >> 52)); /* Q64, |r| < 2^-7 */
+    int64_t q = HM_FX_EXP_C6;
+    q = HM_FX_EXP_C5 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C4 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C3 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C2 + hm_smulhi(r, q);                       /* Q63 */
+    const int64_t r2 = hm_smulhi(r, r);                       /* Q64 */
+    const int64_t p = r + hm_smulhi(r2, q) * 2;               /* expm1(r), Q64 */
+    const uint64_t T = HM_FXEXP_TAB[(uint32_t)k & 127u];      /* 2^(j/128), Q63 */
+    const uint64_t tp = hm_umulhi(T, (uint64_t)(p < 0 ? -p : p));
+    uint64_t y = p < 0 ? T - tp : T + tp;                     /* Q63 */
+    int e = (int)(k >> 7);
+    if (!(y >> 63)) {
+        y <<= 1;
+        e -= 1;
+    }
+    return hm_make_double(0, y, e, 0);
+}
+
+HM_FN double hm_exp_i(double x)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint64_t a = u & 0x7fffffffffffffffULL;
+    if (a >= 0x4087500000000000ULL) { /* |x| >= 746, inf or NaN */
+        if (a > 0x7ff0000000000000ULL)
+            return x;
+        return (u >> 63) ? 0.0 : HUGE_VAL;
+    }
+    const int e = (int)(a >> 52) - 1023;
+    const uint64_t M = (a & 0x000fffffffffffffULL) | (a >> 52 ? 0x0010000000000000ULL : 0);
+    hm_i128 X;
+    if (e + 12 >= 0)
+        X = (hm_i128)((hm_u128)M << (e + 12));
+    else
+        X = (hm_i128)(e + 12 > -64 ? (M >> (-(e + 12))) : 0);
+    return hm_exp_q64((u >> 63) ? -X : X);
+}
+
+/* x**y for x >= 0 (Fortran real**real): exp(y * log(x)) with log kept in
+ * fixed point (no rounding of the intermediate). */
+HM_FN double hm_pow_i(double x, double y)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint64_t uy = hm_d2b(y);
+    const uint64_t ay = uy & 0x7fffffffffffffffULL;
+    if (ay == 0 || u == 0x3ff0000000000000ULL)
+        return 1.0;
+    const int ey = (int)(ay >> 52) - 1023;
+    if (u - 1 >= 0x7fefffffffffffffULL || ey > 40) {
+        /* x zero, negative, inf or NaN, or |y| >= 2^41 (inf/NaN included):
+         * the exp(y * log(x)) definition in FP64 */
+        return hm_exp_t(y * hm_log_t(x, HM_LOG_TAB), HM_EXP_TAB);
+    }
+    int near1, tneg, te;
+    uint64_t tmant;
+    const hm_i128 S = hm_log_fx(u, &near1, &tneg, &tmant, &te) >> 52; /* Q64, |S| < 2^74 */
+    const uint64_t My = (ay & 0x000fffffffffffffULL) | (ay >> 52 ? 0x0010000000000000ULL : 0);
+    const int neg = (S < 0) != (int)(uy >> 63);
+    const hm_u128 aS = (hm_u128)(S < 0 ? -S : S);
+    /* aS * My < 2^74 * 2^53: fits in 127 bits */
+    const hm_u128 prod = ((hm_u128)((uint64_t)(aS >> 64) * My) << 64) +
+                         (((hm_u128)hm_umulhi((uint64_t)aS, My) << 64) | (uint64_t)((uint64_t)aS * My));
+    const int sh = 52 - ey; /* >= 12 */
+    const hm_i128 P = (hm_i128)(sh < 127 ? prod >> sh : 0);
+    return hm_exp_q64(neg ? -P : P);
+}
+
+#ifndef HM_FP64_MATH
+HM_FN double hm_log(double x) { return hm_log_i(x); }
+HM_FN double hm_exp(double x) { return hm_exp_i(x); }
+HM_FN double hm_pow(double x, double y) { return hm_pow_i(x, y); }
+#else
 HM_FN double hm_log(double x) { return hm_log_t(x, HM_LOG_TAB); }
 HM_FN double hm_exp(double x) { return hm_exp_t(x, HM_EXP_TAB); }
 HM_FN double hm_pow(double x, double y) { return hm_pow_t(x, y, HM_LOG_TAB, HM_EXP_TAB); }
+#endif
 
 #endif /* MHM_HMATH_H */

@@ -81,10 +81,14 @@ struct AccArgs {
     double *qout;                 // [M][n_steps][n_nodes] by level position
 };
 
+// Wavefront routing: the chunk is cut into sub-chunks of `sub` steps; launch
+// `tick` advances sub-chunk (tick - level) of every node whose level is in
+// [lvl_lo, lvl_hi] (positions pos_begin .. pos_end-1).
 struct RouteArgs {
     int32_t n_nodes, n_members, n_steps;
-    int32_t lvl_begin, lvl_end; // positions of this level
-    int32_t write_qmod;
+    int32_t pos_begin, pos_end;
+    int32_t tick, sub;
+    const int32_t *pos_level;   // [n_nodes] topological level of each position
     const int32_t *up_ptr;      // [n_nodes+1]
     const int32_t *up_pos;      // upstream positions in rank order
     const int8_t *pos_flags;    // bit0: is link (has C1/C2), bit1: add qOUT

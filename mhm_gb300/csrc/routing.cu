@@ -44,38 +44,61 @@ __global__ void __launch_bounds__(256) runoff_acc_kernel(const AccArgs a)
     a.qout[((size_t)m * a.n_steps + t) * L + pos] = q;
 }
 
-// One topological level: each (member, node) of the level advances through
-// the chunk.  L11_routing body, src/mRM/mo_mrm_routing.f90:435-478.
-__global__ void __launch_bounds__(128) route_level_kernel(const RouteArgs a)
+// One wavefront tick: each (member, node) of the active levels advances its
+// sub-chunk (tick - level) of `sub` <= SUB steps.  L11_routing body,
+// src/mRM/mo_mrm_routing.f90:435-478.  Inflow sums keep the reference order:
+// per step, ((0 + qTR(up_1)) + qTR(up_2) + ...) + qOUT, upstream links in
+// netPerm rank order; the upstream series of the whole sub-chunk are loaded
+// first (independent loads), then the Muskingum recurrence runs.
+template <int SUB>
+__global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
 {
-    const int width = a.lvl_end - a.lvl_begin;
+    const int width = a.pos_end - a.pos_begin;
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)width * a.n_members) return;
     const int m = (int)(gid / width);
-    const int pos = a.lvl_begin + (int)(gid - (int64_t)m * width);
+    const int pos = a.pos_begin + (int)(gid - (int64_t)m * width);
+    const int s = a.tick - __ldg(a.pos_level + pos);
+    const int t0 = s * a.sub;
+    if (s < 0 || t0 >= a.n_steps) return;
+    const int nt = min(a.sub, a.n_steps - t0);
     const int64_t L = a.n_nodes;
     const size_t ms = (size_t)m * L;
-    const size_t series = (size_t)m * a.n_steps * L;
+    const size_t base = ((size_t)m * a.n_steps + t0) * L; // row t0 of member m
     const int ub = __ldg(a.up_ptr + pos), ue = __ldg(a.up_ptr + pos + 1);
     const int flags = __ldg(a.pos_flags + pos);
     const bool is_link = flags & 1;
     const bool add_qout = flags & 2;
-    const double c1 = is_link ? __ldg(a.C1 + ms + pos) : 0.0;
-    const double c2 = is_link ? __ldg(a.C2 + ms + pos) : 0.0;
+    double qtin[SUB];
+#pragma unroll
+    for (int t = 0; t < SUB; ++t) qtin[t] = 0.0; // netNode_qTIN(:, IT) = 0
+    for (int j = ub; j < ue; ++j) {
+        const double *up = a.qtr + base + __ldg(a.up_pos + j);
+#pragma unroll
+        for (int t = 0; t < SUB; ++t)
+            if (t < nt) qtin[t] = qtin[t] + __ldcg(up + (size_t)t * L);
+    }
+    if (add_qout) {
+#pragma unroll
+        for (int t = 0; t < SUB; ++t)
+            if (t < nt) qtin[t] = qtin[t] + __ldcg(a.qout + base + (size_t)t * L + pos);
+    }
     double qtin1 = a.qtin1[ms + pos];
     double qtr1 = a.qtr1[ms + pos];
-    for (int t = 0; t < a.n_steps; ++t) {
-        const size_t row = series + (size_t)t * L;
-        double qtin = 0.0; // netNode_qTIN(:, IT) = 0
-        for (int j = ub; j < ue; ++j) qtin = qtin + a.qtr[row + __ldg(a.up_pos + j)];
-        if (add_qout) qtin = qtin + __ldg(a.qout + row + pos);
-        if (is_link) {
-            double qtr = qtr1 + c1 * (qtin1 - qtr1) + c2 * (qtin - qtin1);
-            a.qtr[row + pos] = qtr;
-            qtr1 = qtr;
+    const double c1 = is_link ? __ldg(a.C1 + ms + pos) : 0.0;
+    const double c2 = is_link ? __ldg(a.C2 + ms + pos) : 0.0;
+#pragma unroll
+    for (int t = 0; t < SUB; ++t) {
+        if (t < nt) {
+            const size_t row = base + (size_t)t * L;
+            if (is_link) {
+                const double qtr = qtr1 + c1 * (qtin1 - qtr1) + c2 * (qtin[t] - qtin1);
+                a.qtr[row + pos] = qtr;
+                qtr1 = qtr;
+            }
+            qtin1 = qtin[t];
+            a.qmod[row + pos] = 0.0 + qtin[t]; // L11_qMod = (0 + Qmod) / real(rout_loop = 1)
         }
-        qtin1 = qtin;
-        a.qmod[row + pos] = 0.0 + qtin; // L11_qMod = (0 + Qmod) / real(rout_loop = 1)
     }
     a.qtin1[ms + pos] = qtin1;
     a.qtr1[ms + pos] = qtr1;
@@ -124,11 +147,15 @@ cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_route_level(const RouteArgs &a, cudaStream_t s)
+cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s)
 {
-    const int64_t n = (int64_t)(a.lvl_end - a.lvl_begin) * a.n_members;
+    const int64_t n = (int64_t)(a.pos_end - a.pos_begin) * a.n_members;
     if (n == 0) return cudaSuccess;
-    route_level_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    const unsigned grid = (unsigned)((n + 127) / 128);
+    if (a.sub <= 4) route_tick_kernel<4><<<grid, 128, 0, s>>>(a);
+    else if (a.sub <= 8) route_tick_kernel<8><<<grid, 128, 0, s>>>(a);
+    else if (a.sub <= 16) route_tick_kernel<16><<<grid, 128, 0, s>>>(a);
+    else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
