@@ -14,6 +14,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "fp64i.h"
 #include "hmath.h"
 #include "mhm_kernels.cuh"
 
@@ -126,6 +127,9 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
     for (int h = 0; h < H; ++h) c.sm[h] = a.reset_sm ? 0.5 * c.fc[h] : S[(size_t)(S_SM + h) * N];
 
     const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
+    const bool sealed = c.fsealed > 0.0;           // frac_sealed > 0 (parameter only)
+    const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
+    const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
     int cur_month = -1;
     double imax = 0.0, petlai = 0.0;
     int cur_doy = -1;
@@ -178,16 +182,17 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
         double throughfall, aet_can;
         {
             double aux = c.interc + prec;
-            if (aux >= imax) {
+            if (hm_ge(aux, imax)) {
                 throughfall = aux - imax;
                 c.interc = imax;
             } else {
                 throughfall = 0.0;
                 c.interc = aux;
             }
-            aet_can = (imax > kEps) ? pet * hm_pow(c.interc / imax, kTwoThird) : 0.0;
-            if (aet_can < 0.0) aet_can = 0.0;
-            if (c.interc > aet_can) {
+            aet_can = hm_gt(imax, kEps) ? pet * hm_pow(hm_div(c.interc, imax), kTwoThird) : 0.0;
+            // a negative storage gives pow() = NaN: these two tests keep IEEE NaN semantics
+            if (hm_lt_ieee(aet_can, 0.0)) aet_can = 0.0;
+            if (hm_gt_ieee(c.interc, aet_can)) {
                 c.interc = c.interc - aet_can;
             } else {
                 aet_can = c.interc;
@@ -197,15 +202,15 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
         // ---- snow_accum_melt, mo_snow_accum_melt.f90:70-158 ----
         double prec_effect;
         {
-            const bool warm = temp > c.tthresh;
+            const bool warm = hm_gt(temp, c.tthresh);
             double rain = warm ? throughfall : 0.0;
             double snowf = warm ? 0.0 : throughfall;
-            double dd = (prec <= c.dd_thr) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
+            double dd = (dd_thr_ok && hm_le(prec, c.dd_thr)) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
             double melt;
             if (warm) {
-                if (c.snow > 0.0) {
+                if (hm_gt0(c.snow)) {
                     double aux = dd * (temp - c.tthresh);
-                    if (aux > c.snow) {
+                    if (hm_gt(aux, c.snow)) {
                         melt = c.snow;
                         c.snow = 0.0;
                     } else {
@@ -226,9 +231,9 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
         double runoff_sealed = 0.0;
         double infil_last;
         {
-            if (c.fsealed > 0.0) {
+            if (sealed) {
                 double tmp = c.seal + prec_effect;
-                if (tmp > c.sthresh) {
+                if (hm_gt(tmp, c.sthresh)) {
                     runoff_sealed = tmp - c.sthresh;
                     c.seal = c.sthresh;
                 } else {
@@ -236,13 +241,13 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
                     c.seal = tmp;
                 }
                 double aet_sealed;
-                if (c.sthresh > kEps) {
-                    aet_sealed = (pet / a.tab.evap[month - 1] - aet_can) * (c.seal / c.sthresh);
-                    if (aet_sealed < 0.0) aet_sealed = 0.0;
+                if (sthresh_pos) {
+                    aet_sealed = (hm_div(pet, a.tab.evap[month - 1]) - aet_can) * hm_div(c.seal, c.sthresh);
+                    if (hm_lt0(aet_sealed)) aet_sealed = 0.0;
                 } else {
                     aet_sealed = DBL_MAX;
                 }
-                if (c.seal > aet_sealed) {
+                if (hm_gt(c.seal, aet_sealed)) {
                     c.seal = c.seal - aet_sealed;
                 } else {
                     c.seal = 0.0;
@@ -255,12 +260,13 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
             for (int h = 0; h < H; ++h) {
                 const double pin = infil;
                 double smh = c.sm[h];
-                if (smh > c.sms[h]) {
+                if (hm_gt(smh, c.sms[h])) {
                     infil = pin;
                 } else {
-                    double frac_runoff = (smh > kEps) ? hm_exp(c.beta[h] * hm_log(smh / c.sms[h])) : 0.0;
+                    double frac_runoff =
+                        hm_gt(smh, kEps) ? hm_exp(c.beta[h] * hm_log(hm_div(smh, c.sms[h]))) : 0.0;
                     double tmp = pin * (1.0 - frac_runoff);
-                    if ((smh + tmp) > c.sms[h]) {
+                    if (hm_gt(smh + tmp, c.sms[h])) {
                         infil = pin + (smh - c.sms[h]);
                         smh = c.sms[h];
                     } else {
@@ -272,28 +278,28 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
                 if (h != 0) aet = aet - aet_above;
                 double stress;
                 if (feddes) {
-                    if (smh >= c.fc[h]) stress = c.froots[h];
-                    else if (smh > c.pw[h]) stress = c.froots[h] * (smh - c.pw[h]) / c.fc_pw[h];
+                    if (hm_ge(smh, c.fc[h])) stress = c.froots[h];
+                    else if (hm_gt(smh, c.pw[h])) stress = hm_div(c.froots[h] * (smh - c.pw[h]), c.fc_pw[h]);
                     else stress = 0.0;
                 } else {
-                    double th = (smh - c.pw[h]) / c.sat_pw[h];
-                    if (th < 0.0) th = 0.0;
-                    if (th > 1.0) th = 1.0;
-                    if (th >= c.jarvis) stress = c.froots[h];
-                    else if (th < c.jarvis) stress = c.froots[h] * (th / c.jarvis);
+                    double th = hm_div(smh - c.pw[h], c.sat_pw[h]);
+                    if (hm_lt0(th)) th = 0.0;
+                    if (hm_gt(th, 1.0)) th = 1.0;
+                    if (hm_ge(th, c.jarvis)) stress = c.froots[h];
+                    else if (hm_lt(th, c.jarvis)) stress = c.froots[h] * hm_div(th, c.jarvis);
                     else stress = 0.0;
                 }
                 aet = aet * stress;
-                if (aet < 0.0) aet = 0.0;
-                if (smh > aet) {
+                if (hm_lt0(aet)) aet = 0.0;
+                if (hm_gt(smh, aet)) {
                     smh = smh - aet;
                 } else {
                     aet = smh - kEps;
                     smh = kEps;
                 }
-                if (smh < kEps) smh = kEps;
+                if (hm_lt(smh, kEps)) smh = kEps;
                 c.sm[h] = smh;
-                if (aet > 0.0) aet_above = aet_above + aet;
+                if (hm_gt0(aet)) aet_above = aet_above + aet;
             }
             infil_last = infil;
         }
@@ -301,20 +307,20 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
         double fast = 0.0, slow = 0.0, base;
         {
             c.unsat = c.unsat + infil_last;
-            if (c.unsat > c.uthresh) {
+            if (hm_gt(c.unsat, c.uthresh)) {
                 double x = c.k0s * (c.unsat - c.uthresh);
                 double y = c.unsat - kEps;
-                fast = (x < y) ? x : y;
+                fast = hm_lt(x, y) ? x : y;
             }
             c.unsat = c.unsat - fast;
-            if (c.unsat > kEps) {
+            if (hm_gt(c.unsat, kEps)) {
                 double x = c.k1s * hm_pow(c.unsat, c.alpha1);
                 double y = c.unsat - kEps;
-                slow = (x < y) ? x : y;
+                slow = hm_lt(x, y) ? x : y;
             }
             c.unsat = c.unsat - slow;
             double perc = c.kps * c.unsat;
-            if (c.unsat > perc) {
+            if (hm_gt(c.unsat, perc)) {
                 c.unsat = c.unsat - perc;
                 c.sat = c.sat + perc * c.karst;
             } else {
@@ -323,7 +329,7 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
             }
         }
         // ---- runoff_sat_zone, mo_runoff.f90:191-212 ----
-        if (c.sat > 0.0) {
+        if (hm_gt0(c.sat)) {
             base = c.k2s * c.sat;
             c.sat = c.sat - base;
         } else {

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "fp64i.h"
 #include "hmath.h"
 #include "mhm_gpu.h"
 #include "mhm_kernels.cuh"
@@ -918,10 +919,10 @@ int mhm_host_free(void *ptr)
 
 int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const double *y, double *out)
 {
-    if (op < 0 || op > 2 || n < 0 || !x || !out || (op == 2 && !y)) return MHM_ERR_INVALID;
+    if (op < 0 || op > 3 || n < 0 || !x || !out || (op >= 2 && !y)) return MHM_ERR_INVALID;
     if (where == 0) {
         for (int64_t i = 0; i < n; ++i)
-            out[i] = op == 0 ? hm_log(x[i]) : op == 1 ? hm_exp(x[i]) : hm_pow(x[i], y[i]);
+            out[i] = op == 0 ? hm_log(x[i]) : op == 1 ? hm_exp(x[i]) : op == 2 ? hm_pow(x[i], y[i]) : hm_div(x[i], y[i]);
         return MHM_OK;
     }
     double *dx = nullptr, *dy = nullptr, *dout = nullptr;
@@ -932,12 +933,12 @@ int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const 
     };
     size_t bytes = (size_t)n * sizeof(double);
     if (cudaMalloc(&dx, bytes) != cudaSuccess || cudaMalloc(&dout, bytes) != cudaSuccess ||
-        (op == 2 && cudaMalloc(&dy, bytes) != cudaSuccess)) {
+        (op >= 2 && cudaMalloc(&dy, bytes) != cudaSuccess)) {
         cleanup();
         return MHM_ERR_OOM;
     }
     cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice);
-    if (op == 2) cudaMemcpy(dy, y, bytes, cudaMemcpyHostToDevice);
+    if (op >= 2) cudaMemcpy(dy, y, bytes, cudaMemcpyHostToDevice);
     cudaError_t e = launch_hmath_eval(op, n, dx, dy, dout, 0);
     g_launches++;
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);

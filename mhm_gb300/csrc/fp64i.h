@@ -1,0 +1,125 @@
+/*
+ * fp64i.h -- IEEE-754 double comparisons and division on the integer pipe.
+ *
+ * GB300's FP64 pipe issues ~0.5 T thread-ops/s, and a double compare (DSETP)
+ * or the refinement steps of a double division occupy it like an FMA; the
+ * integer pipes are tens of times faster.  These functions return exactly
+ * what the IEEE operations return (round-to-nearest-even), so kernels that
+ * use them stay bit-identical to host code using plain C operators.
+ *
+ * Comparisons: hm_gt/ge/lt/le follow IEEE for all non-NaN operands (+0 == -0,
+ * infinities ordered); the *_ieee variants are also false for NaN operands.
+ * Division: hm_div(a, b) == a / b for all inputs; normal/zero operands with a
+ * normal result take the integer path (float reciprocal seed, two Newton
+ * steps in 64-bit fixed point, exact remainder correction, RNE); everything
+ * else (subnormal, infinite, NaN, zero divisor, out-of-range results) uses
+ * the native division.
+ */
+#ifndef MHM_FP64I_H
+#define MHM_FP64I_H
+
+#include "hmath.h"
+
+/* order key: monotone in the value for non-NaN doubles, +0 and -0 -> 0 */
+HM_FN int64_t hm_okey(double x)
+{
+    const int64_t b = (int64_t)hm_d2b(x);
+    const int64_t m = b & 0x7fffffffffffffffLL;
+    return b < 0 ? -m : m;
+}
+HM_FN int hm_isnan_i(double x) { return (hm_d2b(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
+HM_FN int hm_gt(double a, double b) { return hm_okey(a) > hm_okey(b); }
+HM_FN int hm_ge(double a, double b) { return hm_okey(a) >= hm_okey(b); }
+HM_FN int hm_lt(double a, double b) { return hm_okey(a) < hm_okey(b); }
+HM_FN int hm_le(double a, double b) { return hm_okey(a) <= hm_okey(b); }
+HM_FN int hm_gt_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(b) && hm_gt(a, b); }
+HM_FN int hm_lt_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(b) && hm_lt(a, b); }
+/* x > 0, x < 0 against the constant zero */
+HM_FN int hm_gt0(double x) { return hm_okey(x) > 0; }
+HM_FN int hm_lt0(double x) { return hm_okey(x) < 0; }
+/* min/max with the selection rules of the reference's (a < b ? a : b) */
+HM_FN double hm_min_sel(double a, double b) { return hm_lt(a, b) ? a : b; }
+
+/* reciprocal seed 1/x in float, correctly rounded on host and device */
+HM_FN float hm_frcp(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+
+HM_FN uint32_t hm_f2b(float f)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint32_t)__float_as_uint(f);
+#else
+    uint32_t b;
+    memcpy(&b, &f, sizeof b);
+    return b;
+#endif
+}
+
+/* a / b, correctly rounded */
+HM_FN double hm_div(double a, double b)
+{
+    const uint64_t ua = hm_d2b(a), ub = hm_d2b(b);
+    const uint32_t eaf = (uint32_t)(ua >> 52) & 0x7ffu, ebf = (uint32_t)(ub >> 52) & 0x7ffu;
+    const uint64_t sign = (ua ^ ub) & 0x8000000000000000ULL;
+    if (ebf - 1u >= 0x7feu || (eaf - 1u >= 0x7feu && (ua << 1) != 0))
+        return a / b; /* b zero/subnormal/inf/NaN, or a subnormal/inf/NaN */
+    if ((ua << 1) == 0)
+        return hm_b2d(sign); /* +-0 / normal */
+    uint64_t Ma = (ua & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t Mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    int e = (int)eaf - (int)ebf; /* unbiased exponent of the quotient */
+    if (Ma < Mb) {
+        Ma <<= 1;
+        e -= 1;
+    }
+    if (e > 1023 || e < -1022)
+        return a / b; /* overflow or subnormal result: native path */
+    uint64_t Q;
+    hm_i128 R;
+    if (Mb == 0x0010000000000000ULL) { /* b is a power of two: exact */
+        Q = Ma << 2;
+        R = 0;
+    } else {
+        /* inv ~ 2^116 / Mb < 2^64: float seed (~24 bits), then two Newton
+         * steps y' = y (2 - Mb y / 2^116), which approach from below */
+        const float fy = hm_frcp((float)(uint32_t)(Mb >> 29)); /* in (2^-24, 2^-23] */
+        const uint32_t fb = hm_f2b(fy);
+        const int sh = (int)((fb >> 23) & 0xffu) - 127 - 23 + 116 - 29; /* 40 or 41 */
+        const uint64_t fm = (uint64_t)((fb & 0x7fffffu) | 0x800000u);
+        uint64_t inv = (sh >= 41 && fm == 0x800000u) ? 0xffffffffffffffffULL : fm << sh;
+        for (int it = 0; it < 2; ++it) {
+            const hm_u128 t = (hm_u128)Mb * inv;
+            const hm_i128 err = (hm_i128)(((hm_u128)1 << 116) - t); /* |err| < 2^94 */
+            const int64_t err_s = (int64_t)(err >> 52);
+            inv = inv + (uint64_t)(hm_smulhi((int64_t)(inv >> 1), err_s) * 2);
+        }
+        /* Q ~ floor(Ma * 2^54 / Mb) in [2^54, 2^55), then exact remainder correction */
+        Q = (uint64_t)(((hm_u128)Ma * inv) >> 62);
+        R = (hm_i128)(((hm_u128)Ma << 54) - (hm_u128)Q * Mb);
+        for (int c = 0; c < 3; ++c) {
+            if (R < 0) {
+                Q -= 1;
+                R += (hm_i128)Mb;
+            } else if (R >= (hm_i128)Mb) {
+                Q += 1;
+                R -= (hm_i128)Mb;
+            }
+        }
+    }
+    /* round Q (55 bits: 53 + guard + round) to nearest even */
+    uint64_t m53 = Q >> 2;
+    const uint32_t g = (uint32_t)(Q & 3u);
+    const int sticky = R != 0;
+    if (g > 2 || (g == 2 && (sticky || (m53 & 1))))
+        m53++;
+    /* m53 in [2^52, 2^53]; a carry to 2^53 moves into the exponent field */
+    return hm_b2d(sign | (((uint64_t)(e + 1022) << 52) + m53));
+}
+
+#endif /* MHM_FP64I_H */

@@ -3,6 +3,7 @@
 // FP64 issue-rate probe (the FP64 roofline denominator).
 #include <cstdint>
 
+#include "fp64i.h"
 #include "hmath.h"
 
 namespace mhm {
@@ -12,7 +13,7 @@ __global__ void hmath_eval_kernel(int op, int64_t n, const double *x, const doub
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double v = x[i];
-    out[i] = op == 0 ? hm_log(v) : op == 1 ? hm_exp(v) : hm_pow(v, y[i]);
+    out[i] = op == 0 ? hm_log(v) : op == 1 ? hm_exp(v) : op == 2 ? hm_pow(v, y[i]) : hm_div(v, y[i]);
 }
 
 // 8 independent DFMA chains per thread keep the FP64 pipe busy; the result is

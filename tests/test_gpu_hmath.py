@@ -35,7 +35,9 @@ def _inputs(n=1 << 20, seed=0):
 
 def test_device_equals_host(lib):
     x, e, y = _inputs()
-    for op, arg, yy in ((0, x, None), (1, e, None), (2, np.abs(x) % 1000.0, y)):
+    xp = np.where(np.isfinite(x), np.abs(x), 1.0) % 1000.0
+    b = np.random.default_rng(9).integers(0, 2**64, len(x), dtype=np.uint64).view(np.float64)
+    for op, arg, yy in ((0, x, None), (1, e, None), (2, xp, y), (3, x, b)):
         d = _eval(lib, op, 1, arg, yy)
         h = _eval(lib, op, 0, arg, yy)
         same = (d.view(np.uint64) == h.view(np.uint64)) | (np.isnan(d) & np.isnan(h))
