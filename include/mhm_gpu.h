@@ -158,6 +158,14 @@ int mhm_set_forcing(mhm_ctx *ctx, int32_t kind, int32_t row0, int32_t n_rows, co
  * mRM_runoff(step, gauge) of the reference).  Blocks until done. */
 int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
 
+/* Asynchronous variant: enqueue the steps and return; the routing of one call
+ * overlaps the cell chain of the next.  q_gauge and host forcing must stay
+ * valid until mhm_sync returns; state access and the set-up calls
+ * synchronise first.  Per-step outputs (mhm_enable_outputs) need mhm_run. */
+int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
+/* Wait for all enqueued work of the context. */
+int mhm_sync(mhm_ctx *ctx);
+
 /* Per-step L1 total runoff [mm TS-1] and L11 discharge of the last mhm_run:
  * optional outputs enabled before the run (adds HBM traffic). */
 int mhm_enable_outputs(mhm_ctx *ctx, int32_t total_runoff, int32_t qmod);

@@ -66,7 +66,7 @@ EXPORTS = [
     "mhm_set_routing_params", "mhm_init_states", "mhm_set_forcing", "mhm_run", "mhm_enable_outputs",
     "mhm_get_outputs", "mhm_get_state", "mhm_set_state", "mhm_get_var", "mhm_set_timing",
     "mhm_get_timing", "mhm_host_alloc", "mhm_host_free", "mhm_version", "mhm_kernel_launch_count",
-    "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar",
+    "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar", "mhm_run_async", "mhm_sync",
 ]
 
 _LIB = None
@@ -99,6 +99,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_init_states.argtypes = [vp, C.c_int32, _dp]
     L.mhm_set_forcing.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
     L.mhm_run.argtypes = [vp, C.c_int32, C.c_int32, _dp]
+    L.mhm_run_async.argtypes = [vp, C.c_int32, C.c_int32, _dp]
+    L.mhm_sync.argtypes = [vp]
     L.mhm_enable_outputs.argtypes = [vp, C.c_int32, C.c_int32]
     L.mhm_get_outputs.argtypes = [vp, _dp, _dp]
     L.mhm_get_state.argtypes = [vp, C.c_int32, C.POINTER(Restart)]

@@ -41,7 +41,8 @@ def _flags(verbose_ptxas: bool) -> list[str]:
     ]
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
-    return f
+    extra = os.environ.get("MHM_NVCC_FLAGS", "").split()
+    return f + extra
 
 
 def _stale() -> bool:

@@ -14,6 +14,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "calendar.h"
 #include "fp64i.h"
 #include "hmath.h"
 #include "mhm_kernels.cuh"
@@ -58,19 +59,22 @@ __device__ double pet_hargreaves(double coeff, double tavg, double tmax, double 
     return coeff * rad * (tavg + kHarSamConst) * sqrt(delta_temp);
 }
 
-template <int H>
+// Per-thread scalars live in registers; the per-horizon parameters and soil
+// moisture live in shared memory, [plane][H][blockDim] (consecutive threads
+// -> consecutive words), so the horizon loop stays rolled: fewer registers
+// (more warps per SM) and a smaller instruction footprint.
 struct CellRegs {
     // states
-    double interc, snow, seal, unsat, sat, sm[H];
+    double interc, snow, seal, unsat, sat;
     // parameters (and parameter-only derived values)
-    double fsealed, one_minus_fsealed_unused;
+    double fsealed;
     double ddinc, ddmax_s, ddnopre_s, dd_thr;
     double tthresh, sthresh, uthresh, karst, alpha1;
     double k0s, k1s, k2s, kps; // c2TSTu / k
     double jarvis;
     double fasp, harsam, lat_rad;
-    double sms[H], froots[H], fc[H], pw[H], beta[H], fc_pw[H], sat_pw[H];
 };
+enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_DEN, HS_SM, HS_PLANES };
 
 } // namespace
 
@@ -88,7 +92,11 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
     double *S = a.states + (size_t)m * ns * N + k;
     auto par = [&](int plane) { return __ldg(P + (size_t)plane * N); };
 
-    CellRegs<H> c;
+    extern __shared__ double hsm[];
+    const int tb = threadIdx.x, B = blockDim.x;
+    auto hs = [&](int plane, int h) -> double & { return hsm[(plane * H + h) * B + tb]; };
+    const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
+    CellRegs c;
     const double c2 = a.c2TSTu;
     c.fsealed = par(P_FSEALED);
     c.ddinc = par(P_DDINC);
@@ -108,25 +116,25 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
     c.fasp = par(P_FASP);
     c.harsam = par(P_HARSAM);
     c.lat_rad = (a.proc_pet == 1) ? kDeg2Rad * __ldg(a.latitude + k) : 0.0;
-#pragma unroll
+#pragma unroll 1
     for (int h = 0; h < H; ++h) {
-        c.froots[h] = par(P_HORIZON + h);
-        c.sms[h] = par(P_HORIZON + H + h);
-        c.fc[h] = par(P_HORIZON + 2 * H + h);
-        c.pw[h] = par(P_HORIZON + 3 * H + h);
-        c.beta[h] = par(P_HORIZON + 4 * H + h);
-        c.fc_pw[h] = c.fc[h] - c.pw[h];   // feddes denominator, mo_soil_moisture.f90:358
-        c.sat_pw[h] = c.sms[h] - c.pw[h]; // jarvis denominator, mo_soil_moisture.f90:435
+        const double fr = par(P_HORIZON + h), sms = par(P_HORIZON + H + h), fc = par(P_HORIZON + 2 * H + h);
+        const double pw = par(P_HORIZON + 3 * H + h);
+        hs(HS_FROOTS, h) = fr;
+        hs(HS_SMS, h) = sms;
+        hs(HS_FC, h) = fc;
+        hs(HS_PW, h) = pw;
+        hs(HS_BETA, h) = par(P_HORIZON + 4 * H + h);
+        // feddes denominator FC-PW (mo_soil_moisture.f90:358), jarvis SMs-PW (:435)
+        hs(HS_DEN, h) = feddes ? fc - pw : sms - pw;
+        hs(HS_SM, h) = a.reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
     }
     c.interc = S[(size_t)S_INTERC * N];
     c.snow = S[(size_t)S_SNOW * N];
     c.seal = S[(size_t)S_SEAL * N];
     c.unsat = S[(size_t)S_UNSAT * N];
     c.sat = S[(size_t)S_SAT * N];
-#pragma unroll
-    for (int h = 0; h < H; ++h) c.sm[h] = a.reset_sm ? 0.5 * c.fc[h] : S[(size_t)(S_SM + h) * N];
 
-    const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
     const bool sealed = c.fsealed > 0.0;           // frac_sealed > 0 (parameter only)
     const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
     const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
@@ -256,19 +264,19 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
             double infil = prec_effect; // prec_effec_soil of horizon 1
             double aet_above = 0.0;     // masked running sum of positive aet above
             const double demand = pet - aet_can;
-#pragma unroll
+#pragma unroll 1
             for (int h = 0; h < H; ++h) {
                 const double pin = infil;
-                double smh = c.sm[h];
-                if (hm_gt(smh, c.sms[h])) {
+                const double sms = hs(HS_SMS, h);
+                double smh = hs(HS_SM, h);
+                if (hm_gt(smh, sms)) {
                     infil = pin;
                 } else {
-                    double frac_runoff =
-                        hm_gt(smh, kEps) ? hm_exp(c.beta[h] * hm_log(hm_div(smh, c.sms[h]))) : 0.0;
+                    double frac_runoff = hm_gt(smh, kEps) ? hm_exp(hs(HS_BETA, h) * hm_log(hm_div(smh, sms))) : 0.0;
                     double tmp = pin * (1.0 - frac_runoff);
-                    if (hm_gt(smh + tmp, c.sms[h])) {
-                        infil = pin + (smh - c.sms[h]);
-                        smh = c.sms[h];
+                    if (hm_gt(smh + tmp, sms)) {
+                        infil = pin + (smh - sms);
+                        smh = sms;
                     } else {
                         infil = pin - tmp;
                         smh = smh + tmp;
@@ -277,16 +285,17 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
                 double aet = demand;
                 if (h != 0) aet = aet - aet_above;
                 double stress;
+                const double froots = hs(HS_FROOTS, h), pw = hs(HS_PW, h);
                 if (feddes) {
-                    if (hm_ge(smh, c.fc[h])) stress = c.froots[h];
-                    else if (hm_gt(smh, c.pw[h])) stress = hm_div(c.froots[h] * (smh - c.pw[h]), c.fc_pw[h]);
+                    if (hm_ge(smh, hs(HS_FC, h))) stress = froots;
+                    else if (hm_gt(smh, pw)) stress = hm_div(froots * (smh - pw), hs(HS_DEN, h));
                     else stress = 0.0;
                 } else {
-                    double th = hm_div(smh - c.pw[h], c.sat_pw[h]);
+                    double th = hm_div(smh - pw, hs(HS_DEN, h));
                     if (hm_lt0(th)) th = 0.0;
                     if (hm_gt(th, 1.0)) th = 1.0;
-                    if (hm_ge(th, c.jarvis)) stress = c.froots[h];
-                    else if (hm_lt(th, c.jarvis)) stress = c.froots[h] * hm_div(th, c.jarvis);
+                    if (hm_ge(th, c.jarvis)) stress = froots;
+                    else if (hm_lt(th, c.jarvis)) stress = froots * hm_div(th, c.jarvis);
                     else stress = 0.0;
                 }
                 aet = aet * stress;
@@ -298,7 +307,7 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
                     smh = kEps;
                 }
                 if (hm_lt(smh, kEps)) smh = kEps;
-                c.sm[h] = smh;
+                hs(HS_SM, h) = smh;
                 if (hm_gt0(aet)) aet_above = aet_above + aet;
             }
             infil_last = infil;
@@ -345,19 +354,48 @@ __global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
     S[(size_t)S_SEAL * N] = c.seal;
     S[(size_t)S_UNSAT * N] = c.unsat;
     S[(size_t)S_SAT * N] = c.sat;
-#pragma unroll
-    for (int h = 0; h < H; ++h) S[(size_t)(S_SM + h) * N] = c.sm[h];
+#pragma unroll 1
+    for (int h = 0; h < H; ++h) S[(size_t)(S_SM + h) * N] = hs(HS_SM, h);
 }
 
-// Host-side launcher: H is a template parameter so the horizon arrays stay in registers.
+// Calendar of steps tt0 .. tt0+n-1: forcing row, month, day flag, day of year.
+__global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
+                                  int32_t stride)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t tt = tt0 + i;
+    const StepDate sd = step_date(jul_start, timestep, tt);
+    StepInfo si;
+    si.row = (int32_t)((tt + stride - 1) / stride); // iMeteoTS, mo_meteo_handler.f90:575-620
+    si.month = (int8_t)sd.month;
+    si.isday = (int8_t)(sd.hour > 6 && sd.hour <= 18); // mo_meteo_handler.f90:1048
+    si.doy = (int16_t)sd.doy;
+    steps[i] = si;
+}
+
+cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
+                              int32_t stride, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    steps_fill_kernel<<<(n + 255) / 256, 256, 0, s>>>(steps, tt0, n, jul_start, timestep, stride);
+    return cudaGetLastError();
+}
+
+// Host-side launcher: H is a template parameter (shared-memory size, loop bounds).
 cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s)
 {
     const int64_t n = (int64_t)a.n_cells * a.n_members;
     const int block = 128;
     const unsigned grid = (unsigned)((n + block - 1) / block);
+    const size_t smem = (size_t)HS_PLANES * H * block * sizeof(double);
     switch (H) {
-#define MHM_CASE(HH) \
-    case HH: cell_chain_kernel<HH><<<grid, block, 0, s>>>(a); break;
+#define MHM_CASE(HH)                                                                                               \
+    case HH:                                                                                                       \
+        if (smem > 48 * 1024)                                                                                      \
+            cudaFuncSetAttribute(cell_chain_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);   \
+        cell_chain_kernel<HH><<<grid, block, smem, s>>>(a);                                                        \
+        break;
         MHM_CASE(1) MHM_CASE(2) MHM_CASE(3) MHM_CASE(4) MHM_CASE(5) MHM_CASE(6) MHM_CASE(7) MHM_CASE(8)
 #undef MHM_CASE
     default: return cudaErrorInvalidValue;

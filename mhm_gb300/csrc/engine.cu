@@ -16,10 +16,13 @@
 #include "hmath.h"
 #include "mhm_gpu.h"
 #include "mhm_kernels.cuh"
+#include "calendar.h"
 #include "network.h"
 
 namespace mhm {
 cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s);
+cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
+                              int32_t stride, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
 cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
 cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
@@ -92,8 +95,13 @@ struct mhm_ctx {
     DevBuf<int8_t> pos_flags;
     // device: per run / chunk
     DevBuf<StepInfo> steps;
-    DevBuf<double> tro, qout, qtr, qmod, q_gauge;
+    DevBuf<double> tro[2], qout, qtr, qmod, q_gauge[2];
     DevBuf<double> stage[5][2];
+    int32_t tc_cap = 0, stage_rows = 0;
+    size_t qg_cap[2] = {0, 0};
+    int64_t chunk_seq = 0, call_seq = 0;
+    bool slot_used[2] = {false, false};
+    bool pending_outputs = false;
     // forcing
     ForcingSrc forc[5];
     // outputs
@@ -101,8 +109,10 @@ struct mhm_ctx {
     std::vector<double> host_tro, host_qmod;
     int32_t last_steps = 0;
     // execution
-    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    cudaStream_t stream = nullptr, copy_stream = nullptr, route_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
+    cudaEvent_t ev_cell_done[2] = {nullptr, nullptr}, ev_acc_done[2] = {nullptr, nullptr};
+    cudaEvent_t ev_route_end = nullptr, run_a = nullptr;
     bool timing = false;
     std::vector<TimedLaunch> pending;
     int64_t t_launches[4] = {0, 0, 0, 0};
@@ -145,19 +155,20 @@ cudaError_t upload(DevBuf<T> &b, const T *host, size_t n, cudaStream_t s)
 struct Bracket {
     mhm_ctx *c;
     int kind;
+    cudaStream_t s;
     cudaEvent_t a = nullptr, b = nullptr;
-    Bracket(mhm_ctx *cc, int k) : c(cc), kind(k)
+    Bracket(mhm_ctx *cc, int k, cudaStream_t st) : c(cc), kind(k), s(st)
     {
         if (c->timing) {
             cudaEventCreate(&a);
             cudaEventCreate(&b);
-            cudaEventRecord(a, c->stream);
+            cudaEventRecord(a, s);
         }
     }
     void done()
     {
         if (c->timing) {
-            cudaEventRecord(b, c->stream);
+            cudaEventRecord(b, s);
             c->pending.push_back({kind, a, b});
         }
     }
@@ -299,14 +310,18 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         return true;
     };
     if (!ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream") ||
-        !ck(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream")) {
+        !ck(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream") ||
+        !ck(cudaStreamCreateWithFlags(&ctx->route_stream, cudaStreamNonBlocking), "route stream")) {
         mhm_ctx_destroy(ctx);
         return MHM_ERR_CUDA;
     }
     for (int i = 0; i < 2; ++i) {
         cudaEventCreateWithFlags(&ctx->ev_copied[i], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&ctx->ev_consumed[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ctx->ev_cell_done[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ctx->ev_acc_done[i], cudaEventDisableTiming);
     }
+    cudaEventCreateWithFlags(&ctx->ev_route_end, cudaEventDisableTiming);
     const size_t N = ctx->N, M = ctx->M, H = ctx->H, L = ctx->L;
     bool ok = true;
     ok = ok && ck(ctx->params.ensure(M * n_param_planes((int)H) * N), "params");
@@ -378,13 +393,19 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
     if (!ctx) return MHM_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->route_stream) cudaStreamSynchronize(ctx->route_stream);
     harvest_timing(ctx);
     for (int i = 0; i < 2; ++i) {
         if (ctx->ev_copied[i]) cudaEventDestroy(ctx->ev_copied[i]);
         if (ctx->ev_consumed[i]) cudaEventDestroy(ctx->ev_consumed[i]);
+        if (ctx->ev_cell_done[i]) cudaEventDestroy(ctx->ev_cell_done[i]);
+        if (ctx->ev_acc_done[i]) cudaEventDestroy(ctx->ev_acc_done[i]);
     }
+    if (ctx->ev_route_end) cudaEventDestroy(ctx->ev_route_end);
+    if (ctx->run_a) cudaEventDestroy(ctx->run_a);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->route_stream) cudaStreamDestroy(ctx->route_stream);
     delete ctx;
     return MHM_OK;
 }
@@ -392,6 +413,7 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
 int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 {
     if (!ctx || !p) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     const size_t N = ctx->N;
     const int H = ctx->H, np = n_param_planes(H);
@@ -435,12 +457,13 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
 {
     if (!ctx || !p5) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
     if (ctx->n_links == 0) return MHM_OK;
     const size_t L = ctx->L;
     CK(cudaMemcpyAsync(ctx->rout_p5.p + 5 * m, p5, 5 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "p5");
-    Bracket br(ctx, 2);
+    Bracket br(ctx, 2, ctx->stream);
     CK(launch_reg_rout(ctx->n_links, ctx->rout_p5.p + 5 * m, ctx->ss_max, (double)ctx->timestep, ctx->length.p,
                        ctx->slope.p, ctx->ffp.p, ctx->link_pos.p, ctx->C1.p + m * L, ctx->C2.p + m * L,
                        ctx->stream),
@@ -454,6 +477,7 @@ int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
 int mhm_init_states(mhm_ctx *ctx, int32_t m, const double *hd)
 {
     if (!ctx || !hd) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     const size_t N = ctx->N;
     const int H = ctx->H, ns = n_state_planes(H);
@@ -516,14 +540,17 @@ int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod)
     return MHM_OK;
 }
 
-int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
+// Enqueue n_steps time steps.  Pipeline: the cell chain of every chunk runs
+// on `stream`, the L1->L11 accumulation, routing and gauge extraction of the
+// same chunk on `route_stream`, so routing of chunk c overlaps the cell chain
+// of chunk c+1 (also across calls).  Double-buffered runoff and forcing
+// staging slots are guarded by events indexed by a per-context chunk counter.
+static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 {
-    if (!ctx) return MHM_ERR_INVALID;
     if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
     const int H = ctx->H;
     CK(cudaSetDevice(ctx->device), "set device");
-    // which forcing kinds the configuration reads
     bool need[5] = {true, true, ctx->proc_pet != 1, ctx->proc_pet == 1, ctx->proc_pet == 1};
     const int32_t stride = (int32_t)std::lround(24.0 / (double)ctx->ntfd);
     const int32_t first_row = (tt0 + stride - 1) / stride;
@@ -544,48 +571,55 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         if (on_device && f.row0 != row0_all)
             return fail(ctx, MHM_ERR_INVALID, "device forcing kinds must share row0");
     }
-    // chunk length from the total-runoff budget
-    size_t per_step = M * N * sizeof(double);
-    int32_t Tc = (int32_t)std::max<size_t>(1, std::min<size_t>((size_t)n_steps, ctx->chunk_bytes / per_step));
+    // chunk length from the total-runoff budget (two slots)
+    const size_t per_step = M * N * sizeof(double);
+    int32_t Tc = (int32_t)std::max<size_t>(1, std::min<size_t>((size_t)n_steps, ctx->chunk_bytes / (2 * per_step)));
     if (!on_device) Tc = std::max<int32_t>(stride, Tc / stride * stride); // whole forcing rows per chunk
-    // calendar for the whole run (absolute forcing row in StepInfo::row)
-    std::vector<StepInfo> si(n_steps);
-    for (int32_t i = 0; i < n_steps; ++i) {
-        const int64_t tt = (int64_t)tt0 + i;
-        StepDate sd = step_date(ctx->jul_start, ctx->timestep, tt);
-        si[i].row = (int32_t)((tt + stride - 1) / stride);
-        si[i].month = (int8_t)sd.month;
-        si[i].isday = (int8_t)(sd.hour > 6 && sd.hour <= 18); // mo_meteo_handler.f90:1048
-        si[i].doy = (int16_t)sd.doy;
+    if (ctx->tc_cap < Tc) {
+        // growing the per-chunk buffers: no older work may still use them
+        CK(cudaStreamSynchronize(ctx->stream), "sync");
+        CK(cudaStreamSynchronize(ctx->route_stream), "sync");
+        CK(cudaStreamSynchronize(ctx->copy_stream), "sync");
+        for (int s = 0; s < 2; ++s) CK(ctx->tro[s].ensure((size_t)Tc * M * N), "total runoff chunk");
+        if (ctx->proc_rout == 1) {
+            CK(ctx->qout.ensure(M * (size_t)Tc * L), "qout chunk");
+            CK(ctx->qtr.ensure(M * (size_t)Tc * L), "qtr chunk");
+            CK(ctx->qmod.ensure(M * (size_t)Tc * L), "qmod chunk");
+        }
+        const int32_t max_rows = (Tc + stride - 1) / stride + 1;
+        for (int k = 0; k < 5; ++k)
+            for (int s = 0; s < 2; ++s) ctx->stage[k][s].release();
+        ctx->stage_rows = max_rows;
+        ctx->tc_cap = Tc;
     }
-    CK(upload(ctx->steps, si.data(), si.size(), ctx->stream), "steps");
-    CK(ctx->tro.ensure((size_t)Tc * M * N), "total runoff chunk");
-    if (ctx->proc_rout == 1) {
-        CK(ctx->qout.ensure(M * (size_t)Tc * L), "qout chunk");
-        CK(ctx->qtr.ensure(M * (size_t)Tc * L), "qtr chunk");
-        CK(ctx->qmod.ensure(M * (size_t)Tc * L), "qmod chunk");
-        if (ctx->G > 0) CK(ctx->q_gauge.ensure(M * (size_t)ctx->G * n_steps), "q_gauge");
-    }
-    if (ctx->out_tro) ctx->host_tro.assign((size_t)n_steps * M * N, 0.0);
-    if (ctx->out_qmod) ctx->host_qmod.assign(M * (size_t)n_steps * L, 0.0);
-    const int32_t max_rows = (Tc + stride - 1) / stride + 1;
     if (!on_device)
         for (int k = 0; k < 5; ++k)
             if (need[k])
-                for (int s = 0; s < 2; ++s) CK(ctx->stage[k][s].ensure((size_t)max_rows * N), "forcing staging");
-
+                for (int s = 0; s < 2; ++s) CK(ctx->stage[k][s].ensure((size_t)ctx->stage_rows * N), "forcing staging");
+    if (ctx->proc_rout == 1 && ctx->G > 0 && q_gauge) {
+        // one device gauge buffer per call in flight: ring of 2
+        const int gs = (int)(ctx->call_seq & 1);
+        if (ctx->qg_cap[gs] < M * (size_t)ctx->G * n_steps) {
+            CK(cudaStreamSynchronize(ctx->route_stream), "sync");
+            CK(ctx->q_gauge[gs].ensure(M * (size_t)ctx->G * n_steps), "q_gauge");
+            ctx->qg_cap[gs] = M * (size_t)ctx->G * n_steps;
+        }
+    }
+    if (ctx->out_tro) ctx->host_tro.assign((size_t)n_steps * M * N, 0.0);
+    if (ctx->out_qmod) ctx->host_qmod.assign(M * (size_t)n_steps * L, 0.0);
     const int nchunks = (n_steps + Tc - 1) / Tc;
-    auto chunk_rows = [&](int c, int32_t &r0, int32_t &r1) {
-        const int32_t s0 = c * Tc, s1 = std::min(n_steps, s0 + Tc) - 1;
-        r0 = si[s0].row;
-        r1 = si[s1].row;
+    auto chunk_rows = [&](int c, int32_t &r0, int32_t &r1) { // forcing rows iMeteoTS of the chunk
+        const int64_t t0 = (int64_t)tt0 + c * Tc, t1 = (int64_t)tt0 + std::min(n_steps, (c + 1) * Tc) - 1;
+        r0 = (int32_t)((t0 + stride - 1) / stride);
+        r1 = (int32_t)((t1 + stride - 1) / stride);
     };
+    const int64_t seq0 = ctx->chunk_seq;
     auto issue_copy = [&](int c) -> int {
         if (on_device || c >= nchunks) return MHM_OK;
-        const int slot = c & 1;
+        const int slot = (int)((seq0 + c) & 1);
         int32_t r0, r1;
         chunk_rows(c, r0, r1);
-        if (c >= 2) CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_consumed[slot], 0), "wait slot");
+        if (ctx->slot_used[slot]) CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_consumed[slot], 0), "wait slot");
         for (int k = 0; k < 5; ++k) {
             if (!need[k]) continue;
             const ForcingSrc &f = ctx->forc[k];
@@ -596,19 +630,23 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         CK(cudaEventRecord(ctx->ev_copied[slot], ctx->copy_stream), "record copied");
         return MHM_OK;
     };
-    cudaEvent_t run_a = nullptr, run_b = nullptr;
-    if (ctx->timing) {
-        cudaEventCreate(&run_a);
-        cudaEventCreate(&run_b);
-        cudaEventRecord(run_a, ctx->stream);
+    if (ctx->timing && !ctx->run_a) {
+        cudaEventCreate(&ctx->run_a);
+        cudaEventRecord(ctx->run_a, ctx->stream);
     }
-    // the stream must not start reading staging slots before the copies are issued
     if (int rc = issue_copy(0)) return rc;
     for (int c = 0; c < nchunks; ++c) {
         if (int rc = issue_copy(c + 1)) return rc;
         const int32_t s0 = c * Tc;
         const int32_t nT = std::min(n_steps, s0 + Tc) - s0;
-        const int slot = c & 1;
+        const int slot = (int)((seq0 + c) & 1);
+        // this chunk's calendar, computed on the device (stream-ordered before the cell chain)
+        CK(ctx->steps.ensure((size_t)ctx->tc_cap), "steps");
+        CK(launch_steps_fill(ctx->steps.p, tt0 + s0, nT, ctx->jul_start, ctx->timestep, stride, ctx->stream),
+           "steps fill");
+        g_launches++;
+        // the runoff slot must have been consumed by the accumulation of chunk (seq - 2)
+        if (ctx->slot_used[slot]) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_acc_done[slot], 0), "wait acc");
         CellArgs a{};
         a.n_cells = ctx->N;
         a.n_members = ctx->M;
@@ -637,44 +675,52 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         a.pet = fp[2];
         a.tmin = fp[3];
         a.tmax = fp[4];
-        a.steps = ctx->steps.p + s0;
+        a.steps = ctx->steps.p;
         a.params = ctx->params.p;
         a.states = ctx->states.p;
-        a.tro = ctx->tro.p;
+        a.tro = ctx->tro[slot].p;
         a.latitude = ctx->latitude.p;
         a.tab = ctx->tab;
         {
-            Bracket br(ctx, 0);
+            Bracket br(ctx, 0, ctx->stream);
             CK(launch_cell_chain(a, H, ctx->stream), "cell chain launch");
             br.done();
             g_launches++;
         }
-        if (!on_device) CK(cudaEventRecord(ctx->ev_consumed[slot], ctx->stream), "record consumed");
         if (ctx->out_tro)
-            CK(cudaMemcpyAsync(ctx->host_tro.data() + (size_t)s0 * M * N, ctx->tro.p, (size_t)nT * M * N * sizeof(double),
-                               cudaMemcpyDeviceToHost, ctx->stream),
+            CK(cudaMemcpyAsync(ctx->host_tro.data() + (size_t)s0 * M * N, ctx->tro[slot].p,
+                               (size_t)nT * M * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
                "tro D2H");
-        if (ctx->proc_rout != 1) continue;
-        AccArgs acc{};
-        acc.n_cells = ctx->N;
-        acc.n_nodes = ctx->L;
-        acc.n_members = ctx->M;
-        acc.n_steps = nT;
-        acc.map_flag = ctx->map_flag;
-        acc.TST = 3600.0 * ctx->timestep;
-        acc.tro = ctx->tro.p;
-        acc.l1_area = ctx->l1_area.p;
-        acc.node_cell_ptr = ctx->node_cell_ptr.p;
-        acc.node_cells = ctx->node_cells.p;
-        acc.pos_l11_l1 = ctx->pos_l11_l1.p;
-        acc.pos_area = ctx->pos_area.p;
-        acc.qout = ctx->qout.p;
-        {
-            Bracket br(ctx, 1);
-            CK(launch_runoff_acc(acc, ctx->stream), "runoff acc launch");
-            br.done();
-            g_launches++;
+        if (!on_device) CK(cudaEventRecord(ctx->ev_consumed[slot], ctx->stream), "record consumed");
+        CK(cudaEventRecord(ctx->ev_cell_done[slot], ctx->stream), "record cell done");
+        ctx->slot_used[slot] = true;
+        // ---- routing of this chunk on route_stream ----
+        cudaStream_t rs = ctx->route_stream;
+        CK(cudaStreamWaitEvent(rs, ctx->ev_cell_done[slot], 0), "wait cell");
+        if (ctx->proc_rout == 1) {
+            AccArgs acc{};
+            acc.n_cells = ctx->N;
+            acc.n_nodes = ctx->L;
+            acc.n_members = ctx->M;
+            acc.n_steps = nT;
+            acc.map_flag = ctx->map_flag;
+            acc.TST = 3600.0 * ctx->timestep;
+            acc.tro = ctx->tro[slot].p;
+            acc.l1_area = ctx->l1_area.p;
+            acc.node_cell_ptr = ctx->node_cell_ptr.p;
+            acc.node_cells = ctx->node_cells.p;
+            acc.pos_l11_l1 = ctx->pos_l11_l1.p;
+            acc.pos_area = ctx->pos_area.p;
+            acc.qout = ctx->qout.p;
+            {
+                Bracket br(ctx, 1, rs);
+                CK(launch_runoff_acc(acc, rs), "runoff acc launch");
+                br.done();
+                g_launches++;
+            }
         }
+        CK(cudaEventRecord(ctx->ev_acc_done[slot], rs), "record acc done");
+        if (ctx->proc_rout != 1) continue;
         RouteArgs r{};
         r.n_nodes = ctx->L;
         r.n_members = ctx->M;
@@ -692,7 +738,7 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
         r.qtin1 = ctx->qtin1.p;
         r.qtr1 = ctx->qtr1.p;
         {
-            Bracket br(ctx, 2);
+            Bracket br(ctx, 2, rs);
             // wavefront: tick k advances sub-chunk k - l of level l
             const int D = ctx->net.n_levels;
             const int n_sub = (nT + r.sub - 1) / r.sub;
@@ -701,12 +747,12 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
                 r.tick = k;
                 r.pos_begin = ctx->net.level_ptr[lo];
                 r.pos_end = ctx->net.level_ptr[hi + 1];
-                CK(launch_route_tick(r, ctx->stream), "route launch");
+                CK(launch_route_tick(r, rs), "route launch");
                 g_launches++;
             }
             br.done();
         }
-        if (ctx->G > 0) {
+        if (ctx->G > 0 && q_gauge) {
             GaugeArgs g{};
             g.n_members = ctx->M;
             g.n_steps = nT;
@@ -716,53 +762,88 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
             g.total_steps = n_steps;
             g.gauge_pos = ctx->gauge_pos_d.p;
             g.qmod = ctx->qmod.p;
-            g.q_gauge = ctx->q_gauge.p;
-            CK(launch_gauge_gather(g, ctx->stream), "gauge launch");
+            g.q_gauge = ctx->q_gauge[(int)(ctx->call_seq & 1)].p;
+            CK(launch_gauge_gather(g, rs), "gauge launch");
             g_launches++;
         }
         if (ctx->out_qmod)
             for (size_t m = 0; m < M; ++m)
                 CK(cudaMemcpyAsync(ctx->host_qmod.data() + (m * n_steps + s0) * L, ctx->qmod.p + m * (size_t)nT * L,
-                                   (size_t)nT * L * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+                                   (size_t)nT * L * sizeof(double), cudaMemcpyDeviceToHost, rs),
                    "qmod D2H");
         if (c == nchunks - 1) {
             // qOUT and Qmod of the last step (restart fields)
             for (size_t m = 0; m < M; ++m) {
                 CK(cudaMemcpyAsync(ctx->qout_last.p + m * L, ctx->qout.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, ctx->stream),
+                                   cudaMemcpyDeviceToDevice, rs),
                    "qout last");
                 CK(cudaMemcpyAsync(ctx->qmod_last.p + m * L, ctx->qmod.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, ctx->stream),
+                                   cudaMemcpyDeviceToDevice, rs),
                    "qmod last");
             }
         }
     }
-    if (ctx->timing) {
-        cudaEventRecord(run_b, ctx->stream);
-        ctx->pending.push_back({3, run_a, run_b});
-    }
+    ctx->chunk_seq += nchunks;
     if (q_gauge && ctx->proc_rout == 1 && ctx->G > 0)
-        CK(cudaMemcpyAsync(q_gauge, ctx->q_gauge.p, M * (size_t)ctx->G * n_steps * sizeof(double),
-                           cudaMemcpyDeviceToHost, ctx->stream),
+        CK(cudaMemcpyAsync(q_gauge, ctx->q_gauge[(int)(ctx->call_seq & 1)].p,
+                           M * (size_t)ctx->G * n_steps * sizeof(double), cudaMemcpyDeviceToHost, ctx->route_stream),
            "q_gauge D2H");
-    CK(cudaStreamSynchronize(ctx->stream), "run sync");
+    ctx->call_seq += 1;
     ctx->last_steps = n_steps;
+    ctx->pending_outputs = ctx->out_tro || ctx->out_qmod;
+    return MHM_OK;
+}
+
+int mhm_sync(mhm_ctx *ctx)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (ctx->timing && ctx->run_a) {
+        cudaEvent_t b;
+        cudaEventCreate(&b);
+        cudaEventRecord(b, ctx->route_stream);
+        ctx->pending.push_back({3, ctx->run_a, b});
+        ctx->run_a = nullptr;
+    }
+    // leave `stream` ordered after all routing work
+    CK(cudaEventRecord(ctx->ev_route_end, ctx->route_stream), "record route end");
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_route_end, 0), "join");
+    CK(cudaStreamSynchronize(ctx->stream), "run sync");
+    CK(cudaStreamSynchronize(ctx->copy_stream), "copy sync");
     harvest_timing(ctx);
-    if (ctx->out_qmod) { // routing-level positions -> node order
+    if (ctx->pending_outputs && ctx->out_qmod) { // routing-level positions -> node order
+        const size_t L = ctx->L;
         std::vector<double> row(L);
-        for (size_t r = 0; r < M * (size_t)n_steps; ++r) {
+        for (size_t r = 0; r < (size_t)ctx->M * (size_t)ctx->last_steps; ++r) {
             double *q = ctx->host_qmod.data() + r * L;
             for (size_t v = 0; v < L; ++v) row[v] = q[ctx->net.pos_of_node[v]];
             std::memcpy(q, row.data(), L * sizeof(double));
         }
     }
+    ctx->pending_outputs = false;
     return MHM_OK;
+}
+
+int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (ctx->out_tro || ctx->out_qmod)
+        return fail(ctx, MHM_ERR_INVALID, "per-step outputs need the synchronous mhm_run");
+    return run_enqueue(ctx, tt0, n_steps, q_gauge);
+}
+
+int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    int rc = run_enqueue(ctx, tt0, n_steps, q_gauge);
+    int rs = mhm_sync(ctx);
+    return rc ? rc : rs;
 }
 
 int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
 {
     if (!ctx || !st) return MHM_ERR_INVALID;
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (int rc = mhm_sync(ctx)) return rc; // states of all enqueued steps
     const size_t N = ctx->N, L = ctx->L;
     const int H = ctx->H, ns = n_state_planes(H);
     const double *S = ctx->states.p + (size_t)m * ns * N;
@@ -808,6 +889,7 @@ int mhm_set_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
 {
     if (!ctx || !st) return MHM_ERR_INVALID;
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (int rc = mhm_sync(ctx)) return rc;
     const size_t N = ctx->N, L = ctx->L;
     const int H = ctx->H, ns = n_state_planes(H);
     double *S = ctx->states.p + (size_t)m * ns * N;

@@ -62,7 +62,7 @@ HM_FN uint32_t hm_f2b(float f)
 }
 
 /* a / b, correctly rounded */
-HM_FN double hm_div(double a, double b)
+HM_FN_BIG double hm_div(double a, double b)
 {
     const uint64_t ua = hm_d2b(a), ub = hm_d2b(b);
     const uint32_t eaf = (uint32_t)(ua >> 52) & 0x7ffu, ebf = (uint32_t)(ub >> 52) & 0x7ffu;
@@ -94,23 +94,28 @@ HM_FN double hm_div(double a, double b)
         const uint64_t fm = (uint64_t)((fb & 0x7fffffu) | 0x800000u);
         uint64_t inv = (sh >= 41 && fm == 0x800000u) ? 0xffffffffffffffffULL : fm << sh;
         for (int it = 0; it < 2; ++it) {
-            const hm_u128 t = (hm_u128)Mb * inv;
-            const hm_i128 err = (hm_i128)(((hm_u128)1 << 116) - t); /* |err| < 2^94 */
-            const int64_t err_s = (int64_t)(err >> 52);
+            /* err = (2^116 - Mb*inv) >> 52, |err| < 2^42: bits 52..115 of the
+             * 128-bit difference, from its two limbs */
+            const uint64_t t_lo = Mb * inv, t_hi = hm_umulhi(Mb, inv);
+            const uint64_t e_lo = (uint64_t)0 - t_lo;
+            const uint64_t e_hi = ((uint64_t)1 << 52) - t_hi - (t_lo != 0);
+            const int64_t err_s = (int64_t)((e_hi << 12) | (e_lo >> 52));
             inv = inv + (uint64_t)(hm_smulhi((int64_t)(inv >> 1), err_s) * 2);
         }
-        /* Q ~ floor(Ma * 2^54 / Mb) in [2^54, 2^55), then exact remainder correction */
-        Q = (uint64_t)(((hm_u128)Ma * inv) >> 62);
-        R = (hm_i128)(((hm_u128)Ma << 54) - (hm_u128)Q * Mb);
+        /* Q ~ floor(Ma * 2^54 / Mb) in [2^54, 2^55) */
+        Q = (hm_umulhi(Ma, inv) << 2) | ((Ma * inv) >> 62);
+        /* exact remainder Ma*2^54 - Q*Mb; |R| < 2^57, so modulo 2^64 suffices */
+        int64_t r = (int64_t)((Ma << 54) - Q * Mb);
         for (int c = 0; c < 3; ++c) {
-            if (R < 0) {
+            if (r < 0) {
                 Q -= 1;
-                R += (hm_i128)Mb;
-            } else if (R >= (hm_i128)Mb) {
+                r += (int64_t)Mb;
+            } else if (r >= (int64_t)Mb) {
                 Q += 1;
-                R -= (hm_i128)Mb;
+                r -= (int64_t)Mb;
             }
         }
+        R = r;
     }
     /* round Q (55 bits: 53 + guard + round) to nearest even */
     uint64_t m53 = Q >> 2;

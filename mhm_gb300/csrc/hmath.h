@@ -34,10 +34,19 @@
 
 #if defined(__CUDACC__)
 #define HM_FN static __host__ __device__ __forceinline__
+/* the large functions (log, exp, pow, div) are compiled out of line: one
+ * copy per kernel keeps the instruction footprint inside the SM's
+ * instruction cache (measured faster than inlining; -DHM_INLINE inlines) */
+#if defined(HM_INLINE)
+#define HM_FN_BIG HM_FN
+#else
+#define HM_FN_BIG static __host__ __device__ __noinline__
+#endif
 #else
 #include <math.h>
 #include <string.h>
 #define HM_FN static inline
+#define HM_FN_BIG static inline
 #endif
 
 #define HM_LOG_N (1 << HM_LOG_NBITS)
@@ -377,7 +386,7 @@ HM_FN double hm_q116_to_double(hm_i128 S)
     return hm_make_double(neg, (uint64_t)(n >> 64), 11 - lz, (uint64_t)n != 0);
 }
 
-HM_FN double hm_log_i(double x)
+HM_FN_BIG double hm_log_i(double x)
 {
     const uint64_t u = hm_d2b(x);
     const uint32_t top = (uint32_t)(u >> 32);
@@ -399,7 +408,7 @@ HM_FN double hm_log_i(double x)
 }
 
 /* exp(X * 2^-64) for a signed Q64 argument */
-HM_FN double hm_exp_q64(hm_i128 X)
+HM_FN_BIG double hm_exp_q64(hm_i128 X)
 {
     if (X > ((hm_i128)710 << 64))
         return HUGE_VAL;
@@ -449,7 +458,7 @@ HM_FN double hm_exp_i(double x)
 
 /* x**y for x >= 0 (Fortran real**real): exp(y * log(x)) with log kept in
  * fixed point (no rounding of the intermediate). */
-HM_FN double hm_pow_i(double x, double y)
+HM_FN_BIG double hm_pow_i(double x, double y)
 {
     const uint64_t u = hm_d2b(x);
     const uint64_t uy = hm_d2b(y);
@@ -476,10 +485,251 @@ HM_FN double hm_pow_i(double x, double y)
     return hm_exp_q64(neg ? -P : P);
 }
 
+/* ---- the same fixed-point algorithms on explicit 64-bit limbs ----
+ * Identical integers (and results) as hm_log_i / hm_exp_i / hm_pow_i above,
+ * with fewer instructions: products of a small integer by a 128-bit
+ * constant as two 64-bit products, shifts of 64-bit values into 128 bits,
+ * and differences known to be small taken modulo 2^64. */
+
+/* (hi, lo) = k * (chi, clo) for |k| < 2^32, as a signed 128-bit value */
+HM_FN void hm_mulk128(int64_t k, uint64_t chi, uint64_t clo, int64_t *rhi, uint64_t *rlo)
+{
+    const uint64_t ak = (uint64_t)(k < 0 ? -k : k);
+    uint64_t lo = ak * clo;
+    uint64_t hi = ak * chi + hm_umulhi(ak, clo);
+    if (k < 0) {
+        hi = ~hi + (lo == 0);
+        lo = (uint64_t)0 - lo;
+    }
+    *rhi = (int64_t)hi;
+    *rlo = lo;
+}
+
+HM_FN void hm_add128(int64_t *hi, uint64_t *lo, int64_t bhi, uint64_t blo)
+{
+    const uint64_t l = *lo + blo;
+    *hi = (int64_t)((uint64_t)*hi + (uint64_t)bhi + (l < blo));
+    *lo = l;
+}
+
+/* log(x) in Q116 as (hi, lo) limbs; same contract as hm_log_fx */
+HM_FN void hm_log_fx2(uint64_t u, int64_t *Shi, uint64_t *Slo, int *near1, int *tneg, uint64_t *tmant, int *te)
+{
+    int64_t kadj = 0;
+    if ((u >> 52) == 0) {
+        const int lz = hm_clz64(u) - 11;
+        u <<= lz;
+        kadj = -lz;
+    }
+    const uint64_t tmp = u - HM_LOG_OFF;
+    const int64_t k = ((int64_t)tmp >> 52) + kadj;
+    const uint32_t i = (uint32_t)(tmp >> (52 - HM_LOG_NBITS)) & (HM_LOG_N - 1);
+    const uint64_t iz = u - (tmp & 0xfff0000000000000ULL);
+    const uint64_t M = (iz & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const uint64_t A = HM_FXLOG_TAB[3 * i];
+    const int64_t R = (int64_t)(M * A) - ((int64_t)1 << 61);
+    const int64_t lchi = (int64_t)HM_FXLOG_TAB[3 * i + 1];
+    const uint64_t lclo = HM_FXLOG_TAB[3 * i + 2];
+    int64_t hi;
+    uint64_t lo;
+    hm_mulk128(k, HM_FX_LN2_Q116_HI, HM_FX_LN2_Q116_LO, &hi, &lo);
+    hm_add128(&hi, &lo, lchi, lclo);
+    *near1 = (k == 0) && (lchi == 0) && (lclo == 0);
+    *tmant = 0;
+    if (R != 0) {
+        const int64_t rq = R * 8;
+        int64_t q = HM_FX_LOG_C7;
+        q = HM_FX_LOG_C6 + hm_smulhi(rq, q);
+        q = HM_FX_LOG_C5 + hm_smulhi(rq, q);
+        q = HM_FX_LOG_C4 + hm_smulhi(rq, q);
+        q = HM_FX_LOG_C3 + hm_smulhi(rq, q);
+        q = HM_FX_LOG_C2 + hm_smulhi(rq, q);
+        const int64_t rqq = hm_smulhi(rq, q);
+        const uint64_t f = (uint64_t)(((int64_t)1 << 62) + (rqq >> 1));
+        const uint64_t aR = (uint64_t)(R < 0 ? -R : R);
+        const int lz = hm_clz64(aR);
+        uint64_t mant = hm_umulhi(aR << lz, f);
+        const int lz2 = hm_clz64(mant);
+        mant <<= lz2;
+        const int e = 4 - lz - lz2;
+        *tneg = R < 0;
+        *tmant = mant;
+        *te = e;
+        const int sh = e + 53; /* <= 46 */
+        int64_t thi;
+        uint64_t tlo;
+        if (sh >= 0) {
+            thi = (int64_t)(sh ? mant >> (64 - sh) : 0);
+            tlo = mant << sh;
+        } else {
+            thi = 0;
+            tlo = mant >> (-sh < 64 ? -sh : 63);
+        }
+        if (R < 0) {
+            thi = (int64_t)(~(uint64_t)thi + (tlo == 0));
+            tlo = (uint64_t)0 - tlo;
+        }
+        hm_add128(&hi, &lo, thi, tlo);
+    }
+    *Shi = hi;
+    *Slo = lo;
+}
+
+HM_FN double hm_q116_to_double2(int64_t hi, uint64_t lo)
+{
+    if (hi == 0 && lo == 0)
+        return 0.0;
+    const int neg = hi < 0;
+    uint64_t h = (uint64_t)hi, l = lo;
+    if (neg) {
+        h = ~h + (l == 0);
+        l = (uint64_t)0 - l;
+    }
+    if (h) {
+        const int lz = hm_clz64(h);
+        const uint64_t top = lz ? (h << lz) | (l >> (64 - lz)) : h;
+        const uint64_t rest = l << lz;
+        return hm_make_double(neg, top, 11 - lz, rest != 0);
+    }
+    const int lz = hm_clz64(l);
+    return hm_make_double(neg, l << lz, 11 - 64 - lz, 0);
+}
+
+HM_FN_BIG double hm_log_i2(double x)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint32_t top = (uint32_t)(u >> 32);
+    if (top >= 0x7ff00000u) {
+        if (u == 0x7ff0000000000000ULL)
+            return x;
+        if ((u << 1) == 0)
+            return -HUGE_VAL;
+        return hm_b2d(0x7ff8000000000000ULL);
+    }
+    if (u == 0)
+        return -HUGE_VAL;
+    int near1, tneg, te;
+    uint64_t tmant;
+    int64_t hi;
+    uint64_t lo;
+    hm_log_fx2(u, &hi, &lo, &near1, &tneg, &tmant, &te);
+    if (near1)
+        return tmant ? hm_make_double(tneg, tmant, te, 0) : 0.0;
+    return hm_q116_to_double2(hi, lo);
+}
+
+/* exp of a Q64 argument given as (Xhi, Xlo) limbs (signed 128) */
+HM_FN_BIG double hm_exp_q64_2(int64_t Xhi, uint64_t Xlo)
+{
+    if (Xhi > 710 || (Xhi == 710 && Xlo > 0))
+        return HUGE_VAL;
+    if (Xhi < -746)
+        return 0.0;
+    const int64_t t = (int64_t)(((uint64_t)Xhi << 52) | (Xlo >> 12)); /* Q52 */
+    const int64_t kq = hm_smulhi(t, (int64_t)HM_FX_INVLN2N_Q54);
+    const int64_t k = (kq + ((int64_t)1 << 41)) >> 42;
+    int64_t phi;
+    uint64_t plo;
+    hm_mulk128(k, HM_FX_LN2N_Q116_HI, HM_FX_LN2N_Q116_LO, &phi, &plo);
+    const int64_t r = (int64_t)(Xlo - (((uint64_t)phi << 12) | (plo >> 52))); /* Q64, exact mod 2^64 */
+    int64_t q = HM_FX_EXP_C6;
+    q = HM_FX_EXP_C5 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C4 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C3 + hm_smulhi(r, q);
+    q = HM_FX_EXP_C2 + hm_smulhi(r, q);
+    const int64_t r2 = hm_smulhi(r, r);
+    const int64_t p = r + hm_smulhi(r2, q) * 2;
+    const uint64_t T = HM_FXEXP_TAB[(uint32_t)k & 127u];
+    const uint64_t tp = hm_umulhi(T, (uint64_t)(p < 0 ? -p : p));
+    uint64_t y = p < 0 ? T - tp : T + tp;
+    int e = (int)(k >> 7);
+    if (!(y >> 63)) {
+        y <<= 1;
+        e -= 1;
+    }
+    return hm_make_double(0, y, e, 0);
+}
+
+HM_FN double hm_exp_i2(double x)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint64_t a = u & 0x7fffffffffffffffULL;
+    if (a >= 0x4087500000000000ULL) {
+        if (a > 0x7ff0000000000000ULL)
+            return x;
+        return (u >> 63) ? 0.0 : HUGE_VAL;
+    }
+    const int e = (int)(a >> 52) - 1023;
+    const uint64_t M = (a & 0x000fffffffffffffULL) | (a >> 52 ? 0x0010000000000000ULL : 0);
+    const int s = e + 12; /* X = M * 2^s, s <= 21 */
+    uint64_t hi, lo;
+    if (s >= 0) {
+        hi = s ? M >> (64 - s) : 0;
+        lo = M << s;
+    } else {
+        hi = 0;
+        lo = s > -64 ? M >> (-s) : 0;
+    }
+    if (u >> 63) {
+        hi = ~hi + (lo == 0);
+        lo = (uint64_t)0 - lo;
+    }
+    return hm_exp_q64_2((int64_t)hi, lo);
+}
+
+HM_FN_BIG double hm_pow_i2(double x, double y)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint64_t uy = hm_d2b(y);
+    const uint64_t ay = uy & 0x7fffffffffffffffULL;
+    if (ay == 0 || u == 0x3ff0000000000000ULL)
+        return 1.0;
+    const int ey = (int)(ay >> 52) - 1023;
+    if (u == 0 && ay < 0x7ff0000000000000ULL) /* +0 ** finite y: exp(y * -inf) */
+        return (uy >> 63) ? HUGE_VAL : 0.0;
+    if (u - 1 >= 0x7fefffffffffffffULL || ey > 40)
+        return hm_exp_t(y * hm_log_t(x, HM_LOG_TAB), HM_EXP_TAB);
+    int near1, tneg, te;
+    uint64_t tmant;
+    int64_t Shi;
+    uint64_t Slo;
+    hm_log_fx2(u, &Shi, &Slo, &near1, &tneg, &tmant, &te);
+    /* S >> 52 (Q64), |S| < 2^74 */
+    int64_t shi = Shi >> 52;
+    uint64_t slo = ((uint64_t)Shi << 12) | (Slo >> 52);
+    const uint64_t My = (ay & 0x000fffffffffffffULL) | (ay >> 52 ? 0x0010000000000000ULL : 0);
+    const int neg = (shi < 0) != (int)(uy >> 63);
+    uint64_t ahi = (uint64_t)shi, alo = slo;
+    if (shi < 0) {
+        ahi = ~ahi + (alo == 0);
+        alo = (uint64_t)0 - alo;
+    }
+    /* prod = |S| * My < 2^127 */
+    const uint64_t plo = alo * My;
+    const uint64_t phi = ahi * My + hm_umulhi(alo, My);
+    const int sh = 52 - ey; /* >= 12 */
+    uint64_t rhi, rlo;
+    if (sh < 64) {
+        rlo = (plo >> sh) | (phi << (64 - sh));
+        rhi = phi >> sh;
+    } else if (sh < 128) {
+        rlo = phi >> (sh - 64);
+        rhi = 0;
+    } else {
+        rlo = 0;
+        rhi = 0;
+    }
+    if (neg) {
+        rhi = ~rhi + (rlo == 0);
+        rlo = (uint64_t)0 - rlo;
+    }
+    return hm_exp_q64_2((int64_t)rhi, rlo);
+}
+
 #ifndef HM_FP64_MATH
-HM_FN double hm_log(double x) { return hm_log_i(x); }
-HM_FN double hm_exp(double x) { return hm_exp_i(x); }
-HM_FN double hm_pow(double x, double y) { return hm_pow_i(x, y); }
+HM_FN double hm_log(double x) { return hm_log_i2(x); }
+HM_FN double hm_exp(double x) { return hm_exp_i2(x); }
+HM_FN double hm_pow(double x, double y) { return hm_pow_i2(x, y); }
 #else
 HM_FN double hm_log(double x) { return hm_log_t(x, HM_LOG_TAB); }
 HM_FN double hm_exp(double x) { return hm_exp_t(x, HM_EXP_TAB); }

@@ -1,4 +1,4 @@
-// network.cpp -- routing-level layout, routing order and step calendar (host).
+// network.cpp -- routing-level layout and routing order (host).
 #include "network.h"
 
 #include <algorithm>
@@ -164,36 +164,6 @@ bool routing_order(int32_t L, int32_t n_outlets, const int32_t *from_n, const in
         net_perm[rank[i] - 1] = i + 1;
     }
     return true;
-}
-
-int64_t gregorian_to_jdn(int32_t y, int32_t m, int32_t d)
-{
-    const int64_t a = (14 - m) / 12;
-    const int64_t yy = (int64_t)y + 4800 - a;
-    const int64_t mm = m + 12 * a - 3;
-    return d + (153 * mm + 2) / 5 + 365 * yy + yy / 4 - yy / 100 + yy / 400 - 32045;
-}
-
-void jdn_to_gregorian(int64_t J, int32_t *y, int32_t *m, int32_t *d)
-{
-    const int64_t f = J + 1401 + (((4 * J + 274277) / 146097) * 3) / 4 - 38;
-    const int64_t e = 4 * f + 3;
-    const int64_t g = (e % 1461) / 4;
-    const int64_t h = 5 * g + 2;
-    *d = (int32_t)((h % 153) / 5 + 1);
-    *m = (int32_t)(((h / 153 + 2) % 12) + 1);
-    *y = (int32_t)(e / 1461 - 4716 + (12 + 2 - *m) / 12);
-}
-
-StepDate step_date(int32_t jul_start, int32_t timestep, int64_t tt)
-{
-    const int64_t hours = (tt - 1) * (int64_t)timestep;
-    const int64_t J = jul_start + hours / 24;
-    StepDate s;
-    s.hour = (int32_t)(hours % 24);
-    jdn_to_gregorian(J, &s.year, &s.month, &s.day);
-    s.doy = (int32_t)(J - gregorian_to_jdn(s.year, 1, 1) + 1);
-    return s;
 }
 
 } // namespace mhm

@@ -35,16 +35,4 @@ bool build_level_network(int32_t n_nodes, int32_t n_outlets, const int32_t *net_
 bool routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n, const int32_t *to_n,
                    int32_t *net_perm, int32_t *r_order, std::string &err);
 
-// Calendar of model step tt (1-based) for a run starting at Julian day number
-// jul_start with `timestep` hours per step: integer Gregorian arithmetic
-// (E. G. Richards' JDN <-> date algorithms), equal to the reference's
-// dec2date(newTime - 0.5) (src/common/mo_common_datetime_type.f90:71-125,
-// src/mHM/mo_mhm_interface_run.f90:360).
-struct StepDate {
-    int32_t year, month, day, hour, doy;
-};
-StepDate step_date(int32_t jul_start, int32_t timestep, int64_t tt);
-int64_t gregorian_to_jdn(int32_t y, int32_t m, int32_t d);
-void jdn_to_gregorian(int64_t jdn, int32_t *y, int32_t *m, int32_t *d);
-
 } // namespace mhm

@@ -184,6 +184,17 @@ class MhmGpu:
         self._last_steps = n_steps
         return q
 
+    def run_async(self, tt0: int, n_steps: int, q_out: np.ndarray | None = None):
+        """Enqueue steps tt0..tt0+n_steps-1 and return at once; q_out
+        ([member, gauge, step] float64, kept alive by the caller) is filled
+        when sync() returns."""
+        self._check(self.L.mhm_run_async(self.ctx, tt0, n_steps, _d(q_out) if q_out is not None else None),
+                    "mhm_run_async")
+        self._last_steps = n_steps
+
+    def sync(self):
+        self._check(self.L.mhm_sync(self.ctx), "mhm_sync")
+
     def get_outputs(self):
         n = self._last_steps
         tro = np.zeros((n, self.n_members, self.dom.n_cells)) if self._out[0] else None
