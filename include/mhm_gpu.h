@@ -204,6 +204,77 @@ int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n,
 int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t n, int32_t *month,
                       int32_t *hour, int32_t *doy);
 
+/* ---- multiscale parameter regionalisation (MPR) ---- */
+
+/* Level-0 inputs of mpr() for one basin and one land-cover scene, with the
+ * classical soil database (iFlag_soilDB = 0): the arguments of
+ * src/MPR/mo_multi_param_reg.f90:67-250 and of the start-up routines
+ * generate_soil_database (src/MPR/mo_soil_database.f90:387-518) and
+ * L0_variable_init (src/MPR/mo_mpr_startup.f90:237-337).  L0 cell arrays are
+ * packed column-major over mask0 like the reference's level-0 arrays; all
+ * class ids are 1-based. */
+typedef struct {
+    int32_t n_cells0;          /* level0%nCells                                  */
+    int32_t nrows0, ncols0;    /* level0 grid                                    */
+    int32_t n_soil_types;      /* nSoilTypes                                     */
+    int32_t max_soil_hor;      /* row stride of the per-soil horizon arrays      */
+    int32_t n_geo_units;       /* nGeoUnits                                      */
+    int32_t n_lai_classes;     /* > 0: LAI from a look-up table by class;
+                                  0: gridded LAI0 [12][n_cells0]                 */
+    int32_t pad_;
+    double frac_sealed_city;   /* fracSealed_cityArea (mhm.nml)                  */
+    const double *horizon_depth;  /* [n_horizons] HorizonDepth_mHM [mm]; the last
+                                     entry is replaced per soil type by RZdepth  */
+    const uint8_t *mask0;      /* [ncols0][nrows0] column-major, 1 inside        */
+    const int32_t *l1_up, *l1_down, *l1_left, *l1_right; /* [n_cells] 1-based L0
+                                  row/column bounds of each L1 cell (mo_grid.f90) */
+    const int32_t *l1_nsub;    /* [n_cells] L0 cells inside each L1 cell         */
+    const int32_t *soil_id0;   /* [n_cells0] L0_soilId                           */
+    const int32_t *lcover0;    /* [n_cells0] L0_LCover (1 forest, 2 sealed, 3 pervious) */
+    const int32_t *geo_unit0;  /* [n_cells0] L0_geoUnit                          */
+    const double *slope0;      /* [n_cells0] L0_slope (its ranks give slope_emp) */
+    const double *aspect0;     /* [n_cells0] L0_asp [deg]                        */
+    const double *y0;          /* [n_cells0] L0 latitude (sign: hemisphere)      */
+    const int32_t *lai_class0; /* [n_cells0] LAI class, n_lai_classes > 0        */
+    const double *lai_lut;     /* [n_lai_classes][12] monthly LAI by class       */
+    const double *lai0;        /* [12][n_cells0] gridded LAI, n_lai_classes == 0 */
+    const int32_t *soil_n_hor;   /* [n_soil_types] soilDB%nHorizons              */
+    const int32_t *soil_n_till;  /* [n_soil_types] soilDB%nTillHorizons          */
+    const double *soil_ud, *soil_ld;   /* [n_soil_types][max_soil_hor] [mm]      */
+    const double *soil_sand, *soil_clay, *soil_dbm; /* [n_soil_types][max_soil_hor] */
+    const double *soil_rz_depth; /* [n_soil_types] soilDB%RZdepth [mm]           */
+    const int32_t *geo_unit_list; /* [n_geo_units] GeoUnitList                   */
+    const int32_t *geo_unit_kar;  /* [n_geo_units] GeoUnitKar (1: karstic)       */
+} mhm_l0_desc;
+
+/* Start-up of MPR for the context's basin: soil horizon weights Wd
+ * (generate_soil_database), the empirical slope distribution slope_emp
+ * (L0_variable_init), the land-cover and karst fractions of each L1 cell
+ * (L0_fractionalCover_in_Lx, src/MPR/mo_upscaling_operators.f90:152-227) and
+ * the device copy of the L0 maps in L1-block order.  Errors where the
+ * reference stops: horizon depths outside a soil type, weights not summing
+ * to 1, class ids out of range. */
+int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0);
+
+/* Start index (0-based) of each process's parameters in the global parameter
+ * vector, processMatrix(:, 3) - processMatrix(:, 2) of
+ * src/MPR/mo_mpr_read_config.f90:390-990: offsets[0..9] for processes 1..10,
+ * offsets[10] = total length. */
+int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_routing, int32_t n_geo_units,
+                     int32_t *offsets);
+
+/* mpr() (src/MPR/mo_multi_param_reg.f90:67-654) for members member0 ..
+ * member0+n-1 from their global parameter vectors gammas[n][n_gamma] (host),
+ * evaluated on the device straight into the members' effective parameters;
+ * with routing on, also reg_rout (src/mRM/mo_mrm_mpr.f90:61-119) from the
+ * routing block of each vector.  Requires mhm_mpr_setup. */
+int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma);
+
+/* Start-up products of mhm_mpr_setup, for checking: "Wd" [n_soil_types]
+ * [n_horizons][max_soil_hor], "slope_emp" [n_cells0], "horizon_depth"
+ * [n_horizons] (after the RZdepth overwrite). */
+int mhm_mpr_get_aux(mhm_ctx *ctx, const char *name, double *out);
+
 /* Pinned host memory for forcing and outputs. */
 int mhm_host_alloc(size_t bytes, void **ptr);
 int mhm_host_free(void *ptr);

@@ -61,12 +61,27 @@ class Restart(C.Structure):
     _fields_ = [(n, _dp) for n in RESTART_FIELDS]
 
 
+class L0Desc(C.Structure):
+    """mhm_l0_desc: level-0 inputs of the parameter regionalisation."""
+    _fields_ = [
+        ("n_cells0", C.c_int32), ("nrows0", C.c_int32), ("ncols0", C.c_int32), ("n_soil_types", C.c_int32),
+        ("max_soil_hor", C.c_int32), ("n_geo_units", C.c_int32), ("n_lai_classes", C.c_int32), ("pad_", C.c_int32),
+        ("frac_sealed_city", C.c_double), ("horizon_depth", _dp), ("mask0", C.POINTER(C.c_uint8)),
+        ("l1_up", _ip), ("l1_down", _ip), ("l1_left", _ip), ("l1_right", _ip), ("l1_nsub", _ip),
+        ("soil_id0", _ip), ("lcover0", _ip), ("geo_unit0", _ip), ("slope0", _dp), ("aspect0", _dp), ("y0", _dp),
+        ("lai_class0", _ip), ("lai_lut", _dp), ("lai0", _dp), ("soil_n_hor", _ip), ("soil_n_till", _ip),
+        ("soil_ud", _dp), ("soil_ld", _dp), ("soil_sand", _dp), ("soil_clay", _dp), ("soil_dbm", _dp),
+        ("soil_rz_depth", _dp), ("geo_unit_list", _ip), ("geo_unit_kar", _ip),
+    ]
+
+
 EXPORTS = [
     "mhm_ctx_create", "mhm_ctx_destroy", "mhm_last_error", "mhm_ctx_stream", "mhm_set_eff_params",
     "mhm_set_routing_params", "mhm_init_states", "mhm_set_forcing", "mhm_run", "mhm_enable_outputs",
     "mhm_get_outputs", "mhm_get_state", "mhm_set_state", "mhm_get_var", "mhm_set_timing",
     "mhm_get_timing", "mhm_host_alloc", "mhm_host_free", "mhm_version", "mhm_kernel_launch_count",
     "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar", "mhm_run_async", "mhm_sync",
+    "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux",
 ]
 
 _LIB = None
@@ -117,5 +132,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_probe_fp64.argtypes = [C.c_int64, C.POINTER(C.c_double)]
     L.mhm_routing_order.argtypes = [C.c_int32, C.c_int32, _ip, _ip, _ip, _ip]
     L.mhm_step_calendar.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip, _ip, _ip]
+    L.mhm_mpr_setup.argtypes = [vp, C.POINTER(L0Desc)]
+    L.mhm_gamma_layout.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip]
+    L.mhm_mpr.argtypes = [vp, C.c_int32, C.c_int32, _dp, C.c_int32]
+    L.mhm_mpr_get_aux.argtypes = [vp, C.c_char_p, _dp]
     _LIB = L
     return L

@@ -17,6 +17,7 @@
 #include "mhm_gpu.h"
 #include "mhm_kernels.cuh"
 #include "calendar.h"
+#include "mpr_host.h"
 #include "network.h"
 
 namespace mhm {
@@ -31,6 +32,7 @@ cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double
                             double *C2, cudaStream_t s);
 cudaError_t launch_hmath_eval(int op, int64_t n, const double *x, const double *y, double *out, cudaStream_t s);
 cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *sink, cudaStream_t s);
+cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s);
 } // namespace mhm
 
 using namespace mhm;
@@ -119,6 +121,12 @@ struct mhm_ctx {
     double t_ms[4] = {0, 0, 0, 0};
     size_t chunk_bytes = (size_t)8 << 30;
     int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
+    // multiscale parameter regionalisation (after mhm_mpr_setup)
+    bool mpr_ready = false;
+    MprSetup mpr;
+    DevBuf<int32_t> mpr_nhor, mpr_ntill, mpr_nsub;
+    DevBuf<uint32_t> mpr_code;
+    DevBuf<double> mpr_soil, mpr_se, mpr_asp, mpr_lai, mpr_frac, mpr_lut, mpr_gamma, mpr_table, mpr_petlai;
     std::string err;
 };
 
@@ -174,6 +182,16 @@ struct Bracket {
     }
 };
 
+// The routing stream gets the highest priority: its wavefront ticks are short,
+// latency-bound launches that should take the next free SM slot ahead of the
+// cell-chain blocks they overlap with.
+cudaError_t route_stream_create(cudaStream_t *s)
+{
+    int lo = 0, hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) hi = 0;
+    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, hi);
+}
+
 void harvest_timing(mhm_ctx *c)
 {
     for (auto &t : c->pending) {
@@ -186,6 +204,52 @@ void harvest_timing(mhm_ctx *c)
         cudaEventDestroy(t.b);
     }
     c->pending.clear();
+}
+
+} // namespace
+
+namespace {
+
+// processMatrix(:, 2) of src/MPR/mo_mpr_read_config.f90:390-990 (and the
+// routing block set there for mRM), accumulated into start offsets
+bool gamma_layout(int32_t proc_sm, int32_t proc_pet, int32_t proc_rout, int32_t n_geo, GammaOffsets &o)
+{
+    int32_t n_sm, n_pet, n_rout;
+    switch (proc_sm) {
+    case 1: n_sm = 17; break;
+    case 2: n_sm = 18; break;
+    case 3: n_sm = 22; break;
+    case 4: n_sm = 21; break;
+    default: return false;
+    }
+    switch (proc_pet) {
+    case -1: n_pet = 5; break;
+    case 0: n_pet = 3; break;
+    case 1: n_pet = 4; break;
+    case 2: n_pet = 2; break;
+    case 3: n_pet = 7; break;
+    default: return false;
+    }
+    switch (proc_rout) {
+    case 0: n_rout = 0; break;
+    case 1: n_rout = 5; break;
+    case 2:
+    case 3: n_rout = 1; break;
+    default: return false;
+    }
+    if (n_geo < 0) return false;
+    o.interc = 0;
+    o.snow = o.interc + 1;
+    o.soil = o.snow + 8;
+    o.runoff = o.soil + n_sm;
+    o.pet = o.runoff + 1;
+    o.interflow = o.pet + n_pet;
+    o.perc = o.interflow + 5;
+    o.routing = o.perc + 3;
+    o.geo = o.routing + n_rout;
+    o.total = o.geo + n_geo; // neutron process 10 off: no parameters
+    o.n_soil_params = n_sm;
+    return true;
 }
 
 } // namespace
@@ -311,7 +375,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     };
     if (!ck(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream") ||
         !ck(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream") ||
-        !ck(cudaStreamCreateWithFlags(&ctx->route_stream, cudaStreamNonBlocking), "route stream")) {
+        !ck(route_stream_create(&ctx->route_stream), "route stream")) {
         mhm_ctx_destroy(ctx);
         return MHM_ERR_CUDA;
     }
@@ -984,6 +1048,154 @@ int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t 
         if (hour) hour[i] = sd.hour;
         if (doy) doy[i] = sd.doy;
     }
+    return MHM_OK;
+}
+
+int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_routing, int32_t n_geo_units,
+                     int32_t *offsets)
+{
+    GammaOffsets o{};
+    if (!offsets || !gamma_layout(proc_soilmoist, proc_pet, proc_routing, n_geo_units, o)) return MHM_ERR_INVALID;
+    const int32_t v[11] = {o.interc, o.snow, o.soil, o.runoff, o.pet, o.interflow, o.perc, o.routing, o.geo,
+                           o.total, o.total};
+    std::memcpy(offsets, v, sizeof(v));
+    return MHM_OK;
+}
+
+int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
+{
+    if (!ctx || !l0) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    ctx->mpr_ready = false;
+    if (ctx->proc_pet != -1 && ctx->proc_pet != 0 && ctx->proc_pet != 1)
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "MPR supports PET cases -1, 0 and 1");
+    if (l0->max_soil_hor > kMprMaxSoilHor)
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "more than 16 soil layers per soil type");
+    MprSetup &m = ctx->mpr;
+    m = MprSetup{};
+    std::string err;
+    if (!mpr_prepare(*l0, ctx->N, ctx->H, m, err)) return fail(ctx, MHM_ERR_INVALID, err);
+    const size_t slots = (size_t)m.max_sub * m.n1, nsh = (size_t)m.n_soil * m.max_hor;
+    std::vector<double> soil;
+    soil.reserve(3 * nsh + m.n_soil + m.Wd.size() + m.H);
+    soil.insert(soil.end(), m.sand.begin(), m.sand.end());
+    soil.insert(soil.end(), m.clay.begin(), m.clay.end());
+    soil.insert(soil.end(), m.dbm.begin(), m.dbm.end());
+    soil.insert(soil.end(), m.rz.begin(), m.rz.end());
+    soil.insert(soil.end(), m.Wd.begin(), m.Wd.end());
+    soil.insert(soil.end(), m.horizon_depth.begin(), m.horizon_depth.end());
+    std::vector<double> frac;
+    frac.reserve(4 * (size_t)m.n1);
+    for (const auto *v : {&m.f_forest, &m.f_sealed, &m.f_perm, &m.f_kar}) frac.insert(frac.end(), v->begin(), v->end());
+    cudaStream_t s = ctx->stream;
+    CK(upload(ctx->mpr_nhor, m.n_hor.data(), m.n_hor.size(), s), "mpr soil");
+    CK(upload(ctx->mpr_ntill, m.n_till.data(), m.n_till.size(), s), "mpr soil");
+    CK(upload(ctx->mpr_nsub, m.nsub.data(), m.nsub.size(), s), "mpr nsub");
+    CK(upload(ctx->mpr_code, m.sub_code.data(), slots, s), "mpr codes");
+    CK(upload(ctx->mpr_soil, soil.data(), soil.size(), s), "mpr soil");
+    CK(upload(ctx->mpr_se, m.sub_se.data(), slots, s), "mpr slope");
+    CK(upload(ctx->mpr_asp, m.sub_asp.data(), slots, s), "mpr aspect");
+    CK(upload(ctx->mpr_frac, frac.data(), frac.size(), s), "mpr fractions");
+    if (m.n_lai_classes > 0) {
+        CK(upload(ctx->mpr_lut, m.lai_lut.data(), m.lai_lut.size(), s), "mpr LAI");
+        ctx->mpr_lai.release();
+    } else {
+        CK(upload(ctx->mpr_lai, m.sub_lai.data(), m.sub_lai.size(), s), "mpr LAI");
+        CK(ctx->mpr_lut.ensure(1), "mpr LAI");
+    }
+    CK(cudaStreamSynchronize(s), "mpr setup");
+    ctx->mpr_ready = true;
+    return MHM_OK;
+}
+
+int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma)
+{
+    if (!ctx || !gammas) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the parameters
+    if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
+    if (n < 1 || member0 < 0 || member0 + n > ctx->M) return fail(ctx, MHM_ERR_INVALID, "members out of range");
+    const MprSetup &m = ctx->mpr;
+    GammaOffsets off{};
+    if (!gamma_layout(ctx->proc_sm, ctx->proc_pet, ctx->proc_rout, m.n_geo, off))
+        return fail(ctx, MHM_ERR_INVALID, "no parameter layout for these processes");
+    if (n_gamma != off.total)
+        return fail(ctx, MHM_ERR_INVALID,
+                    "parameter vector has " + std::to_string(n_gamma) + " entries, expected " + std::to_string(off.total));
+    cudaStream_t s = ctx->stream;
+    const int ts = mpr_table_stride(ctx->H);
+    const size_t slots = (size_t)m.max_sub * m.n1, nsh = (size_t)m.n_soil * m.max_hor;
+    CK(upload(ctx->mpr_gamma, gammas, (size_t)n * n_gamma, s), "parameters");
+    CK(ctx->mpr_table.ensure((size_t)n * m.n_keys * ts), "mpr table");
+    CK(ctx->mpr_petlai.ensure(std::max<size_t>(1, (size_t)n * 3 * m.n_lai_classes * 12)), "mpr table");
+    MprArgs a{};
+    a.n1 = m.n1;
+    a.max_sub = m.max_sub;
+    a.H = ctx->H;
+    a.proc_sm = ctx->proc_sm;
+    a.proc_pet = ctx->proc_pet;
+    a.n_soil = m.n_soil;
+    a.max_hor = m.max_hor;
+    a.n_keys = m.n_keys;
+    a.n_lai_classes = m.n_lai_classes;
+    a.n_gamma = n_gamma;
+    a.n_members = n;
+    a.off = off;
+    a.dpth_t_last = m.dpth_t_last;
+    a.n_hor = ctx->mpr_nhor.p;
+    a.n_till = ctx->mpr_ntill.p;
+    const double *sp = ctx->mpr_soil.p;
+    a.sand = sp;
+    a.clay = sp + nsh;
+    a.dbm = sp + 2 * nsh;
+    a.rz = sp + 3 * nsh;
+    a.Wd = a.rz + m.n_soil;
+    a.hd = a.Wd + m.Wd.size();
+    a.lai_lut = ctx->mpr_lut.p;
+    a.nsub = ctx->mpr_nsub.p;
+    a.code = ctx->mpr_code.p;
+    a.se = ctx->mpr_se.p;
+    a.asp = ctx->mpr_asp.p;
+    a.lai = (m.n_lai_classes > 0) ? nullptr : ctx->mpr_lai.p;
+    a.f_forest = ctx->mpr_frac.p;
+    a.f_sealed = a.f_forest + m.n1;
+    a.f_perm = a.f_sealed + m.n1;
+    a.f_kar = a.f_perm + m.n1;
+    a.gamma = ctx->mpr_gamma.p;
+    a.table = ctx->mpr_table.p;
+    a.petlai = ctx->mpr_petlai.p;
+    const int64_t np = n_param_planes(ctx->H);
+    a.member_stride = np * ctx->N;
+    a.params = ctx->params.p + (size_t)member0 * a.member_stride;
+    (void)slots;
+    CK(launch_mpr(a, s), "mpr");
+    g_launches += 2;
+    if (ctx->proc_rout == 1 && ctx->n_links > 0) {
+        const size_t L = ctx->L;
+        for (int32_t i = 0; i < n; ++i) {
+            const int32_t mm = member0 + i;
+            const double *p5 = ctx->mpr_gamma.p + (size_t)i * n_gamma + off.routing;
+            CK(cudaMemcpyAsync(ctx->rout_p5.p + 5 * mm, p5, 5 * sizeof(double), cudaMemcpyDeviceToDevice, s), "p5");
+            CK(launch_reg_rout(ctx->n_links, ctx->rout_p5.p + 5 * mm, ctx->ss_max, (double)ctx->timestep,
+                               ctx->length.p, ctx->slope.p, ctx->ffp.p, ctx->link_pos.p, ctx->C1.p + mm * L,
+                               ctx->C2.p + mm * L, s),
+               "reg_rout");
+            g_launches++;
+        }
+    }
+    CK(cudaStreamSynchronize(s), "mpr sync");
+    return MHM_OK;
+}
+
+int mhm_mpr_get_aux(mhm_ctx *ctx, const char *name, double *out)
+{
+    if (!ctx || !name || !out) return MHM_ERR_INVALID;
+    if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
+    const std::vector<double> *v = nullptr;
+    if (!std::strcmp(name, "Wd")) v = &ctx->mpr.Wd;
+    else if (!std::strcmp(name, "slope_emp")) v = &ctx->mpr.slope_emp;
+    else if (!std::strcmp(name, "horizon_depth")) v = &ctx->mpr.horizon_depth;
+    if (!v) return fail(ctx, MHM_ERR_INVALID, std::string("unknown MPR start-up product ") + name);
+    std::memcpy(out, v->data(), v->size() * sizeof(double));
     return MHM_OK;
 }
 

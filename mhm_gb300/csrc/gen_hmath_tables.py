@@ -169,6 +169,7 @@ def fixed_point_tables(lt):
     print("#define HM_FX_LN2N_Q116_HI 0x%016xULL" % hi)
     print("#define HM_FX_LN2N_Q116_LO 0x%016xULL" % lo)
     print("#define HM_FX_INVLN2N_Q54 0x%016xULL /* round(128/ln2 * 2^54) */" % q(128 / ln2, 54))
+    print("#define HM_FX_INVLN10_Q64 0x%016xULL /* round(2^64 / ln10) */" % q(1 / mp.log(10), 64))
     # log1p(r) = r * (1 + r * q(r)), q = -1/2 + r/3 - r^2/4 + r^3/5 - r^4/6 + r^5/7 (Q63)
     for n in range(2, 8):
         v = q(mp.mpf((-1) ** (n + 1)) / n, 63)

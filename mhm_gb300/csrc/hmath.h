@@ -726,7 +726,50 @@ HM_FN_BIG double hm_pow_i2(double x, double y)
     return hm_exp_q64_2((int64_t)rhi, rlo);
 }
 
+/* log10(x) = log(x) / ln 10 from the fixed-point logarithm, one rounding */
+HM_FN_BIG double hm_log10_i2(double x)
+{
+    const uint64_t u = hm_d2b(x);
+    const uint32_t top = (uint32_t)(u >> 32);
+    if (top >= 0x7ff00000u || u == 0)
+        return hm_log_i2(x); /* +-0, negative, inf, NaN: same special values */
+    int near1, tneg, te;
+    uint64_t tmant;
+    int64_t hi;
+    uint64_t lo;
+    hm_log_fx2(u, &hi, &lo, &near1, &tneg, &tmant, &te);
+    const uint64_t c = HM_FX_INVLN10_Q64;
+    if (near1) { /* log(x) = log1p(r), a floating value (tneg, tmant, te) */
+        if (!tmant)
+            return 0.0;
+        uint64_t m = hm_umulhi(tmant, c); /* mant * c / 2^64 */
+        int e = te;
+        const int lz = hm_clz64(m);
+        m <<= lz;
+        e -= lz;
+        return hm_make_double(tneg, m, e, 0);
+    }
+    const int neg = hi < 0;
+    uint64_t ah = (uint64_t)hi, al = lo;
+    if (neg) {
+        ah = ~ah + (al == 0);
+        al = (uint64_t)0 - al;
+    }
+    /* (|S| * c) >> 64 in Q116 */
+    uint64_t rlo = ah * c;
+    uint64_t rhi = hm_umulhi(ah, c);
+    const uint64_t add = hm_umulhi(al, c);
+    rlo += add;
+    rhi += (rlo < add);
+    if (neg) {
+        rhi = ~rhi + (rlo == 0);
+        rlo = (uint64_t)0 - rlo;
+    }
+    return hm_q116_to_double2((int64_t)rhi, rlo);
+}
+
 #ifndef HM_FP64_MATH
+HM_FN double hm_log10(double x) { return hm_log10_i2(x); }
 HM_FN double hm_log(double x) { return hm_log_i2(x); }
 HM_FN double hm_exp(double x) { return hm_exp_i2(x); }
 HM_FN double hm_pow(double x, double y) { return hm_pow_i2(x, y); }
@@ -734,6 +777,7 @@ HM_FN double hm_pow(double x, double y) { return hm_pow_i2(x, y); }
 HM_FN double hm_log(double x) { return hm_log_t(x, HM_LOG_TAB); }
 HM_FN double hm_exp(double x) { return hm_exp_t(x, HM_EXP_TAB); }
 HM_FN double hm_pow(double x, double y) { return hm_pow_t(x, y, HM_LOG_TAB, HM_EXP_TAB); }
+HM_FN double hm_log10(double x) { return hm_log_t(x, HM_LOG_TAB) / 2.302585092994045684; }
 #endif
 
 #endif /* MHM_HMATH_H */

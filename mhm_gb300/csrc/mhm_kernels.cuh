@@ -107,4 +107,38 @@ struct GaugeArgs {
     double *q_gauge;       // [M][n_gauges][total_steps]
 };
 
+// ---- multiscale parameter regionalisation ----
+constexpr int kMprMaxSoilHor = 16;
+// entries of one (soil, land cover) row of the per-member soil table
+__host__ __device__ constexpr int mpr_table_stride(int H) { return 5 * H + 4; }
+enum MprTableCol : int { MT_INV_SMS = 0, MT_INV_BETA = 1, MT_INV_PW = 2, MT_INV_FC = 3, MT_INV_FROOTS = 4 };
+
+// start of each process's block in the global parameter vector
+struct GammaOffsets {
+    int32_t interc, snow, soil, runoff, pet, interflow, perc, routing, geo, total;
+    int32_t n_soil_params;
+};
+
+struct MprArgs {
+    int32_t n1, max_sub, H, proc_sm, proc_pet;
+    int32_t n_soil, max_hor, n_keys, n_lai_classes, n_gamma, n_members;
+    GammaOffsets off;
+    double dpth_t_last;            // RZdepth of the last L0 cell's soil
+    // soil database [n_soil] / [n_soil][max_hor] / Wd [n_soil][H][max_hor]
+    const int32_t *n_hor, *n_till;
+    const double *sand, *clay, *dbm, *rz, *Wd, *hd;
+    const double *lai_lut;         // [n_lai][12]
+    // L0 sub-cells of every L1 cell, slot-major [max_sub][n1]
+    const int32_t *nsub;           // [n1]
+    const uint32_t *code;
+    const double *se, *asp;
+    const double *lai;             // [12][max_sub][n1] gridded LAI or null
+    const double *f_forest, *f_sealed, *f_perm, *f_kar; // [n1]
+    const double *gamma;           // [n_members][n_gamma]
+    double *table;                 // [n_members][n_keys][stride]
+    double *petlai;                // [n_members][3][n_lai][12] reciprocal factors
+    double *params;                // effective parameters of the first member
+    int64_t member_stride;         // doubles between members' parameter blocks
+};
+
 } // namespace mhm

@@ -163,6 +163,67 @@ void ora_default_states(const ora_domain *d, const double *horizon_depth, ora_st
 /* which elementary-function build this is: 0 = hmath, 1 = libm */
 int ora_math_kind(void);
 
+/* ---- multiscale parameter regionalisation (mhm_oracle_mpr.c) ---- */
+/* One land-cover scene, iFlag_soilDB = 0.  L0 cells are packed column-major
+ * over mask0 (0-based k0); id0_2d[col * nrows0 + row] is k0 or -1 outside the
+ * mask.  L1 cell k1 covers L0 rows up1..down1 and columns left1..right1
+ * (1-based, inclusive) and holds nsub1 valid L0 cells. */
+typedef struct {
+    int32_t nCells0, nrows0, ncols0, nCells1;
+    int32_t nH;        /* nSoilHorizons_mHM (>= 2) */
+    int32_t nSoil;     /* soil types in the database (ids 1..nSoil) */
+    int32_t maxHor;    /* stride of the per-soil horizon arrays */
+    int32_t nGeo;      /* geological units */
+    int32_t proc_sm;   /* processMatrix(3,1): 1..4 */
+    int32_t proc_pet;  /* processMatrix(5,1): -1, 0, 1 */
+    int32_t n_soil_params; /* processMatrix(3,2): 17, 18, 22 or 21 */
+    int32_t pad_;
+    double fracSealed_cityArea;
+    const int32_t *id0_2d;                        /* [ncols0 * nrows0] */
+    const int32_t *up1, *down1, *left1, *right1, *nsub1; /* [nCells1] */
+    const int32_t *LCover0, *soilId0, *geoUnit0;  /* [nCells0], 1-based class ids */
+    const double *slope_emp0, *Asp0, *y0;         /* [nCells0] */
+    const double *LAI0;                           /* [12][nCells0] */
+    const int32_t *present, *nHor, *nTill;        /* [nSoil] */
+    const double *sand, *clay, *DbM;              /* [nSoil][maxHor] */
+    const double *RZdepth;                        /* [nSoil] */
+    const double *Wd;                             /* [nSoil][nH][maxHor] */
+    const double *horizonDepth;                   /* [nH], as left by ora_soil_weights */
+    const int32_t *geoUnitList, *geoUnitKar;      /* [nGeo] */
+} ora_mpr_domain;
+
+/* global parameters by process, in namelist order */
+typedef struct {
+    const double *interc;    /* [1] canopyInterceptionFactor */
+    const double *snow;      /* [8] */
+    const double *soil;      /* [n_soil_params] */
+    const double *runoff;    /* [1] imperviousStorageCapacity */
+    const double *pet;       /* [3] aspect, [4] Hargreaves-Samani, [5] LAI correction */
+    const double *interflow; /* [5] */
+    const double *perc;      /* [3] */
+    const double *geo;       /* [nGeo] */
+} ora_gamma;
+
+/* L1 outputs: per-cell [nCells1], per-horizon [nH][nCells1], monthly [12][nCells1] */
+typedef struct {
+    double *fSealed, *alpha, *degDayInc, *degDayMax, *degDayNoPre, *fAsp, *HarSamCoeff;
+    double *karstLoss, *kFastFlow, *kSlowFlow, *kBaseFlow, *kPerco;
+    double *jarvis_c1, *tempThresh, *unsatThresh, *sealedThresh;
+    double *maxInter, *petLAIcorFactor;
+    double *fRoots, *SMs, *FC, *PW, *beta;
+} ora_mpr_out;
+
+int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o);
+void ora_hydro_cond(const double *param4, double sand, double clay, double *Ks);
+void ora_genuchten(const double *param6, double sand, double clay, double Db, double *thetaS,
+                   double *n, double *alpha);
+void ora_field_cap(double Ks, double thetaS, double n, double *thetaFC);
+void ora_pwp(double n, double alpha, double thetaS, double *thetaPWP);
+/* Wd [nSoil][nH][maxHor]; horizonDepth[nH-1] is overwritten (see the source) */
+int ora_soil_weights(int nSoil, int maxHor, const int32_t *nHor, const double *UD, const double *LD,
+                     const double *RZdepth, int nH, double *horizonDepth, double *Wd);
+int ora_slope_emp(int n, const double *slope, double *slope_emp);
+
 #ifdef __cplusplus
 }
 #endif
