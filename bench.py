@@ -286,7 +286,7 @@ def run_gpu(args) -> dict:
     per_launch_s = (t_cell / max(n_cell, 1)) * 1e-3
     alg_bytes = ALG_BYTES_PER_CELL_STEP * N * chunk
     achieved = alg_bytes / per_launch_s / 1e9
-    tb = traffic_from_profiles("cell_chain_large.md")
+    tb = traffic_from_profiles("cell_chain_kernel_H6_hourly.md")
     fp64_line = {"peak": fp64_peak / 1e12 if fp64_peak else None, "unit": "TFLOP/s",
                  "peak_source": "measured live (DFMA probe, 2 FLOP per DFMA)"}
     ops = traffic_from_profiles_ops()
@@ -326,7 +326,7 @@ def run_gpu(args) -> dict:
 
 
 def traffic_from_profiles_ops():
-    f = ROOT / "profiles" / "cell_chain_large.md"
+    f = ROOT / "profiles" / "cell_chain_kernel_H6_hourly.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():

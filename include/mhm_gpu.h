@@ -130,6 +130,10 @@ void *mhm_ctx_stream(mhm_ctx *ctx);
 /* Effective parameters of `member` (the restart path of
  * mhm_interface_run_prepare, src/mHM/mo_mhm_interface_run.f90:221-231). */
 int mhm_set_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
+/* The member's effective parameters copied back into the (host) arrays the
+ * struct points to; NULL fields are skipped.  For checking mhm_mpr against
+ * the reference's L1_* arrays. */
+int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
 
 /* Muskingum coefficients C1/C2 of `member` from the five routing parameters
  * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device). */
@@ -269,6 +273,15 @@ int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_rout
  * with routing on, also reg_rout (src/mRM/mo_mrm_mpr.f90:61-119) from the
  * routing block of each vector.  Requires mhm_mpr_setup. */
 int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma);
+
+/* The two parameter-independent start-up steps of mhm_mpr_setup as host
+ * utilities (no device needed): soil horizon weights Wd [n_soil][n_h]
+ * [max_hor] of generate_soil_database (src/MPR/mo_soil_database.f90:387-518;
+ * horizon_depth[n_h-1] is overwritten as there), and the empirical slope
+ * distribution of L0_variable_init (src/MPR/mo_mpr_startup.f90:237-337). */
+int mhm_soil_weights(int32_t n_soil, int32_t max_hor, const int32_t *n_hor, const double *ud, const double *ld,
+                     const double *rz_depth, int32_t n_h, double *horizon_depth, double *wd);
+int mhm_slope_emp(int32_t n, const double *slope, double *slope_emp);
 
 /* Start-up products of mhm_mpr_setup, for checking: "Wd" [n_soil_types]
  * [n_horizons][max_soil_hor], "slope_emp" [n_cells0], "horizon_depth"

@@ -81,7 +81,8 @@ EXPORTS = [
     "mhm_get_outputs", "mhm_get_state", "mhm_set_state", "mhm_get_var", "mhm_set_timing",
     "mhm_get_timing", "mhm_host_alloc", "mhm_host_free", "mhm_version", "mhm_kernel_launch_count",
     "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar", "mhm_run_async", "mhm_sync",
-    "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux",
+    "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux", "mhm_get_eff_params",
+    "mhm_soil_weights", "mhm_slope_emp",
 ]
 
 _LIB = None
@@ -110,6 +111,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_ctx_stream.argtypes = [vp]
     L.mhm_ctx_stream.restype = vp
     L.mhm_set_eff_params.argtypes = [vp, C.c_int32, C.POINTER(EffParams)]
+    L.mhm_get_eff_params.argtypes = [vp, C.c_int32, C.POINTER(EffParams)]
     L.mhm_set_routing_params.argtypes = [vp, C.c_int32, _dp]
     L.mhm_init_states.argtypes = [vp, C.c_int32, _dp]
     L.mhm_set_forcing.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
@@ -136,5 +138,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_gamma_layout.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip]
     L.mhm_mpr.argtypes = [vp, C.c_int32, C.c_int32, _dp, C.c_int32]
     L.mhm_mpr_get_aux.argtypes = [vp, C.c_char_p, _dp]
+    L.mhm_soil_weights.argtypes = [C.c_int32, C.c_int32, _ip, _dp, _dp, _dp, C.c_int32, _dp, _dp]
+    L.mhm_slope_emp.argtypes = [C.c_int32, _dp, _dp]
     _LIB = L
     return L

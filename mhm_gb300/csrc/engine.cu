@@ -208,6 +208,7 @@ void harvest_timing(mhm_ctx *c)
 
 } // namespace
 
+
 namespace {
 
 // processMatrix(:, 2) of src/MPR/mo_mpr_read_config.f90:390-990 (and the
@@ -514,6 +515,40 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
                            cudaMemcpyHostToDevice, ctx->stream),
            "horizon params");
     }
+    CK(cudaStreamSynchronize(ctx->stream), "params sync");
+    return MHM_OK;
+}
+
+int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
+{
+    if (!ctx || !p) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const size_t N = ctx->N;
+    const int H = ctx->H, np = n_param_planes(H);
+    const double *base = ctx->params.p + (size_t)m * np * N;
+    const double *scalars[16] = {p->fSealed,   p->alpha,     p->degDayInc, p->degDayMax,   p->degDayNoPre,
+                                 p->fAsp,      p->HarSamCoeff, p->karstLoss, p->kFastFlow, p->kSlowFlow,
+                                 p->kBaseFlow, p->kPerco,    p->jarvis_thresh_c1, p->tempThresh, p->unsatThresh,
+                                 p->sealedThresh};
+    struct Part {
+        const double *dst;
+        int plane, n_planes;
+    };
+    const Part parts[] = {{p->maxInter, P_MAXINTER, 12},          {p->petLAIcorFactor, P_PETLAI, 12},
+                          {p->fRoots, P_HORIZON, H},              {p->soilMoistSat, P_HORIZON + H, H},
+                          {p->soilMoistFC, P_HORIZON + 2 * H, H}, {p->wiltingPoint, P_HORIZON + 3 * H, H},
+                          {p->soilMoistExp, P_HORIZON + 4 * H, H}};
+    for (int i = 0; i < 16; ++i)
+        if (scalars[i])
+            CK(cudaMemcpyAsync(const_cast<double *>(scalars[i]), base + (size_t)i * N, N * sizeof(double),
+                               cudaMemcpyDeviceToHost, ctx->stream),
+               "params");
+    for (const Part &q : parts)
+        if (q.dst)
+            CK(cudaMemcpyAsync(const_cast<double *>(q.dst), base + (size_t)q.plane * N,
+                               (size_t)q.n_planes * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+               "params");
     CK(cudaStreamSynchronize(ctx->stream), "params sync");
     return MHM_OK;
 }
@@ -1183,6 +1218,23 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
         }
     }
     CK(cudaStreamSynchronize(s), "mpr sync");
+    return MHM_OK;
+}
+
+int mhm_soil_weights(int32_t n_soil, int32_t max_hor, const int32_t *n_hor, const double *ud, const double *ld,
+                     const double *rz_depth, int32_t n_h, double *horizon_depth, double *wd)
+{
+    if (n_soil < 1 || max_hor < 1 || n_h < 1 || !n_hor || !ud || !ld || !rz_depth || !horizon_depth || !wd)
+        return MHM_ERR_INVALID;
+    std::string err;
+    return soil_weights(n_soil, max_hor, n_hor, ud, ld, rz_depth, n_h, horizon_depth, wd, err) ? MHM_OK
+                                                                                              : MHM_ERR_INVALID;
+}
+
+int mhm_slope_emp(int32_t n, const double *slope, double *slope_emp)
+{
+    if (n < 0 || (n > 0 && (!slope || !slope_emp))) return MHM_ERR_INVALID;
+    slope_empirical(n, slope, slope_emp);
     return MHM_OK;
 }
 

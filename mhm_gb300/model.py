@@ -146,6 +146,63 @@ class MhmGpu:
             if rlist[m] is not None:
                 self.set_routing_params(rlist[m], m)
 
+    def get_eff_params(self, member: int = 0) -> dict[str, np.ndarray]:
+        """The member's effective parameters (L1_* arrays) read back."""
+        N, H = self.dom.n_cells, self.dom.n_horizons
+        sizes = {"maxInter": 12 * N, "petLAIcorFactor": 12 * N, "fRoots": H * N, "soilMoistSat": H * N,
+                 "soilMoistFC": H * N, "wiltingPoint": H * N, "soilMoistExp": H * N}
+        out = {n: np.zeros(sizes.get(n, N)) for n in _lib.EFF_PARAM_FIELDS}
+        ep = _lib.EffParams(**{n: _d(a) for n, a in out.items()})
+        self._check(self.L.mhm_get_eff_params(self.ctx, member, C.byref(ep)), "mhm_get_eff_params")
+        return out
+
+    # ---- parameter regionalisation (mpr_eval) ----
+    def mpr_setup(self, l0):
+        """Level-0 maps and soil database of the basin (mhm_l0_desc from a
+        synth.L0Maps)."""
+        hold = []
+
+        def k(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dt)
+            hold.append(a)
+            return a
+
+        d = _lib.L0Desc()
+        d.n_cells0, d.nrows0, d.ncols0 = l0.n_cells0, l0.nrows0, l0.ncols0
+        d.n_soil_types, d.max_soil_hor, d.n_geo_units = l0.n_soil, l0.max_hor, l0.n_geo
+        gridded = getattr(l0, "gridded_lai", False)
+        d.n_lai_classes = 0 if gridded else int(l0.lai_lut.shape[0])
+        d.frac_sealed_city = l0.frac_sealed_city
+        d.horizon_depth = _d(k(l0.horizon_depth))
+        d.mask0 = k(l0.mask0, np.uint8).ctypes.data_as(C.POINTER(C.c_uint8))
+        for n in ("l1_up", "l1_down", "l1_left", "l1_right", "l1_nsub", "soil_id0", "lcover0", "geo_unit0",
+                  "soil_n_hor", "soil_n_till", "geo_unit_list", "geo_unit_kar"):
+            setattr(d, n, _i(k(getattr(l0, n), np.int32)))
+        for n in ("slope0", "aspect0", "y0", "soil_ud", "soil_ld", "soil_sand", "soil_clay", "soil_dbm",
+                  "soil_rz_depth"):
+            setattr(d, n, _d(k(getattr(l0, n))))
+        if gridded:
+            d.lai0 = _d(k(l0.lai0()))
+        else:
+            d.lai_class0 = _i(k(l0.lai_class0, np.int32))
+            d.lai_lut = _d(k(l0.lai_lut))
+        self._check(self.L.mhm_mpr_setup(self.ctx, C.byref(d)), "mhm_mpr_setup")
+        self._l0 = l0
+
+    def mpr(self, gammas: np.ndarray, member0: int = 0):
+        """mpr() (and reg_rout) for members member0.. from global parameter
+        vectors [n][n_gamma] (or one vector)."""
+        g = np.ascontiguousarray(np.atleast_2d(gammas), np.float64)
+        self._check(self.L.mhm_mpr(self.ctx, member0, g.shape[0], _d(g), g.shape[1]), "mhm_mpr")
+
+    def mpr_aux(self, name: str) -> np.ndarray:
+        l0 = self._l0
+        size = {"Wd": l0.n_soil * self.dom.n_horizons * l0.max_hor, "slope_emp": l0.n_cells0,
+                "horizon_depth": self.dom.n_horizons}[name]
+        out = np.zeros(size)
+        self._check(self.L.mhm_mpr_get_aux(self.ctx, name.encode(), _d(out)), "mhm_mpr_get_aux")
+        return out
+
     # ---- forcing (set_meteo) ----
     def set_forcing(self, kind: int, row0: int, data, on_device: bool = False):
         """data: numpy [rows, N] (host) or an object with data_ptr() (device)."""

@@ -364,3 +364,135 @@ def make_daily_forcing(dom: Domain, n_days: int, seed: int = 2, d0: int = 1) -> 
     pet = _hargreaves_daily(temp, tmax, tmin, dom.latitude[None, :], doy[:, None])
     return {k: np.ascontiguousarray(v, np.float64) for k, v in
             dict(pre=pre, temp=temp, tmin=tmin, tmax=tmax, pet=pet).items()}
+
+
+@dataclass
+class L0Maps:
+    """Level-0 inputs of the parameter regionalisation (the fields of
+    mhm_l0_desc), for an L1 grid subdivided `factor` x `factor`."""
+    nrows0: int
+    ncols0: int
+    factor: int
+    mask0: np.ndarray          # [ncols0 * nrows0] uint8, column-major
+    l1_up: np.ndarray          # [N] int32 1-based L0 bounds of each L1 cell
+    l1_down: np.ndarray
+    l1_left: np.ndarray
+    l1_right: np.ndarray
+    l1_nsub: np.ndarray
+    soil_id0: np.ndarray       # [N0] int32
+    lcover0: np.ndarray        # [N0] int32 (1 forest, 2 sealed, 3 pervious)
+    geo_unit0: np.ndarray      # [N0] int32
+    slope0: np.ndarray         # [N0] degrees
+    aspect0: np.ndarray        # [N0] degrees
+    y0: np.ndarray             # [N0] latitude
+    lai_class0: np.ndarray     # [N0] int32 1-based
+    lai_lut: np.ndarray        # [n_lai, 12]
+    soil_n_hor: np.ndarray     # [n_soil] int32
+    soil_n_till: np.ndarray
+    soil_ud: np.ndarray        # [n_soil, max_hor]
+    soil_ld: np.ndarray
+    soil_sand: np.ndarray
+    soil_clay: np.ndarray
+    soil_dbm: np.ndarray
+    soil_rz_depth: np.ndarray  # [n_soil]
+    geo_unit_list: np.ndarray  # [n_geo] int32
+    geo_unit_kar: np.ndarray   # [n_geo] int32
+    horizon_depth: np.ndarray  # [H]
+    frac_sealed_city: float = 0.6
+
+    @property
+    def n_cells0(self) -> int:
+        return int(self.soil_id0.size)
+
+    @property
+    def n_soil(self) -> int:
+        return int(self.soil_n_hor.size)
+
+    @property
+    def max_hor(self) -> int:
+        return int(self.soil_ud.shape[1])
+
+    @property
+    def n_geo(self) -> int:
+        return int(self.geo_unit_list.size)
+
+    def lai0(self) -> np.ndarray:
+        """Gridded LAI [12][N0] (the look-up table expanded)."""
+        return np.ascontiguousarray(self.lai_lut[self.lai_class0 - 1].T)
+
+
+LAI_LUT_12 = np.array([[0.5 + c * 0.4 + (2.0 + c * 0.3) * max(0.0, np.sin(np.pi * (m - 2) / 9.0))
+                        for m in range(12)] for c in range(12)])
+
+
+def make_l0(dom: Domain, factor: int = 4, seed: int = 4, n_soil: int = 10, holes: float = 0.0,
+            lat_shift: float = 0.0, max_hor: int = 4) -> L0Maps:
+    """L0 maps under the L1 grid of `dom`: 10 soil types with 2-4 layers
+    (sand 5-90 %, clay 2-60 %, DbM 1.2-1.7, root-zone depth below the modelled
+    horizons), 5 land-cover classes mapped to {1 forest, 1, 3 pervious, 3,
+    2 sealed}, 12 LAI classes, 4 geological units (ids 1, 2, 4, 7; unit 4
+    karstic; L0 cells may carry id 5, which maps to its nearest unit), slopes
+    on a 0.1 degree grid (so ranks tie), aspect 0-360.  `holes` masks that
+    fraction of L0 cells out (at least one stays in every L1 block)."""
+    rng = np.random.default_rng(seed)
+    nr, nc, f = dom.nrows, dom.ncols, factor
+    nr0, nc0 = nr * f, nc * f
+    H = dom.n_horizons
+    # mask: full, minus random holes; keep each block's first cell
+    mask2 = np.ones((nr0, nc0), bool)
+    if holes > 0:
+        mask2 &= rng.random((nr0, nc0)) >= holes
+        mask2[::f, ::f] = True
+    mask_cm = np.ascontiguousarray(mask2.T.reshape(-1)).astype(np.uint8)
+    # L1 cell k (column-major over the full L1 grid): row k % nr, col k // nr
+    k = np.arange(nr * nc)
+    r1, c1 = k % nr, k // nr
+    up = (r1 * f + 1).astype(np.int32)
+    down = ((r1 + 1) * f).astype(np.int32)
+    left = (c1 * f + 1).astype(np.int32)
+    right = ((c1 + 1) * f).astype(np.int32)
+    blocks = mask2.reshape(nr, f, nc, f).sum(axis=(1, 3))       # [nr, nc]
+    nsub = np.ascontiguousarray(blocks.T.reshape(-1), np.int32)
+    # packed L0 cells (column-major over the mask)
+    rows0, cols0 = np.nonzero(mask2.T)                          # cols0 = row index, rows0 = col index
+    ii, jj = cols0, rows0                                       # L0 row, col of each packed cell
+    n0 = ii.size
+    # soil types: coarse patches (3 L1 cells) with 20 % speckle
+    pr, pc = max(1, nr0 // (3 * f)) + 1, max(1, nc0 // (3 * f)) + 1
+    patch = rng.integers(1, n_soil + 1, (pr, pc))
+    soil = patch[ii * pr // nr0, jj * pc // nc0]
+    speck = rng.random(n0) < 0.2
+    soil = np.where(speck, rng.integers(1, n_soil + 1, n0), soil).astype(np.int32)
+    lc_map = np.array([1, 1, 3, 3, 2], np.int32)
+    lcover = lc_map[rng.integers(0, 5, n0)]
+    geo_list = np.array([1, 2, 4, 7], np.int32)
+    geo = np.array([1, 2, 4, 5, 7], np.int32)[rng.integers(0, 5, n0)]
+    slope = np.round(rng.uniform(0.0, 30.0, n0), 1)
+    aspect = rng.uniform(0.0, 360.0, n0)
+    lat = dom.latitude[(jj // f) * nr + (ii // f)] + lat_shift
+    lai_class = rng.integers(1, 13, n0).astype(np.int32)
+    # soil database
+    hd = dom.horizon_depth.copy()
+    top = hd[H - 2] if H >= 2 else 0.0
+    nh = rng.integers(2, max_hor + 1, n_soil).astype(np.int32)
+    ud = np.zeros((n_soil, max_hor))
+    ld = np.zeros((n_soil, max_hor))
+    rz = np.round(rng.uniform(top + 100.0, top + 1500.0, n_soil), -1)
+    for s in range(n_soil):
+        cuts = np.sort(rng.choice(np.arange(10.0, rz[s], 10.0), nh[s] - 1, replace=False))
+        b = np.concatenate([[0.0], cuts, [rz[s]]])
+        ud[s, :nh[s]] = b[:-1]
+        ld[s, :nh[s]] = b[1:]
+    ntill = np.minimum(nh, rng.integers(1, 3, n_soil)).astype(np.int32)
+    sand = rng.uniform(5.0, 90.0, (n_soil, max_hor))
+    clay = rng.uniform(2.0, 60.0, (n_soil, max_hor))
+    clay = np.minimum(clay, np.maximum(2.0, 100.0 - sand))
+    dbm = rng.uniform(1.2, 1.7, (n_soil, max_hor))
+    c = np.ascontiguousarray
+    return L0Maps(nrows0=nr0, ncols0=nc0, factor=f, mask0=mask_cm, l1_up=up, l1_down=down, l1_left=left,
+                  l1_right=right, l1_nsub=nsub, soil_id0=c(soil), lcover0=c(lcover.astype(np.int32)),
+                  geo_unit0=c(geo), slope0=c(slope), aspect0=c(aspect), y0=c(lat, np.float64),
+                  lai_class0=c(lai_class), lai_lut=c(LAI_LUT_12), soil_n_hor=c(nh), soil_n_till=c(ntill),
+                  soil_ud=c(ud), soil_ld=c(ld), soil_sand=c(sand), soil_clay=c(clay), soil_dbm=c(dbm),
+                  soil_rz_depth=c(rz), geo_unit_list=geo_list, geo_unit_kar=np.array([0, 0, 1, 0], np.int32),
+                  horizon_depth=c(hd))

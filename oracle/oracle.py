@@ -64,6 +64,34 @@ class OraForcing(C.Structure):
                 ("forc_row0", C.c_int32), ("n_rows", C.c_int32)]
 
 
+class OraMprDomain(C.Structure):
+    _fields_ = [
+        ("nCells0", C.c_int32), ("nrows0", C.c_int32), ("ncols0", C.c_int32), ("nCells1", C.c_int32),
+        ("nH", C.c_int32), ("nSoil", C.c_int32), ("maxHor", C.c_int32), ("nGeo", C.c_int32),
+        ("proc_sm", C.c_int32), ("proc_pet", C.c_int32), ("n_soil_params", C.c_int32), ("pad_", C.c_int32),
+        ("fracSealed_cityArea", C.c_double), ("id0_2d", _ip),
+        ("up1", _ip), ("down1", _ip), ("left1", _ip), ("right1", _ip), ("nsub1", _ip),
+        ("LCover0", _ip), ("soilId0", _ip), ("geoUnit0", _ip), ("slope_emp0", _dp), ("Asp0", _dp), ("y0", _dp),
+        ("LAI0", _dp), ("present", _ip), ("nHor", _ip), ("nTill", _ip), ("sand", _dp), ("clay", _dp),
+        ("DbM", _dp), ("RZdepth", _dp), ("Wd", _dp), ("horizonDepth", _dp), ("geoUnitList", _ip),
+        ("geoUnitKar", _ip),
+    ]
+
+
+class OraGamma(C.Structure):
+    _fields_ = [(n, _dp) for n in ("interc", "snow", "soil", "runoff", "pet", "interflow", "perc", "geo")]
+
+
+MPR_OUT_FIELDS = ["fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "HarSamCoeff",
+                  "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco", "jarvis_c1", "tempThresh",
+                  "unsatThresh", "sealedThresh", "maxInter", "petLAIcorFactor", "fRoots", "SMs", "FC", "PW",
+                  "beta"]
+
+
+class OraMprOut(C.Structure):
+    _fields_ = [(n, _dp) for n in MPR_OUT_FIELDS]
+
+
 _LIBS: dict[str, C.CDLL] = {}
 
 
@@ -120,6 +148,12 @@ def load(kind: str = "hmath") -> C.CDLL:
                           C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int]
     L.ora_default_states.argtypes = [C.POINTER(OraDomain), _dp, C.POINTER(OraState)]
     L.ora_math_kind.restype = C.c_int
+    L.ora_mpr.argtypes = [C.POINTER(OraMprDomain), C.POINTER(OraGamma), C.POINTER(OraMprOut)]
+    L.ora_mpr.restype = C.c_int
+    L.ora_soil_weights.argtypes = [C.c_int, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _dp, _dp]
+    L.ora_soil_weights.restype = C.c_int
+    L.ora_slope_emp.argtypes = [C.c_int, _dp, _dp]
+    L.ora_slope_emp.restype = C.c_int
     _LIBS[kind] = L
     return L
 
@@ -198,3 +232,75 @@ class OracleRun:
         if rc != 0:
             raise RuntimeError(f"ora_run failed ({rc})")
         return q, tro, qm
+
+
+# oracle output name -> mhm_eff_params name
+MPR_TO_EFF = {"jarvis_c1": "jarvis_thresh_c1", "SMs": "soilMoistSat", "FC": "soilMoistFC", "PW": "wiltingPoint",
+              "beta": "soilMoistExp"}
+
+
+def oracle_mpr(n1: int, H: int, l0, gamma: np.ndarray, offsets, proc_sm: int = 1, proc_pet: int = 0,
+               kind: str = "hmath") -> dict:
+    """mpr() and its start-up (soil weights, slope_emp) on the CPU for one
+    member.  `l0` carries the fields of mhm_l0_desc (mhm_gb300.synth.L0Maps),
+    `offsets` the start of each process block in `gamma` (processes 1..10,
+    then the total).  Returns the L1 parameters under mhm_eff_params names and
+    the start-up products "Wd", "slope_emp", "horizon_depth"."""
+    L = load(kind)
+    keep = []
+
+    def k(a, dt=np.float64):
+        a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+        return a
+
+    nS, mH = l0.n_soil, l0.max_hor
+    hd = k(l0.horizon_depth.copy())
+    Wd = k(np.zeros(nS * H * mH))
+    rc = L.ora_soil_weights(nS, mH, _i(k(l0.soil_n_hor, np.int32)), _d(k(l0.soil_ud)), _d(k(l0.soil_ld)),
+                            _d(k(l0.soil_rz_depth)), H, _d(hd), _d(Wd))
+    if rc != 0:
+        raise RuntimeError(f"ora_soil_weights failed ({rc})")
+    n0 = l0.n_cells0
+    se = k(np.zeros(n0))
+    L.ora_slope_emp(n0, _d(k(l0.slope0)), _d(se))
+    mask = l0.mask0.astype(bool)
+    id0 = np.full(mask.size, -1, np.int32)
+    id0[mask] = np.arange(n0, dtype=np.int32)
+    present = np.zeros(nS, np.int32)
+    present[np.unique(l0.soil_id0) - 1] = 1
+    g = k(gamma)
+    d = OraMprDomain()
+    d.nCells0, d.nrows0, d.ncols0, d.nCells1 = n0, l0.nrows0, l0.ncols0, n1
+    d.nH, d.nSoil, d.maxHor, d.nGeo = H, nS, mH, l0.n_geo
+    d.proc_sm, d.proc_pet = proc_sm, proc_pet
+    d.n_soil_params = int(offsets[3] - offsets[2])
+    d.fracSealed_cityArea = l0.frac_sealed_city
+    d.id0_2d = _i(k(id0, np.int32))
+    for n, a in (("up1", l0.l1_up), ("down1", l0.l1_down), ("left1", l0.l1_left), ("right1", l0.l1_right),
+                 ("nsub1", l0.l1_nsub), ("LCover0", l0.lcover0), ("soilId0", l0.soil_id0),
+                 ("geoUnit0", l0.geo_unit0), ("present", present), ("nHor", l0.soil_n_hor),
+                 ("nTill", l0.soil_n_till), ("geoUnitList", l0.geo_unit_list), ("geoUnitKar", l0.geo_unit_kar)):
+        setattr(d, n, _i(k(a, np.int32)))
+    for n, a in (("Asp0", l0.aspect0), ("y0", l0.y0), ("LAI0", l0.lai0()), ("sand", l0.soil_sand),
+                 ("clay", l0.soil_clay), ("DbM", l0.soil_dbm), ("RZdepth", l0.soil_rz_depth)):
+        setattr(d, n, _d(k(a)))
+    d.slope_emp0 = _d(se)
+    d.Wd = _d(Wd)
+    d.horizonDepth = _d(hd)
+    gm = OraGamma()
+    for i, n in enumerate(("interc", "snow", "soil", "runoff", "pet", "interflow", "perc")):
+        setattr(gm, n, C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[i])), _dp))
+    gm.geo = C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[8])), _dp)
+    sizes = {"maxInter": 12 * n1, "petLAIcorFactor": 12 * n1, "fRoots": H * n1, "SMs": H * n1, "FC": H * n1,
+             "PW": H * n1, "beta": H * n1}
+    out = {n: np.zeros(sizes.get(n, n1)) for n in MPR_OUT_FIELDS}
+    o = OraMprOut(**{n: _d(out[n]) for n in MPR_OUT_FIELDS})
+    rc = L.ora_mpr(C.byref(d), C.byref(gm), C.byref(o))
+    if rc != 0:
+        raise RuntimeError(f"ora_mpr failed ({rc})")
+    res = {MPR_TO_EFF.get(n, n): v for n, v in out.items()}
+    res["Wd"] = Wd
+    res["slope_emp"] = se
+    res["horizon_depth"] = hd
+    return res
