@@ -274,6 +274,18 @@ int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_rout
  * routing block of each vector.  Requires mhm_mpr_setup. */
 int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma);
 
+/* mhm_mpr for one member that allocates no device memory: the parameter
+ * vector and the soil tables live in a static device scratch of 65,536
+ * doubles (512 KiB).  No counterpart in the reference (its mpr() allocates
+ * Fortran temporaries on the host); it exists for callers that size device
+ * memory once and must not cudaMalloc/cudaFree afterwards.  Returns
+ * MHM_ERR_INVALID when the member needs more scratch than that (many soil
+ * types or horizons; use mhm_mpr).  The scratch is shared per device:
+ * overlapping calls race.  The first call on a device looks the scratch up
+ * (cudaGetSymbolAddress) and must come before any stream capture starts on
+ * that device.  Synchronises the context's stream before returning. */
+int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n_gamma);
+
 /* The two parameter-independent start-up steps of mhm_mpr_setup as host
  * utilities (no device needed): soil horizon weights Wd [n_soil][n_h]
  * [max_hor] of generate_soil_database (src/MPR/mo_soil_database.f90:387-518;

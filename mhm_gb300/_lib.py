@@ -82,7 +82,7 @@ EXPORTS = [
     "mhm_get_timing", "mhm_host_alloc", "mhm_host_free", "mhm_version", "mhm_kernel_launch_count",
     "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar", "mhm_run_async", "mhm_sync",
     "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux", "mhm_get_eff_params",
-    "mhm_soil_weights", "mhm_slope_emp",
+    "mhm_soil_weights", "mhm_slope_emp", "mhm_mpr_noalloc",
 ]
 
 _LIB = None
@@ -140,5 +140,6 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_mpr_get_aux.argtypes = [vp, C.c_char_p, _dp]
     L.mhm_soil_weights.argtypes = [C.c_int32, C.c_int32, _ip, _dp, _dp, _dp, C.c_int32, _dp, _dp]
     L.mhm_slope_emp.argtypes = [C.c_int32, _dp, _dp]
+    L.mhm_mpr_noalloc.argtypes = [vp, C.c_int32, _dp, C.c_int32]
     _LIB = L
     return L

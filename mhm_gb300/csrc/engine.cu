@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -208,6 +209,16 @@ void harvest_timing(mhm_ctx *c)
 
 } // namespace
 
+// Scratch of mhm_mpr_noalloc: the parameter vector, the soil table and the
+// LAI-correction table of one member, in one statically sized device array
+// so that the call needs no device allocation.  65,536 doubles = 512 KiB.
+constexpr size_t kMprScratchDoubles = 65536;
+static __device__ __align__(256) double g_mpr_scratch[kMprScratchDoubles];
+// its address on each device, looked up on first use
+constexpr int kMaxScratchDevices = 64;
+static std::mutex g_scratch_mu;
+static double *g_scratch_addr[kMaxScratchDevices] = {};
+static inline size_t align32(size_t n) { return (n + 31) & ~(size_t)31; } // 256-byte steps
 
 namespace {
 
@@ -1216,6 +1227,120 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
                "reg_rout");
             g_launches++;
         }
+    }
+    CK(cudaStreamSynchronize(s), "mpr sync");
+    return MHM_OK;
+}
+
+// mhm_mpr for one member without any device allocation.  mhm_mpr keeps its
+// parameter vectors and soil tables in context buffers that grow with the
+// number of members per call, i.e. it may cudaMalloc/cudaFree.  Callers that
+// must not do that use this variant: a serving loop or calibration driver
+// that sized its device memory once up front and runs several contexts side
+// by side -- cudaMalloc can fail once that budget is taken, and cudaFree may
+// synchronise the whole device, stalling the other contexts' streams.  Here
+// the per-call data live in g_mpr_scratch, whose address is looked up once
+// per device (cudaGetSymbolAddress, with the device current); all other
+// buffers were allocated by mhm_ctx_create and mhm_mpr_setup.
+//
+// Nothing in the scratch has to start at zero: the parameter vector is
+// copied in first, and every table entry the upscaling reads is written by
+// the table kernel earlier on the same stream.  The scratch is shared by all
+// contexts on a device, so two calls whose work overlaps (from two host
+// threads, or on different contexts' streams) race on it; the call
+// synchronises its stream before returning, so consecutive calls from one
+// thread are safe.  The first call on a device performs the address lookup,
+// which may load the module: make that first call before any stream capture
+// begins on the device.
+int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n_gamma)
+{
+    if (!ctx || !gamma) return MHM_ERR_INVALID;
+    if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
+    if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    const MprSetup &m = ctx->mpr;
+    GammaOffsets off{};
+    if (!gamma_layout(ctx->proc_sm, ctx->proc_pet, ctx->proc_rout, m.n_geo, off))
+        return fail(ctx, MHM_ERR_INVALID, "no parameter layout for these processes");
+    if (n_gamma != off.total) return fail(ctx, MHM_ERR_INVALID, "parameter vector length does not match the layout");
+    const int ts = mpr_table_stride(ctx->H);
+    const size_t n_table = (size_t)m.n_keys * ts, n_petlai = (size_t)3 * m.n_lai_classes * 12;
+    const size_t need = align32((size_t)n_gamma) + align32(n_table) + n_petlai;
+    if (need > kMprScratchDoubles)
+        return fail(ctx, MHM_ERR_INVALID,
+                    "mhm_mpr_noalloc needs " + std::to_string(need) + " doubles of scratch; the static scratch holds " +
+                        std::to_string(kMprScratchDoubles) + " (512 KiB): use mhm_mpr");
+    if (ctx->device < 0 || ctx->device >= kMaxScratchDevices)
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "device ordinal beyond the scratch address table");
+    CK(cudaSetDevice(ctx->device), "set device");
+    double *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        if (!g_scratch_addr[ctx->device]) {
+            void *p = nullptr;
+            CK(cudaGetSymbolAddress(&p, g_mpr_scratch), "scratch address");
+            g_scratch_addr[ctx->device] = static_cast<double *>(p);
+        }
+        scratch = g_scratch_addr[ctx->device];
+    }
+    cudaStream_t s = ctx->stream;
+    // after every step already enqueued on this context (cell chain on
+    // `stream`, routing on `route_stream`) has read the old parameters
+    CK(cudaEventRecord(ctx->ev_route_end, ctx->route_stream), "record route end");
+    CK(cudaStreamWaitEvent(s, ctx->ev_route_end, 0), "join");
+    double *d_gamma = scratch;
+    double *d_table = scratch + align32((size_t)n_gamma);
+    double *d_petlai = d_table + align32(n_table);
+    CK(cudaMemcpyAsync(d_gamma, gamma, (size_t)n_gamma * sizeof(double), cudaMemcpyHostToDevice, s), "parameters");
+    const size_t nsh = (size_t)m.n_soil * m.max_hor;
+    MprArgs a{};
+    a.n1 = m.n1;
+    a.max_sub = m.max_sub;
+    a.H = ctx->H;
+    a.proc_sm = ctx->proc_sm;
+    a.proc_pet = ctx->proc_pet;
+    a.n_soil = m.n_soil;
+    a.max_hor = m.max_hor;
+    a.n_keys = m.n_keys;
+    a.n_lai_classes = m.n_lai_classes;
+    a.n_gamma = n_gamma;
+    a.n_members = 1;
+    a.off = off;
+    a.dpth_t_last = m.dpth_t_last;
+    a.n_hor = ctx->mpr_nhor.p;
+    a.n_till = ctx->mpr_ntill.p;
+    a.sand = ctx->mpr_soil.p;
+    a.clay = a.sand + nsh;
+    a.dbm = a.sand + 2 * nsh;
+    a.rz = a.sand + 3 * nsh;
+    a.Wd = a.rz + m.n_soil;
+    a.hd = a.Wd + m.Wd.size();
+    a.lai_lut = ctx->mpr_lut.p;
+    a.nsub = ctx->mpr_nsub.p;
+    a.code = ctx->mpr_code.p;
+    a.se = ctx->mpr_se.p;
+    a.asp = ctx->mpr_asp.p;
+    a.lai = (m.n_lai_classes > 0) ? nullptr : ctx->mpr_lai.p;
+    a.f_forest = ctx->mpr_frac.p;
+    a.f_sealed = a.f_forest + m.n1;
+    a.f_perm = a.f_sealed + m.n1;
+    a.f_kar = a.f_perm + m.n1;
+    a.gamma = d_gamma;
+    a.table = d_table;
+    a.petlai = d_petlai;
+    a.member_stride = (int64_t)n_param_planes(ctx->H) * ctx->N;
+    a.params = ctx->params.p + (size_t)member * a.member_stride;
+    CK(launch_mpr(a, s), "mpr");
+    g_launches += 2;
+    if (ctx->proc_rout == 1 && ctx->n_links > 0) {
+        const size_t L = ctx->L;
+        CK(cudaMemcpyAsync(ctx->rout_p5.p + 5 * member, d_gamma + off.routing, 5 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s),
+           "p5");
+        CK(launch_reg_rout(ctx->n_links, ctx->rout_p5.p + 5 * member, ctx->ss_max, (double)ctx->timestep,
+                           ctx->length.p, ctx->slope.p, ctx->ffp.p, ctx->link_pos.p, ctx->C1.p + member * L,
+                           ctx->C2.p + member * L, s),
+           "reg_rout");
+        g_launches++;
     }
     CK(cudaStreamSynchronize(s), "mpr sync");
     return MHM_OK;

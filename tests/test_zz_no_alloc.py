@@ -1,0 +1,61 @@
+"""mhm_mpr_noalloc: the parameter regionalisation of one member with its
+per-call data in the library's static device scratch, called through the C
+ABI and compared with mhm_mpr on the same inputs, two calls in a row.
+
+The file name sorts last so that the test also runs after every other test
+in one session (the scratch is a process-wide device array)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mhm_gb300 import params, synth
+
+_dp = C.POINTER(C.c_double)
+
+RTOL = 1e-12   # the two paths run the same kernels: expected bit-equal
+
+
+def _close(a, b):
+    return np.allclose(a, b, rtol=RTOL, atol=0.0)
+
+
+@pytest.mark.gpu
+def test_mpr_noalloc_matches_mpr_two_calls_in_a_row():
+    from mhm_gb300.model import MhmGpu
+    dom = synth.make_domain(12, 10, 3, l11_factor=2, seed=1)
+    l0 = synth.make_l0(dom, 4, seed=4, holes=0.1)
+    gam = params.random_gammas(2, 1, 0, 1, l0.n_geo, seed=21)
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=2)
+    try:
+        g.mpr_setup(l0)
+        for call in range(2):
+            gm = np.ascontiguousarray(gam[call])
+            g.mpr(gm, member0=0)                                   # existing entry point
+            rc = g.L.mhm_mpr_noalloc(g.ctx, 1, gm.ctypes.data_as(_dp), gm.size)
+            assert rc == 0, g.L.mhm_last_error(g.ctx)
+            want, got = g.get_eff_params(0), g.get_eff_params(1)
+            for name in want:
+                assert _close(got[name], want[name]), (call, name)
+            st0, st1 = g.get_state(0), g.get_state(1)
+            assert _close(st1["C1"], st0["C1"]) and _close(st1["C2"], st0["C2"]), call
+    finally:
+        g.close()
+
+
+@pytest.mark.gpu
+def test_mpr_noalloc_rejects_tables_beyond_the_scratch():
+    from mhm_gb300.model import MhmGpu
+    dom = synth.make_domain(4, 4, 6, l11_factor=2, seed=1)
+    # 1000 soil types x 3 land covers x (5*6+4) doubles > 65,536
+    l0 = synth.make_l0(dom, 2, seed=4, n_soil=1000)
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=1)
+    try:
+        g.mpr_setup(l0)
+        gm = params.default_gamma(1, 0, 1, l0.n_geo)
+        rc = g.L.mhm_mpr_noalloc(g.ctx, 0, gm.ctypes.data_as(_dp), gm.size)
+        assert rc != 0
+        assert b"scratch" in g.L.mhm_last_error(g.ctx)
+        g.mpr(gm)   # the allocating entry point handles it
+    finally:
+        g.close()
