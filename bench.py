@@ -196,6 +196,8 @@ def run_gpu(args) -> dict:
     g.prepare(params, synth.ROUTING_PARAMS_DEFAULT)
     pre, temp, pet = device_forcing(dom, chunk, seed=2 + rank, device=device)
     stream = torch.cuda.ExternalStream(g.stream, device=device)
+    g.set_meteo(1, pre, temp, pet, on_device=True)
+    tune = g.autotune(1, chunk)   # register variant x routing sub-chunk, states restored
 
     G = len(dom.gauge_node)
     qbufs = [np.zeros((1, G, chunk)) for _ in range(2)]
@@ -316,13 +318,163 @@ def run_gpu(args) -> dict:
         "kernel_time_ms": {"cell_chain": t_cell, "runoff_acc": t_acc, "routing": t_rt,
                            "timed_region": ms},
         "clocks": clk.summary(),
+        "autotune": tune,
     }
+    g.close()
+    if rank == 0 and not args.no_ensemble:
+        out["batched"] = run_ensemble(args, device)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(dom, params, args)
-    g.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+ENSEMBLE = dict(nrows=200, ncols=200, H=3, l11_factor=4, l0_factor=4, members=256, chunk=240)
+
+
+def run_ensemble(args, device, plain_members: int = 8) -> dict:
+    """The calibration-ensemble workload: L1 200 x 200 (40,000 cells), 3 soil
+    horizons, L0 = L1/4, 256 parameter sets drawn uniformly within the
+    namelist bounds, hourly.  Batched: one context holds all 256 members
+    (device MPR for all of them in one call, one cell-chain launch per chunk
+    over member x cell, routing of all members per wavefront tick).  Plain:
+    the one-parameter-set drop-in, members one after another (each with its
+    own MPR and run), timed on `plain_members` members.  Both advance every
+    member by the same chunks of 240 steps; throughput counts member x cell x
+    step."""
+    import torch
+    from mhm_gb300 import params as gparams
+    from mhm_gb300 import synth
+    from mhm_gb300.model import MhmGpu
+    E = ENSEMBLE
+    dom = synth.make_domain(E["nrows"], E["ncols"], E["H"], E["l11_factor"], seed=1, dem_kind="fractal",
+                            fractal_beta=3.0, tilt=0.001)
+    l0 = synth.make_l0(dom, E["l0_factor"], seed=4)
+    M, chunk, N = E["members"], E["chunk"], dom.n_cells
+    gam = gparams.random_gammas(M, 1, 0, 1, l0.n_geo, seed=3)
+    pre, temp, pet = device_forcing(dom, chunk, seed=2, device=device)
+    G = len(dom.gauge_node)
+    K = max(1, min(args.steps, 3))
+
+    def timed(g, q, n_steps, first_step):
+        stream = torch.cuda.ExternalStream(g.stream, device=device)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(first_step, first_step + n_steps):
+            g.set_meteo(1 + s * chunk, pre, temp, pet, on_device=True)
+            g.run_async(1 + s * chunk, chunk, q[s & 1])
+        g.sync()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # batched
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=M, device=device.index)
+    g.mpr_setup(l0)
+    g.mpr(gam)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.mpr(gam)
+    mpr_ms = (time.perf_counter() - t0) * 1e3
+    for m in range(M):
+        g.init_states(m)
+    g.set_meteo(1, pre, temp, pet, on_device=True)
+    tune = g.autotune(1, 48)
+    qb = [np.zeros((M, G, chunk)) for _ in range(2)]
+    timed(g, qb, 2, 0)                      # warm-up
+    ms_b = timed(g, qb, K, 2)
+    g.close()
+    vb = float(M) * N * chunk * K / (ms_b * 1e-3)
+    # plain: one member per run, one after another
+    p = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=1, device=device.index)
+    p.mpr_setup(l0)
+    qp = [np.zeros((1, G, chunk)) for _ in range(2)]
+    p.mpr(gam[0])
+    p.init_states(0)
+    p.set_meteo(1, pre, temp, pet, on_device=True)
+    tune_p = p.autotune(1, 48)
+    timed(p, qp, 2, 0)                      # warm-up
+    ms_p, mpr_p = 0.0, 0.0
+    for m in range(plain_members):
+        t0 = time.perf_counter()
+        p.mpr(gam[m])
+        mpr_p += (time.perf_counter() - t0) * 1e3
+        p.init_states(0)
+        ms_p += timed(p, qp, K, 0)
+    p.close()
+    vp = float(plain_members) * N * chunk * K / (ms_p * 1e-3)
+    return {"workload": f"calibration ensemble: L1 {E['nrows']}x{E['ncols']} ({N} cells), {E['H']} soil horizons, "
+                        f"L0 = L1/{E['l0_factor']}, {M} parameter sets within the namelist bounds, hourly, "
+                        f"{dom.n_nodes} L11 nodes; {K} chunks of {chunk} steps per member",
+            "value": vb, "unit": UNIT, "plain_value": vp, "speedup_vs_plain": vb / vp, "members": M,
+            "plain_members_timed": plain_members, "ms_batched": ms_b, "ms_plain": ms_p,
+            "mpr_ms_all_members": mpr_ms, "mpr_ms_per_member_plain": mpr_p / plain_members,
+            "autotune_batched": tune, "autotune_plain": tune_p}
+
+
+def run_serving(args) -> dict:
+    """The serving workload: a catalogue of basins (cell counts log-uniform in
+    1e3..1e6, 2-6 soil horizons, each with its own D8 network), Poisson
+    arrivals at each rate, each request a random parameter vector within the
+    namelist bounds, a 30..365-day hourly horizon and a warm start from the
+    basin's device-resident 90-day spin-up; HBM budget 150 GB.  The server
+    (continuous batching) and the one-run-at-a-time path serve the same
+    request stream; p50/p99 latency and cell-step throughput for both."""
+    import torch
+    from mhm_gb300 import serve
+    torch.cuda.set_device(0)
+    basins = serve.make_catalogue(args.serve_basins, seed=11)
+    out = {"metric": "serving: p50/p99 latency [s] and cell-timesteps/s (mHM+mRM, FP64)", "unit": "s",
+           "catalogue": [b.name for b in basins], "hbm_budget_gb": 150, "rates": []}
+    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16)
+    srv.close()
+    for rate in args.serve_rates:
+        reqs = serve.make_requests(basins, args.serve_requests, rate, seed=int(rate))
+        srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16)
+        batched = srv.serve(reqs)
+        plain_reqs = serve.make_requests(basins, args.serve_requests, rate, seed=int(rate))
+        plain = serve.serve_plain(basins, plain_reqs, 240)
+        same = all(np.array_equal(a.discharge(), b.discharge()) for a, b in zip(
+            sorted(reqs, key=lambda r: r.rid), sorted(plain_reqs, key=lambda r: r.rid)))
+        out["rates"].append({"rate_per_s": rate, "batched": batched, "plain": plain,
+                             "throughput_ratio": batched["throughput"] / plain["throughput"],
+                             "results_identical": bool(same)})
+    return out
+
+
+def run_uneven(args) -> dict:
+    """Batched uneven basins: 64 basins with cell counts log-uniform in
+    1e3..2.5e5, 2-6 soil horizons, 90..730-day hourly horizons, each with its
+    own D8 network, all submitted at once; every basin's context is
+    autotuned (register variant, routing sub-chunk) on its first chunk.  The
+    server runs the basins' contexts side by side on their own streams
+    within the 150 GB budget; the plain path runs them one after another."""
+    import torch
+    from mhm_gb300 import serve
+    torch.cuda.set_device(0)
+    basins = serve.make_catalogue(args.uneven_basins, seed=21, n_min=1e3, n_max=2.5e5)
+    rng = np.random.default_rng(22)
+    from mhm_gb300 import params as gparams
+    reqs, reqs_p = [], []
+    for i, b in enumerate(basins):
+        g = gparams.random_gammas(1, 1, 0, 1, b.l0.n_geo, seed=300 + i)[0]
+        days = int(rng.integers(90, 731))
+        reqs.append(serve.Request(rid=i, basin=i, gamma=g, horizon=24 * days))
+        reqs_p.append(serve.Request(rid=i, basin=i, gamma=g, horizon=24 * days))
+    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=1, spinup_steps=0, autotune=True)
+    batched = srv.serve(reqs, timeout_s=3000)
+    plain = serve.serve_plain(basins, reqs_p, 240)
+    same = all(np.array_equal(a.discharge(), b.discharge()) for a, b in zip(reqs, reqs_p))
+    cells = [b.n_cells for b in basins]
+    return {"metric": "batched uneven basins: cell-timesteps/s (mHM+mRM, FP64)", "unit": UNIT,
+            "basins": len(basins), "cells_min": int(min(cells)), "cells_max": int(max(cells)),
+            "routing_levels": [b.dom.depth_stats()[0] for b in basins],
+            "value": batched["throughput"], "plain_value": plain["throughput"],
+            "speedup_vs_plain": batched["throughput"] / plain["throughput"],
+            "makespan_s": batched["wall_s"], "plain_makespan_s": plain["wall_s"], "results_identical": bool(same),
+            "autotune": srv.tuned}
 
 
 def traffic_from_profiles_ops():
@@ -389,9 +541,22 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--serve", action="store_true", help="measure the serving loop instead (p50/p99 latency)")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0, 500.0])
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-basins", type=int, default=12)
+    ap.add_argument("--uneven", action="store_true", help="measure the batched uneven-basins workload instead")
+    ap.add_argument("--uneven-basins", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.serve:
+        print(json.dumps(run_serving(args)))
+        return
+    if args.uneven:
+        print(json.dumps(run_uneven(args)))
+        return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))

@@ -170,11 +170,48 @@ int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
 /* Wait for all enqueued work of the context. */
 int mhm_sync(mhm_ctx *ctx);
 
+/* Members at different model steps (continuous batching of independent runs
+ * of one basin): member m advances its own steps member_tt0[m] ..
+ * member_tt0[m]+n_steps-1 (calendar and SM initialisation at its step 1 as in
+ * mhm_run), all members reading rows 0..n_steps-1 of the device forcing
+ * window set by mhm_set_forcing; member_tt0[m] <= 0 leaves member m idle (its
+ * cell and routing states untouched, its discharge zero).  Hourly steps with hourly forcing
+ * only.  Each member's results equal a run of that member alone from the
+ * same states over the same forcing rows.  Enqueues and returns like
+ * mhm_run_async. */
+int mhm_run_members_async(mhm_ctx *ctx, const int32_t *member_tt0, int32_t n_steps, double *q_gauge);
+
+/* Autotuner (no counterpart in the reference): times n_steps from step tt0
+ * with every combination of the cell-chain register variant (sized for 4, 6
+ * or 8 resident blocks per SM) and the routing wavefront sub-chunk (4, 8 or
+ * 16 steps), restoring all members' states before each trial and after the
+ * last, and keeps the fastest for the context's later runs.  Needs the
+ * forcing for those steps.  ms_out (may be NULL) receives the 9 trial times
+ * in (variant, sub-chunk) order. */
+int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out);
+
+/* Device-resident restart states: n_slots snapshot slots per context (each
+ * one member's cell and routing states); save/load copy on the device,
+ * ordered after the context's enqueued work (warm starts without a host
+ * round trip). */
+int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots);
+int mhm_snapshot_save(mhm_ctx *ctx, int32_t member, int32_t slot);
+int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member);
+
 /* Per-step L1 total runoff [mm TS-1] and L11 discharge of the last mhm_run:
  * optional outputs enabled before the run (adds HBM traffic). */
 int mhm_enable_outputs(mhm_ctx *ctx, int32_t total_runoff, int32_t qmod);
 /* total_runoff [n_steps][member][n_cells]; qmod [member][n_steps][n_nodes] */
 int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod);
+
+/* Per-step cell fluxes of the following mhm_run calls (the aET and
+ * percolation outputs of src/mHM/mo_write_fluxes_states.f90, per step instead
+ * of aggregated): total actual evapotranspiration (canopy + sealed share +
+ * soil share, mm per step) and the karstic percolation loss
+ * (1 - fSealed) * perc * (1 - karstLoss), both [n_steps][member][n_cells].
+ * With precipitation and total runoff they close the cell water balance. */
+int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on);
+int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss);
 
 /* Restart state of one member (host buffers). */
 int mhm_get_state(mhm_ctx *ctx, int32_t member, const mhm_restart *st);

@@ -83,6 +83,8 @@ EXPORTS = [
     "mhm_hmath_eval", "mhm_probe_fp64", "mhm_routing_order", "mhm_step_calendar", "mhm_run_async", "mhm_sync",
     "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux", "mhm_get_eff_params",
     "mhm_soil_weights", "mhm_slope_emp", "mhm_mpr_noalloc",
+    "mhm_run_members_async", "mhm_snapshot_alloc", "mhm_snapshot_save", "mhm_snapshot_load", "mhm_autotune",
+    "mhm_enable_fluxes", "mhm_get_fluxes",
 ]
 
 _LIB = None
@@ -141,5 +143,12 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_soil_weights.argtypes = [C.c_int32, C.c_int32, _ip, _dp, _dp, _dp, C.c_int32, _dp, _dp]
     L.mhm_slope_emp.argtypes = [C.c_int32, _dp, _dp]
     L.mhm_mpr_noalloc.argtypes = [vp, C.c_int32, _dp, C.c_int32]
+    L.mhm_run_members_async.argtypes = [vp, _ip, C.c_int32, _dp]
+    L.mhm_snapshot_alloc.argtypes = [vp, C.c_int32]
+    L.mhm_autotune.argtypes = [vp, C.c_int32, C.c_int32, _ip, _ip, _dp]
+    L.mhm_enable_fluxes.argtypes = [vp, C.c_int32]
+    L.mhm_get_fluxes.argtypes = [vp, _dp, _dp]
+    L.mhm_snapshot_save.argtypes = [vp, C.c_int32, C.c_int32]
+    L.mhm_snapshot_load.argtypes = [vp, C.c_int32, C.c_int32]
     _LIB = L
     return L

@@ -1,362 +1,12 @@
-// cell_chain.cu -- the mHM L1 cell chain as one time-looping kernel.
-//
-// One thread advances one (member, cell) through a chunk of time steps with
-// all states and effective parameters in registers; forcing is read once per
-// step as coalesced [step][cell] rows and the step's total runoff is written
-// as a coalesced [step][member][cell] row.  The arithmetic of every step is
-// the reference's, in the reference's order (compiled with --fmad=false;
-// log/exp/pow from hmath.h), so a step here equals a step of
-//   mHM() cell loop              src/mHM/mo_mhm.f90:458-517
-//   get_corrected_pet/temp/prec  src/meteo/mo_meteo_handler.f90:915-1285
-// bit for bit.  Expressions that depend on parameters only (c2TSTu/k, the
-// degree-day threshold, FC-PW, ...) are evaluated once per chunk: the same
-// operands give the same bits as the reference's per-step evaluation.
-#include <cfloat>
-#include <cmath>
-
-#include "calendar.h"
-#include "fp64i.h"
-#include "hmath.h"
-#include "mhm_kernels.cuh"
+// cell_chain.cu -- launchers of the cell-chain kernel (register variant for
+// 4 resident blocks per SM) and of the step-calendar kernel.  Variants sized
+// for 6 and 8 resident blocks per SM live in cell_chain_o6.cu / _o8.cu.
+#include "cell_chain_impl.cuh"
 
 namespace mhm {
 
-namespace {
-
-constexpr double kEps = DBL_EPSILON; // src/common/mo_common_constants.f90:25
-constexpr double kTwoThird = 2.0 / 3.0;
-constexpr double kPiD = 3.141592653589793238462643383279502884197;
-constexpr double kTwoPiD = 6.283185307179586476925286766559005768394;
-constexpr double kDaySecs = 86400.0, kYearDays = 365.0, kSolarConst = 1367.0, kSpecHeatET = 2.45e06;
-constexpr double kDeg2Rad = 3.141592653589793238462643383279502884197 / 180.0;
-constexpr double kHarSamConst = 17.800;
-
-// src/mHM/mo_pet.f90:314-355 (CUDA's sin/cos/tan/acos; only the daily-forcing
-// Hargreaves variant uses it)
-__device__ double extraterr_rad_approx(int doy, double latitude)
-{
-    double dr = 1.0 + 0.0330 * cos(kTwoPiD * doy / kYearDays);
-    double delta = 0.4090 * sin(kTwoPiD * doy / kYearDays - 1.3900);
-    double arg = -tan(latitude) * tan(delta);
-    if (arg < -1.0) arg = -1.0;
-    if (arg > 1.0) arg = 1.0;
-    double omega = acos(arg);
-    return kDaySecs / kPiD / kSpecHeatET * kSolarConst * dr *
-           (omega * sin(latitude) * sin(delta) + cos(latitude) * cos(delta) * sin(omega));
-}
-
-// FORCES mo_utils LE (in-tree copy pre-proc/mtCLIM/mo_utils.f90 lesserequal_dp)
-__device__ __forceinline__ bool le_dp(double a, double b)
-{
-    return !(((kEps * fabs(b) - fabs(a - b)) < 0.0) && (a > b));
-}
-
-// src/mHM/mo_pet.f90:73-116
-__device__ double pet_hargreaves(double coeff, double tavg, double tmax, double tmin, double rad)
-{
-    double delta_temp = tmax - tmin;
-    if (le_dp(delta_temp, 0.0) || le_dp(tavg, -kHarSamConst)) return 0.0;
-    return coeff * rad * (tavg + kHarSamConst) * sqrt(delta_temp);
-}
-
-// Per-thread scalars live in registers; the per-horizon parameters and soil
-// moisture live in shared memory, [plane][H][blockDim] (consecutive threads
-// -> consecutive words), so the horizon loop stays rolled: fewer registers
-// (more warps per SM) and a smaller instruction footprint.
-struct CellRegs {
-    // states
-    double interc, snow, seal, unsat, sat;
-    // parameters (and parameter-only derived values)
-    double fsealed;
-    double ddinc, ddmax_s, ddnopre_s, dd_thr;
-    double tthresh, sthresh, uthresh, karst, alpha1;
-    double k0s, k1s, k2s, kps; // c2TSTu / k
-    double jarvis;
-    double fasp, harsam, lat_rad;
-};
-enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_DEN, HS_SM, HS_PLANES };
-
-} // namespace
-
-template <int H>
-__global__ void __launch_bounds__(128) cell_chain_kernel(const CellArgs a)
-{
-    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t N = a.n_cells;
-    if (gid >= N * a.n_members) return;
-    const int m = (int)(gid / N);
-    const int k = (int)(gid - (int64_t)m * N);
-    const int np = n_param_planes(H);
-    const int ns = n_state_planes(H);
-    const double *P = a.params + (size_t)m * np * N + k;
-    double *S = a.states + (size_t)m * ns * N + k;
-    auto par = [&](int plane) { return __ldg(P + (size_t)plane * N); };
-
-    extern __shared__ double hsm[];
-    const int tb = threadIdx.x, B = blockDim.x;
-    auto hs = [&](int plane, int h) -> double & { return hsm[(plane * H + h) * B + tb]; };
-    const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
-    CellRegs c;
-    const double c2 = a.c2TSTu;
-    c.fsealed = par(P_FSEALED);
-    c.ddinc = par(P_DDINC);
-    c.ddmax_s = par(P_DDMAX) * c2;   // mo_mhm.f90:463
-    c.ddnopre_s = par(P_DDNOPRE) * c2; // mo_mhm.f90:464
-    c.dd_thr = (c.ddmax_s - c.ddnopre_s) / c.ddinc; // mo_snow_accum_melt.f90:137
-    c.tthresh = par(P_TTHRESH);
-    c.sthresh = par(P_STHRESH);
-    c.uthresh = par(P_UTHRESH);
-    c.karst = par(P_KARST);
-    c.alpha1 = 1.0 + par(P_ALPHA); // mo_runoff.f90:139
-    c.k1s = c2 / par(P_K1);        // mo_mhm.f90:484
-    c.kps = c2 / par(P_KP);
-    c.k0s = c2 / par(P_K0);
-    c.k2s = c2 / par(P_K2);        // mo_mhm.f90:488
-    c.jarvis = par(P_JARVIS);
-    c.fasp = par(P_FASP);
-    c.harsam = par(P_HARSAM);
-    c.lat_rad = (a.proc_pet == 1) ? kDeg2Rad * __ldg(a.latitude + k) : 0.0;
-#pragma unroll 1
-    for (int h = 0; h < H; ++h) {
-        const double fr = par(P_HORIZON + h), sms = par(P_HORIZON + H + h), fc = par(P_HORIZON + 2 * H + h);
-        const double pw = par(P_HORIZON + 3 * H + h);
-        hs(HS_FROOTS, h) = fr;
-        hs(HS_SMS, h) = sms;
-        hs(HS_FC, h) = fc;
-        hs(HS_PW, h) = pw;
-        hs(HS_BETA, h) = par(P_HORIZON + 4 * H + h);
-        // feddes denominator FC-PW (mo_soil_moisture.f90:358), jarvis SMs-PW (:435)
-        hs(HS_DEN, h) = feddes ? fc - pw : sms - pw;
-        hs(HS_SM, h) = a.reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
-    }
-    c.interc = S[(size_t)S_INTERC * N];
-    c.snow = S[(size_t)S_SNOW * N];
-    c.seal = S[(size_t)S_SEAL * N];
-    c.unsat = S[(size_t)S_UNSAT * N];
-    c.sat = S[(size_t)S_SAT * N];
-
-    const bool sealed = c.fsealed > 0.0;           // frac_sealed > 0 (parameter only)
-    const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
-    const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
-    int cur_month = -1;
-    double imax = 0.0, petlai = 0.0;
-    int cur_doy = -1;
-    double rad = 0.0;
-    const size_t out_stride = (size_t)a.n_members * N;
-    double *tro = a.tro + (size_t)m * N + k;
-
-    for (int t = 0; t < a.n_steps; ++t) {
-        const StepInfo si = a.steps[t];
-        const int month = si.month;
-        if (month != cur_month) { // iLAI = month (LUT-based LAI)
-            cur_month = month;
-            imax = par(P_MAXINTER + month - 1);
-            if (a.proc_pet == -1) petlai = par(P_PETLAI + month - 1);
-        }
-        const size_t f = (size_t)(si.row - a.row_base) * N + k;
-        // ---- meteo for the step (mo_meteo_handler.f90:915-1285) ----
-        double pv;
-        if (a.proc_pet == 0) {
-            pv = c.fasp * __ldg(a.pet + f);
-        } else if (a.proc_pet == -1) {
-            pv = petlai * __ldg(a.pet + f);
-        } else {
-            if (si.doy != cur_doy) {
-                cur_doy = si.doy;
-                rad = extraterr_rad_approx(cur_doy, c.lat_rad);
-            }
-            pv = c.fasp * pet_hargreaves(c.harsam, __ldg(a.temp + f), __ldg(a.tmax + f), __ldg(a.tmin + f), rad);
-        }
-        double pet, temp, prec;
-        if (a.is_hourly) {
-            pet = pv;
-            temp = __ldg(a.temp + f);
-            prec = __ldg(a.pre + f);
-        } else { // temporal_disagg_*_daynight, mo_meteo_temporal_tools.f90:66-161
-            const int mi = month - 1;
-            const double nd = a.nTstepDay;
-            if (nd > 1.0) {
-                pet = 2.0 * pv * (si.isday ? a.tab.fday_pet[mi] : a.tab.fnight_pet[mi]) / nd;
-                temp = __ldg(a.temp + f) + (si.isday ? a.tab.fday_temp[mi] : a.tab.fnight_temp[mi]);
-                prec = 2.0 * __ldg(a.pre + f) * (si.isday ? a.tab.fday_prec[mi] : a.tab.fnight_prec[mi]) / nd;
-            } else {
-                pet = pv;
-                temp = __ldg(a.temp + f);
-                prec = __ldg(a.pre + f);
-            }
-        }
-
-        // ---- canopy_interc, mo_canopy_interc.f90:75-133 ----
-        double throughfall, aet_can;
-        {
-            double aux = c.interc + prec;
-            if (hm_ge(aux, imax)) {
-                throughfall = aux - imax;
-                c.interc = imax;
-            } else {
-                throughfall = 0.0;
-                c.interc = aux;
-            }
-            aet_can = hm_gt(imax, kEps) ? pet * hm_pow(hm_div(c.interc, imax), kTwoThird) : 0.0;
-            // a negative storage gives pow() = NaN: these two tests keep IEEE NaN semantics
-            if (hm_lt_ieee(aet_can, 0.0)) aet_can = 0.0;
-            if (hm_gt_ieee(c.interc, aet_can)) {
-                c.interc = c.interc - aet_can;
-            } else {
-                aet_can = c.interc;
-                c.interc = 0.0;
-            }
-        }
-        // ---- snow_accum_melt, mo_snow_accum_melt.f90:70-158 ----
-        double prec_effect;
-        {
-            const bool warm = hm_gt(temp, c.tthresh);
-            double rain = warm ? throughfall : 0.0;
-            double snowf = warm ? 0.0 : throughfall;
-            double dd = (dd_thr_ok && hm_le(prec, c.dd_thr)) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
-            double melt;
-            if (warm) {
-                if (hm_gt0(c.snow)) {
-                    double aux = dd * (temp - c.tthresh);
-                    if (hm_gt(aux, c.snow)) {
-                        melt = c.snow;
-                        c.snow = 0.0;
-                    } else {
-                        melt = aux;
-                        c.snow = c.snow - aux;
-                    }
-                } else {
-                    melt = 0.0;
-                    c.snow = 0.0;
-                }
-            } else {
-                melt = 0.0;
-                c.snow = c.snow + snowf;
-            }
-            prec_effect = melt + rain;
-        }
-        // ---- soil_moisture, mo_soil_moisture.f90:176-286 ----
-        double runoff_sealed = 0.0;
-        double infil_last;
-        {
-            if (sealed) {
-                double tmp = c.seal + prec_effect;
-                if (hm_gt(tmp, c.sthresh)) {
-                    runoff_sealed = tmp - c.sthresh;
-                    c.seal = c.sthresh;
-                } else {
-                    runoff_sealed = 0.0;
-                    c.seal = tmp;
-                }
-                double aet_sealed;
-                if (sthresh_pos) {
-                    aet_sealed = (hm_div(pet, a.tab.evap[month - 1]) - aet_can) * hm_div(c.seal, c.sthresh);
-                    if (hm_lt0(aet_sealed)) aet_sealed = 0.0;
-                } else {
-                    aet_sealed = DBL_MAX;
-                }
-                if (hm_gt(c.seal, aet_sealed)) {
-                    c.seal = c.seal - aet_sealed;
-                } else {
-                    c.seal = 0.0;
-                }
-            }
-            double infil = prec_effect; // prec_effec_soil of horizon 1
-            double aet_above = 0.0;     // masked running sum of positive aet above
-            const double demand = pet - aet_can;
-#pragma unroll 1
-            for (int h = 0; h < H; ++h) {
-                const double pin = infil;
-                const double sms = hs(HS_SMS, h);
-                double smh = hs(HS_SM, h);
-                if (hm_gt(smh, sms)) {
-                    infil = pin;
-                } else {
-                    double frac_runoff = hm_gt(smh, kEps) ? hm_exp(hs(HS_BETA, h) * hm_log(hm_div(smh, sms))) : 0.0;
-                    double tmp = pin * (1.0 - frac_runoff);
-                    if (hm_gt(smh + tmp, sms)) {
-                        infil = pin + (smh - sms);
-                        smh = sms;
-                    } else {
-                        infil = pin - tmp;
-                        smh = smh + tmp;
-                    }
-                }
-                double aet = demand;
-                if (h != 0) aet = aet - aet_above;
-                double stress;
-                const double froots = hs(HS_FROOTS, h), pw = hs(HS_PW, h);
-                if (feddes) {
-                    if (hm_ge(smh, hs(HS_FC, h))) stress = froots;
-                    else if (hm_gt(smh, pw)) stress = hm_div(froots * (smh - pw), hs(HS_DEN, h));
-                    else stress = 0.0;
-                } else {
-                    double th = hm_div(smh - pw, hs(HS_DEN, h));
-                    if (hm_lt0(th)) th = 0.0;
-                    if (hm_gt(th, 1.0)) th = 1.0;
-                    if (hm_ge(th, c.jarvis)) stress = froots;
-                    else if (hm_lt(th, c.jarvis)) stress = froots * hm_div(th, c.jarvis);
-                    else stress = 0.0;
-                }
-                aet = aet * stress;
-                if (hm_lt0(aet)) aet = 0.0;
-                if (hm_gt(smh, aet)) {
-                    smh = smh - aet;
-                } else {
-                    aet = smh - kEps;
-                    smh = kEps;
-                }
-                if (hm_lt(smh, kEps)) smh = kEps;
-                hs(HS_SM, h) = smh;
-                if (hm_gt0(aet)) aet_above = aet_above + aet;
-            }
-            infil_last = infil;
-        }
-        // ---- runoff_unsat_zone, mo_runoff.f90:74-154 ----
-        double fast = 0.0, slow = 0.0, base;
-        {
-            c.unsat = c.unsat + infil_last;
-            if (hm_gt(c.unsat, c.uthresh)) {
-                double x = c.k0s * (c.unsat - c.uthresh);
-                double y = c.unsat - kEps;
-                fast = hm_lt(x, y) ? x : y;
-            }
-            c.unsat = c.unsat - fast;
-            if (hm_gt(c.unsat, kEps)) {
-                double x = c.k1s * hm_pow(c.unsat, c.alpha1);
-                double y = c.unsat - kEps;
-                slow = hm_lt(x, y) ? x : y;
-            }
-            c.unsat = c.unsat - slow;
-            double perc = c.kps * c.unsat;
-            if (hm_gt(c.unsat, perc)) {
-                c.unsat = c.unsat - perc;
-                c.sat = c.sat + perc * c.karst;
-            } else {
-                c.sat = c.sat + c.unsat * c.karst;
-                c.unsat = 0.0;
-            }
-        }
-        // ---- runoff_sat_zone, mo_runoff.f90:191-212 ----
-        if (hm_gt0(c.sat)) {
-            base = c.k2s * c.sat;
-            c.sat = c.sat - base;
-        } else {
-            base = 0.0;
-            c.sat = 0.0;
-        }
-        // ---- L1_total_runoff, mo_runoff.f90:248-274 ----
-        tro[(size_t)t * out_stride] = ((base + slow + fast) * (1.0 - c.fsealed)) + (runoff_sealed * c.fsealed);
-    }
-
-    S[(size_t)S_INTERC * N] = c.interc;
-    S[(size_t)S_SNOW * N] = c.snow;
-    S[(size_t)S_SEAL * N] = c.seal;
-    S[(size_t)S_UNSAT * N] = c.unsat;
-    S[(size_t)S_SAT * N] = c.sat;
-#pragma unroll 1
-    for (int h = 0; h < H; ++h) S[(size_t)(S_SM + h) * N] = hs(HS_SM, h);
-}
+cudaError_t launch_cell_chain_o6(const CellArgs &a, int H, cudaStream_t s);
+cudaError_t launch_cell_chain_o8(const CellArgs &a, int H, cudaStream_t s);
 
 // Calendar of steps tt0 .. tt0+n-1: forcing row, month, day flag, day of year.
 __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
@@ -382,25 +32,16 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
     return cudaGetLastError();
 }
 
-// Host-side launcher: H is a template parameter (shared-memory size, loop bounds).
-cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s)
+// occ = resident blocks per SM the kernel's registers are sized for (4, 6, 8)
+cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s)
 {
-    const int64_t n = (int64_t)a.n_cells * a.n_members;
-    const int block = 128;
-    const unsigned grid = (unsigned)((n + block - 1) / block);
-    const size_t smem = (size_t)HS_PLANES * H * block * sizeof(double);
-    switch (H) {
-#define MHM_CASE(HH)                                                                                               \
-    case HH:                                                                                                       \
-        if (smem > 48 * 1024)                                                                                      \
-            cudaFuncSetAttribute(cell_chain_kernel<HH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);   \
-        cell_chain_kernel<HH><<<grid, block, smem, s>>>(a);                                                        \
-        break;
-        MHM_CASE(1) MHM_CASE(2) MHM_CASE(3) MHM_CASE(4) MHM_CASE(5) MHM_CASE(6) MHM_CASE(7) MHM_CASE(8)
-#undef MHM_CASE
-    default: return cudaErrorInvalidValue;
+    if (H < 1 || H > kMaxHorizons) return cudaErrorInvalidValue;
+    if (a.flux_aet) return launch_cell_chain_variant<4, true>(a, H, s); // flux outputs: one variant
+    switch (occ) {
+    case 6: return launch_cell_chain_o6(a, H, s);
+    case 8: return launch_cell_chain_o8(a, H, s);
+    default: return launch_cell_chain_variant<4>(a, H, s);
     }
-    return cudaGetLastError();
 }
 
 } // namespace mhm

@@ -1,0 +1,13 @@
+// cell_chain_o8.cu -- the cell-chain kernel with registers sized for 8
+// resident blocks per SM (more warps to hide latency, some values spilled).
+#include "cell_chain_impl.cuh"
+
+namespace mhm {
+
+cudaError_t launch_cell_chain_o8(const CellArgs &a, int H, cudaStream_t s)
+{
+    if (H < 1 || H > kMaxHorizons) return cudaErrorInvalidValue;
+    return launch_cell_chain_variant<8>(a, H, s);
+}
+
+} // namespace mhm

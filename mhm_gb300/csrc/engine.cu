@@ -22,7 +22,7 @@
 #include "network.h"
 
 namespace mhm {
-cudaError_t launch_cell_chain(const CellArgs &a, int H, cudaStream_t s);
+cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s);
 cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
                               int32_t stride, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
@@ -107,8 +107,21 @@ struct mhm_ctx {
     bool pending_outputs = false;
     // forcing
     ForcingSrc forc[5];
+    // gauge series of the calls in flight: device -> pinned staging (an
+    // asynchronous copy; a copy into pageable memory would block the host
+    // until the routing finished) -> the caller's buffer at the next
+    // synchronisation point
+    struct GaugeStage {
+        double *pinned = nullptr;
+        size_t cap = 0, bytes = 0;
+        double *dst = nullptr;
+        cudaEvent_t ev = nullptr;
+        bool active = false;
+    } qg_stage[2];
     // outputs
-    int32_t out_tro = 0, out_qmod = 0;
+    int32_t out_tro = 0, out_qmod = 0, out_flux = 0;
+    DevBuf<double> flux_d[2];
+    std::vector<double> host_aet, host_loss;
     std::vector<double> host_tro, host_qmod;
     int32_t last_steps = 0;
     // execution
@@ -122,6 +135,19 @@ struct mhm_ctx {
     double t_ms[4] = {0, 0, 0, 0};
     size_t chunk_bytes = (size_t)8 << 30;
     int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
+    int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
+    // member mode (mhm_run_members_async) and device-resident state snapshots
+    DevBuf<StepInfo> steps_all;
+    int64_t steps_all_filled = 0;
+    // per-call member table in a ring: a call may be enqueued while the
+    // routing of earlier calls (on route_stream) still reads theirs
+    DevBuf<int32_t> member_s0[4];
+    cudaEvent_t ev_members_done[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t member_calls = 0;
+    const int32_t *member_s0_cur = nullptr;
+    std::vector<int32_t> member_s0_h;
+    DevBuf<double> snap;
+    int32_t n_snap = 0;
     // multiscale parameter regionalisation (after mhm_mpr_setup)
     bool mpr_ready = false;
     MprSetup mpr;
@@ -460,6 +486,10 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         int v = std::atoi(s);
         if (v >= 1 && v <= 16) ctx->route_sub = v;
     }
+    if (const char *s = std::getenv("MHM_CELL_OCC")) {
+        int v = std::atoi(s);
+        if (v == 4 || v == 6 || v == 8) ctx->cell_occ = v;
+    }
     *out = ctx;
     return MHM_OK;
 }
@@ -478,6 +508,12 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
         if (ctx->ev_acc_done[i]) cudaEventDestroy(ctx->ev_acc_done[i]);
     }
     if (ctx->ev_route_end) cudaEventDestroy(ctx->ev_route_end);
+    for (auto &st : ctx->qg_stage) {
+        if (st.pinned) cudaFreeHost(st.pinned);
+        if (st.ev) cudaEventDestroy(st.ev);
+    }
+    for (cudaEvent_t e : ctx->ev_members_done)
+        if (e) cudaEventDestroy(e);
     if (ctx->run_a) cudaEventDestroy(ctx->run_a);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
@@ -655,7 +691,18 @@ int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod)
 // same chunk on `route_stream`, so routing of chunk c overlaps the cell chain
 // of chunk c+1 (also across calls).  Double-buffered runoff and forcing
 // staging slots are guarded by events indexed by a per-context chunk counter.
-static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
+// hand a staged gauge series to the caller's buffer once its copy is done
+static int finish_gauge_stage(mhm_ctx *ctx, mhm_ctx::GaugeStage &st)
+{
+    if (!st.active) return MHM_OK;
+    CK(cudaEventSynchronize(st.ev), "gauge copy");
+    std::memcpy(st.dst, st.pinned, st.bytes);
+    st.active = false;
+    return MHM_OK;
+}
+
+static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge,
+                       const int32_t *member_tt0 = nullptr)
 {
     if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
@@ -663,8 +710,12 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     CK(cudaSetDevice(ctx->device), "set device");
     bool need[5] = {true, true, ctx->proc_pet != 1, ctx->proc_pet == 1, ctx->proc_pet == 1};
     const int32_t stride = (int32_t)std::lround(24.0 / (double)ctx->ntfd);
-    const int32_t first_row = (tt0 + stride - 1) / stride;
-    const int32_t last_row = (tt0 + n_steps - 1 + stride - 1) / stride;
+    const bool members = member_tt0 != nullptr;
+    if (members && (stride != 1 || ctx->ntfd != 24))
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "per-member steps need hourly steps with hourly forcing");
+    // member mode reads the first n_steps rows of the device forcing window
+    const int32_t first_row = members ? ctx->forc[0].row0 : (tt0 + stride - 1) / stride;
+    const int32_t last_row = members ? ctx->forc[0].row0 + n_steps - 1 : (tt0 + n_steps - 1 + stride - 1) / stride;
     int on_device = -1;
     int32_t row0_all = 0;
     for (int k = 0; k < 5; ++k) {
@@ -716,6 +767,11 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         }
     }
     if (ctx->out_tro) ctx->host_tro.assign((size_t)n_steps * M * N, 0.0);
+    if (ctx->out_flux) {
+        for (int k = 0; k < 2; ++k) CK(ctx->flux_d[k].ensure((size_t)ctx->tc_cap * M * N), "flux outputs");
+        ctx->host_aet.assign((size_t)n_steps * M * N, 0.0);
+        ctx->host_loss.assign((size_t)n_steps * M * N, 0.0);
+    }
     if (ctx->out_qmod) ctx->host_qmod.assign(M * (size_t)n_steps * L, 0.0);
     const int nchunks = (n_steps + Tc - 1) / Tc;
     auto chunk_rows = [&](int c, int32_t &r0, int32_t &r1) { // forcing rows iMeteoTS of the chunk
@@ -740,6 +796,37 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         CK(cudaEventRecord(ctx->ev_copied[slot], ctx->copy_stream), "record copied");
         return MHM_OK;
     };
+    if (members) {
+        if (!on_device) return fail(ctx, MHM_ERR_INVALID, "per-member steps need device forcing");
+        int32_t max_t0 = 0;
+        ctx->member_s0_h.assign(M, -1);
+        for (size_t m = 0; m < M; ++m) {
+            if (member_tt0[m] > 0) ctx->member_s0_h[m] = member_tt0[m] - 1;
+            max_t0 = std::max(max_t0, member_tt0[m]);
+        }
+        const int64_t need_steps = (int64_t)std::max(max_t0, 1) - 1 + n_steps;
+        if (need_steps > ctx->steps_all_filled) {
+            // calendar of steps 1 .. need_steps (grown in 8760-step blocks)
+            const int64_t cap = ((need_steps + 8759) / 8760) * 8760;
+            CK(cudaStreamSynchronize(ctx->stream), "sync");
+            CK(ctx->steps_all.ensure((size_t)cap), "member steps");
+            CK(launch_steps_fill(ctx->steps_all.p, 1, (int32_t)cap, ctx->jul_start, ctx->timestep, 1, ctx->stream),
+               "steps fill");
+            g_launches++;
+            ctx->steps_all_filled = cap;
+        }
+        const int r = (int)(ctx->member_calls & 3);
+        if (!ctx->ev_members_done[r]) {
+            CK(cudaEventCreateWithFlags(&ctx->ev_members_done[r], cudaEventDisableTiming), "event");
+        } else {
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_members_done[r], 0), "wait member table");
+        }
+        CK(ctx->member_s0[r].ensure(M), "member steps");
+        CK(cudaMemcpyAsync(ctx->member_s0[r].p, ctx->member_s0_h.data(), M * sizeof(int32_t), cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "member steps");
+        ctx->member_s0_cur = ctx->member_s0[r].p;
+    }
     if (ctx->timing && !ctx->run_a) {
         cudaEventCreate(&ctx->run_a);
         cudaEventRecord(ctx->run_a, ctx->stream);
@@ -751,10 +838,12 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         const int32_t nT = std::min(n_steps, s0 + Tc) - s0;
         const int slot = (int)((seq0 + c) & 1);
         // this chunk's calendar, computed on the device (stream-ordered before the cell chain)
-        CK(ctx->steps.ensure((size_t)ctx->tc_cap), "steps");
-        CK(launch_steps_fill(ctx->steps.p, tt0 + s0, nT, ctx->jul_start, ctx->timestep, stride, ctx->stream),
-           "steps fill");
-        g_launches++;
+        if (!members) {
+            CK(ctx->steps.ensure((size_t)ctx->tc_cap), "steps");
+            CK(launch_steps_fill(ctx->steps.p, tt0 + s0, nT, ctx->jul_start, ctx->timestep, stride, ctx->stream),
+               "steps fill");
+            g_launches++;
+        }
         // the runoff slot must have been consumed by the accumulation of chunk (seq - 2)
         if (ctx->slot_used[slot]) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_acc_done[slot], 0), "wait acc");
         CellArgs a{};
@@ -786,14 +875,25 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.tmin = fp[3];
         a.tmax = fp[4];
         a.steps = ctx->steps.p;
+        if (members) {
+            a.steps = ctx->steps_all.p;
+            a.member_step0 = ctx->member_s0_cur;
+            a.step_shift = s0;
+            a.reset_ok = !ctx->read_states;
+            a.reset_sm = 0;
+        }
         a.params = ctx->params.p;
         a.states = ctx->states.p;
         a.tro = ctx->tro[slot].p;
         a.latitude = ctx->latitude.p;
         a.tab = ctx->tab;
+        if (ctx->out_flux) {
+            a.flux_aet = ctx->flux_d[0].p;
+            a.flux_loss = ctx->flux_d[1].p;
+        }
         {
             Bracket br(ctx, 0, ctx->stream);
-            CK(launch_cell_chain(a, H, ctx->stream), "cell chain launch");
+            CK(launch_cell_chain(a, H, ctx->cell_occ, ctx->stream), "cell chain launch");
             br.done();
             g_launches++;
         }
@@ -801,6 +901,14 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             CK(cudaMemcpyAsync(ctx->host_tro.data() + (size_t)s0 * M * N, ctx->tro[slot].p,
                                (size_t)nT * M * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
                "tro D2H");
+        if (ctx->out_flux) {
+            CK(cudaMemcpyAsync(ctx->host_aet.data() + (size_t)s0 * M * N, ctx->flux_d[0].p,
+                               (size_t)nT * M * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+               "flux D2H");
+            CK(cudaMemcpyAsync(ctx->host_loss.data() + (size_t)s0 * M * N, ctx->flux_d[1].p,
+                               (size_t)nT * M * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+               "flux D2H");
+        }
         if (!on_device) CK(cudaEventRecord(ctx->ev_consumed[slot], ctx->stream), "record consumed");
         CK(cudaEventRecord(ctx->ev_cell_done[slot], ctx->stream), "record cell done");
         ctx->slot_used[slot] = true;
@@ -822,6 +930,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             acc.pos_l11_l1 = ctx->pos_l11_l1.p;
             acc.pos_area = ctx->pos_area.p;
             acc.qout = ctx->qout.p;
+            acc.member_step0 = members ? ctx->member_s0_cur : nullptr;
             {
                 Bracket br(ctx, 1, rs);
                 CK(launch_runoff_acc(acc, rs), "runoff acc launch");
@@ -847,6 +956,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         r.qmod = ctx->qmod.p;
         r.qtin1 = ctx->qtin1.p;
         r.qtr1 = ctx->qtr1.p;
+        r.member_step0 = members ? ctx->member_s0_cur : nullptr;
         {
             Bracket br(ctx, 2, rs);
             // wavefront: tick k advances sub-chunk k - l of level l
@@ -873,6 +983,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             g.gauge_pos = ctx->gauge_pos_d.p;
             g.qmod = ctx->qmod.p;
             g.q_gauge = ctx->q_gauge[(int)(ctx->call_seq & 1)].p;
+            g.member_step0 = members ? ctx->member_s0_cur : nullptr;
             CK(launch_gauge_gather(g, rs), "gauge launch");
             g_launches++;
         }
@@ -884,6 +995,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         if (c == nchunks - 1) {
             // qOUT and Qmod of the last step (restart fields)
             for (size_t m = 0; m < M; ++m) {
+                if (members && ctx->member_s0_h[m] < 0) continue; // idle member keeps its restart fields
                 CK(cudaMemcpyAsync(ctx->qout_last.p + m * L, ctx->qout.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
                                    cudaMemcpyDeviceToDevice, rs),
                    "qout last");
@@ -894,10 +1006,31 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         }
     }
     ctx->chunk_seq += nchunks;
-    if (q_gauge && ctx->proc_rout == 1 && ctx->G > 0)
-        CK(cudaMemcpyAsync(q_gauge, ctx->q_gauge[(int)(ctx->call_seq & 1)].p,
-                           M * (size_t)ctx->G * n_steps * sizeof(double), cudaMemcpyDeviceToHost, ctx->route_stream),
+    if (q_gauge && ctx->proc_rout == 1 && ctx->G > 0) {
+        auto &st = ctx->qg_stage[(int)(ctx->call_seq & 1)];
+        const size_t bytes = M * (size_t)ctx->G * n_steps * sizeof(double);
+        if (int rc = finish_gauge_stage(ctx, st)) return rc; // the call two back used this slot
+        if (st.cap < bytes) {
+            if (st.pinned) cudaFreeHost(st.pinned);
+            st.pinned = nullptr;
+            st.cap = 0;
+            CK(cudaMallocHost((void **)&st.pinned, bytes), "gauge staging");
+            st.cap = bytes;
+        }
+        if (!st.ev) CK(cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming), "event");
+        CK(cudaMemcpyAsync(st.pinned, ctx->q_gauge[(int)(ctx->call_seq & 1)].p, bytes, cudaMemcpyDeviceToHost,
+                           ctx->route_stream),
            "q_gauge D2H");
+        CK(cudaEventRecord(st.ev, ctx->route_stream), "record gauge copy");
+        st.dst = q_gauge;
+        st.bytes = bytes;
+        st.active = true;
+    }
+    if (members) {
+        // the table may be reused once this call's routing has finished
+        CK(cudaEventRecord(ctx->ev_members_done[ctx->member_calls & 3], ctx->route_stream), "record member table");
+        ctx->member_calls += 1;
+    }
     ctx->call_seq += 1;
     ctx->last_steps = n_steps;
     ctx->pending_outputs = ctx->out_tro || ctx->out_qmod;
@@ -919,6 +1052,8 @@ int mhm_sync(mhm_ctx *ctx)
     CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_route_end, 0), "join");
     CK(cudaStreamSynchronize(ctx->stream), "run sync");
     CK(cudaStreamSynchronize(ctx->copy_stream), "copy sync");
+    for (auto &st : ctx->qg_stage)
+        if (int rc = finish_gauge_stage(ctx, st)) return rc;
     harvest_timing(ctx);
     if (ctx->pending_outputs && ctx->out_qmod) { // routing-level positions -> node order
         const size_t L = ctx->L;
@@ -936,9 +1071,137 @@ int mhm_sync(mhm_ctx *ctx)
 int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 {
     if (!ctx) return MHM_ERR_INVALID;
-    if (ctx->out_tro || ctx->out_qmod)
+    if (ctx->out_tro || ctx->out_qmod || ctx->out_flux)
         return fail(ctx, MHM_ERR_INVALID, "per-step outputs need the synchronous mhm_run");
     return run_enqueue(ctx, tt0, n_steps, q_gauge);
+}
+
+int mhm_run_members_async(mhm_ctx *ctx, const int32_t *member_tt0, int32_t n_steps, double *q_gauge)
+{
+    if (!ctx || !member_tt0) return MHM_ERR_INVALID;
+    if (ctx->out_tro || ctx->out_qmod || ctx->out_flux)
+        return fail(ctx, MHM_ERR_INVALID, "per-step outputs need the synchronous mhm_run");
+    return run_enqueue(ctx, 1, n_steps, q_gauge, member_tt0);
+}
+
+int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots)
+{
+    if (!ctx || n_slots < 0) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    const size_t per = (size_t)n_state_planes(ctx->H) * ctx->N + 4 * (size_t)ctx->L;
+    ctx->snap.release();
+    ctx->n_snap = 0;
+    CK(ctx->snap.ensure(per * (size_t)n_slots), "snapshots");
+    ctx->n_snap = n_slots;
+    return MHM_OK;
+}
+
+// device-to-device copy of one member's states (cells and routing) to or from
+// a snapshot slot, ordered after all work enqueued on the context
+static int snapshot_copy(mhm_ctx *ctx, int32_t member, int32_t slot, bool save)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (member < 0 || member >= ctx->M || slot < 0 || slot >= ctx->n_snap)
+        return fail(ctx, MHM_ERR_INVALID, "member or snapshot slot out of range");
+    CK(cudaSetDevice(ctx->device), "set device");
+    const size_t N = ctx->N, L = ctx->L, ns = n_state_planes(ctx->H);
+    const size_t per = ns * N + 4 * L;
+    double *sp = ctx->snap.p + (size_t)slot * per;
+    struct Part {
+        double *member_ptr;
+        size_t n;
+    };
+    const Part parts[5] = {{ctx->states.p + (size_t)member * ns * N, ns * N},
+                           {ctx->qtin1.p ? ctx->qtin1.p + (size_t)member * L : nullptr, L},
+                           {ctx->qtr1.p ? ctx->qtr1.p + (size_t)member * L : nullptr, L},
+                           {ctx->qout_last.p ? ctx->qout_last.p + (size_t)member * L : nullptr, L},
+                           {ctx->qmod_last.p ? ctx->qmod_last.p + (size_t)member * L : nullptr, L}};
+    cudaStream_t s = ctx->stream;
+    CK(cudaEventRecord(ctx->ev_route_end, ctx->route_stream), "record route end");
+    CK(cudaStreamWaitEvent(s, ctx->ev_route_end, 0), "join");
+    size_t off = 0;
+    for (const Part &q : parts) {
+        if (q.member_ptr && q.n) {
+            double *dst = save ? sp + off : q.member_ptr;
+            const double *src = save ? q.member_ptr : sp + off;
+            CK(cudaMemcpyAsync(dst, src, q.n * sizeof(double), cudaMemcpyDeviceToDevice, s), "snapshot copy");
+        }
+        off += q.n;
+    }
+    return MHM_OK;
+}
+
+int mhm_snapshot_save(mhm_ctx *ctx, int32_t member, int32_t slot) { return snapshot_copy(ctx, member, slot, true); }
+
+int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member) { return snapshot_copy(ctx, member, slot, false); }
+
+int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out)
+{
+    if (!ctx || n_steps < 1) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    const size_t N = ctx->N, M = ctx->M, L = ctx->L, ns = n_state_planes(ctx->H);
+    // every trial starts from the same states: keep a device copy
+    DevBuf<double> keep;
+    const bool rout = ctx->proc_rout == 1 && L > 0;
+    const size_t n_cells_st = M * ns * N, n_rt = rout ? 4 * M * L : 0;
+    CK(keep.ensure(n_cells_st + n_rt), "autotune state copy");
+    double *const rt[4] = {ctx->qtin1.p, ctx->qtr1.p, ctx->qout_last.p, ctx->qmod_last.p};
+    auto copy_states = [&](bool save) -> int {
+        CK(cudaMemcpyAsync(save ? keep.p : ctx->states.p, save ? ctx->states.p : keep.p, n_cells_st * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream),
+           "state copy");
+        for (int i = 0; rout && i < 4; ++i)
+            CK(cudaMemcpyAsync(save ? keep.p + n_cells_st + i * M * L : rt[i],
+                               save ? rt[i] : keep.p + n_cells_st + i * M * L, M * L * sizeof(double),
+                               cudaMemcpyDeviceToDevice, ctx->stream),
+               "state copy");
+        return MHM_OK;
+    };
+    const int32_t out_t = ctx->out_tro, out_q = ctx->out_qmod, out_f = ctx->out_flux;
+    ctx->out_tro = ctx->out_qmod = ctx->out_flux = 0;
+    const int32_t occ0 = ctx->cell_occ, sub0 = ctx->route_sub;
+    int rc = copy_states(true);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int occs[3] = {4, 6, 8}, subs[3] = {4, 8, 16};
+    float best = 1e30f;
+    int best_occ = occ0, best_sub = sub0;
+    for (int trial = -1; rc == MHM_OK && trial < 9; ++trial) {
+        const int ti = trial < 0 ? 0 : trial;   // trial -1: untimed warm-up
+        ctx->cell_occ = occs[ti / 3];
+        ctx->route_sub = rout ? subs[ti % 3] : sub0;
+        if (!rout && ti % 3 != 0) continue;
+        if ((rc = copy_states(false))) break;
+        cudaEventRecord(e0, ctx->stream);
+        if ((rc = run_enqueue(ctx, tt0, n_steps, nullptr))) break;
+        if ((rc = mhm_sync(ctx))) break;
+        cudaEventRecord(e1, ctx->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = fail(ctx, MHM_ERR_CUDA, "autotune timing");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (trial >= 0 && ms_out) ms_out[trial] = ms;
+        if (trial >= 0 && ms < best) {
+            best = ms;
+            best_occ = ctx->cell_occ;
+            best_sub = ctx->route_sub;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->cell_occ = rc == MHM_OK ? best_occ : occ0;
+    ctx->route_sub = rc == MHM_OK ? best_sub : sub0;
+    ctx->out_tro = out_t;
+    ctx->out_qmod = out_q;
+    ctx->out_flux = out_f;
+    if (int r2 = copy_states(false)) rc = rc ? rc : r2;
+    if (int r3 = mhm_sync(ctx)) rc = rc ? rc : r3;
+    if (occ_out) *occ_out = ctx->cell_occ;
+    if (sub_out) *sub_out = ctx->route_sub;
+    return rc;
 }
 
 int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
@@ -947,6 +1210,29 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
     int rc = run_enqueue(ctx, tt0, n_steps, q_gauge);
     int rs = mhm_sync(ctx);
     return rc ? rc : rs;
+}
+
+int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    ctx->out_flux = on ? 1 : 0;
+    if (!on) {
+        for (auto &b : ctx->flux_d) b.release();
+        ctx->host_aet.clear();
+        ctx->host_loss.clear();
+    }
+    return MHM_OK;
+}
+
+int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    if (!ctx->out_flux) return fail(ctx, MHM_ERR_INVALID, "flux outputs are not enabled");
+    if (aet) std::memcpy(aet, ctx->host_aet.data(), ctx->host_aet.size() * sizeof(double));
+    if (loss) std::memcpy(loss, ctx->host_loss.data(), ctx->host_loss.size() * sizeof(double));
+    return MHM_OK;
 }
 
 int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)

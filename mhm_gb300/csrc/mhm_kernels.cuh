@@ -66,6 +66,18 @@ struct CellArgs {
     double *tro;                                  // [n_steps][M][n_cells]
     const double *latitude;                       // [n_cells]
     MonthTables tab;
+    // member mode (each member at its own model step; hourly, device forcing
+    // window shared by all members): member m's step t of this chunk is
+    // steps[member_step0[m] + step_shift + t] and reads window row
+    // step_shift + t; member_step0[m] < 0 marks an idle member (no work,
+    // zero runoff).  member_step0 == nullptr: all members at the same step.
+    const int32_t *member_step0;
+    int32_t step_shift;
+    int32_t reset_ok;   // member mode: SM = 0.5 * FC when a member is at its step 1
+    // optional per-step fluxes [n_steps][M][n_cells] (nullptr = off): total
+    // actual ET (canopy + sealed + soil, area weighted) and the percolation
+    // lost to (or, karstLoss > 1, gained from) outside the cell
+    double *flux_aet, *flux_loss;
 };
 
 struct AccArgs {
@@ -79,6 +91,7 @@ struct AccArgs {
     const int32_t *pos_l11_l1;    // [n_nodes] 0-based L1 cell of the node (!map_flag)
     const double *pos_area;       // [n_nodes] L11 area by position
     double *qout;                 // [M][n_steps][n_nodes] by level position
+    const int32_t *member_step0;  // member mode: < 0 marks an idle member (skipped)
 };
 
 // Wavefront routing: the chunk is cut into sub-chunks of `sub` steps; launch
@@ -97,6 +110,7 @@ struct RouteArgs {
     double *qtr;                // [M][n_steps][n_nodes] routed outflow series
     double *qmod;               // [M][n_steps][n_nodes] (if write_qmod)
     double *qtin1, *qtr1;       // [M][n_nodes] state (previous step)
+    const int32_t *member_step0; // member mode: < 0 marks an idle member (skipped)
 };
 
 struct GaugeArgs {
@@ -105,6 +119,7 @@ struct GaugeArgs {
     const int32_t *gauge_pos;
     const double *qmod;    // [M][n_steps][n_nodes]
     double *q_gauge;       // [M][n_gauges][total_steps]
+    const int32_t *member_step0; // member mode: idle members get zero discharge
 };
 
 // ---- multiscale parameter regionalisation ----

@@ -28,6 +28,7 @@ __global__ void __launch_bounds__(256) runoff_acc_kernel(const AccArgs a)
     const int64_t tm = gid / L; // t * M + m
     const int m = (int)(tm % a.n_members);
     const int t = (int)(tm / a.n_members);
+    if (a.member_step0 && a.member_step0[m] < 0) return; // idle member
     const double *row = a.tro + (size_t)tm * a.n_cells;
     double q;
     if (a.map_flag) {
@@ -57,6 +58,7 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (int64_t)width * a.n_members) return;
     const int m = (int)(gid / width);
+    if (a.member_step0 && a.member_step0[m] < 0) return; // idle member: routing states untouched
     const int pos = a.pos_begin + (int)(gid - (int64_t)m * width);
     const int s = a.tick - __ldg(a.pos_level + pos);
     const int t0 = s * a.sub;
@@ -114,7 +116,9 @@ __global__ void gauge_gather_kernel(const GaugeArgs a)
     const int64_t mg = gid / a.n_steps;
     const int g = (int)(mg % a.n_gauges);
     const int m = (int)(mg / a.n_gauges);
-    const double v = a.qmod[((size_t)m * a.n_steps + t) * a.n_nodes + __ldg(a.gauge_pos + g)];
+    const double v = (a.member_step0 && a.member_step0[m] < 0)
+                         ? 0.0
+                         : a.qmod[((size_t)m * a.n_steps + t) * a.n_nodes + __ldg(a.gauge_pos + g)];
     a.q_gauge[((size_t)m * a.n_gauges + g) * a.total_steps + a.step_offset + t] = v;
 }
 

@@ -249,6 +249,45 @@ class MhmGpu:
                     "mhm_run_async")
         self._last_steps = n_steps
 
+    def run_members_async(self, member_tt0, n_steps: int, q_out: np.ndarray | None = None):
+        """Enqueue n_steps for every member from its own step member_tt0[m]
+        (<= 0: idle); forcing = rows 0..n_steps-1 of the device window."""
+        t0 = np.ascontiguousarray(member_tt0, np.int32)
+        self._t0_keep = t0
+        self._check(self.L.mhm_run_members_async(self.ctx, _i(t0), n_steps, _d(q_out) if q_out is not None else None),
+                    "mhm_run_members_async")
+        self._last_steps = n_steps
+
+    def enable_fluxes(self, on: bool = True):
+        self._check(self.L.mhm_enable_fluxes(self.ctx, 1 if on else 0), "mhm_enable_fluxes")
+        self._fluxes = on
+
+    def get_fluxes(self) -> tuple[np.ndarray, np.ndarray]:
+        """(aET, karst loss) of the last run, each [step, member, cell]."""
+        n = self._last_steps
+        aet = np.zeros((n, self.n_members, self.dom.n_cells))
+        loss = np.zeros_like(aet)
+        self._check(self.L.mhm_get_fluxes(self.ctx, _d(aet), _d(loss)), "mhm_get_fluxes")
+        return aet, loss
+
+    def autotune(self, tt0: int, n_steps: int) -> dict:
+        """Pick the fastest cell-chain register variant and routing sub-chunk
+        by timing n_steps from tt0 (states restored afterwards)."""
+        occ = C.c_int32()
+        sub = C.c_int32()
+        ms = np.zeros(9)
+        self._check(self.L.mhm_autotune(self.ctx, tt0, n_steps, C.byref(occ), C.byref(sub), _d(ms)), "mhm_autotune")
+        return {"cell_blocks_per_sm": occ.value, "route_sub_steps": sub.value, "trial_ms": ms.tolist()}
+
+    def snapshot_alloc(self, n_slots: int):
+        self._check(self.L.mhm_snapshot_alloc(self.ctx, n_slots), "mhm_snapshot_alloc")
+
+    def snapshot_save(self, member: int, slot: int):
+        self._check(self.L.mhm_snapshot_save(self.ctx, member, slot), "mhm_snapshot_save")
+
+    def snapshot_load(self, slot: int, member: int):
+        self._check(self.L.mhm_snapshot_load(self.ctx, slot, member), "mhm_snapshot_load")
+
     def sync(self):
         self._check(self.L.mhm_sync(self.ctx), "mhm_sync")
 

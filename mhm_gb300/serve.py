@@ -1,0 +1,342 @@
+"""Serving loop: continuous batching of mHM + mRM runs on one GPU.
+
+A request is one forecast run on a basin of the catalogue: a global
+parameter vector (regionalised on the device by MPR), a horizon in hourly
+steps and a warm start from the basin's restart state, which stays resident
+on the device as a snapshot.  The server keeps, per basin with work, one
+context whose members are request slots; every iteration it
+
+  1. admits waiting requests into free slots (device MPR for the slot, the
+     restart snapshot loaded into it) -- creating a basin's context only when
+     its device footprint fits the HBM budget, and retiring contexts that
+     have gone idle to make room;
+  2. enqueues one chunk of steps for every context with work, each member at
+     its own model step (mhm_run_members_async), so the contexts' kernels
+     overlap on the device;
+  3. waits, hands each active slot its chunk of outlet discharge, and frees
+     the slots whose horizon is complete.
+
+Requests that arrive while others run join at the next chunk boundary of
+their basin's context.  A member's arithmetic does not depend on the other
+members, the slot it occupies or when it was admitted, so each result equals
+the same run executed alone (`run_alone`).
+
+Forcing: each basin has a device-resident window of `chunk` hourly rows that
+every chunk of every run reads (the synthetic forecast repeats every
+`chunk` steps), so admitting a run at any chunk boundary reads the same
+forcing it would alone.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import params as gparams
+from . import synth
+from .model import MhmGpu
+
+
+@dataclass
+class Basin:
+    name: str
+    dom: synth.Domain
+    l0: synth.L0Maps
+    window: tuple = ()          # device forcing window (pre, temp, pet) [chunk, N]
+    restart: dict | None = None  # host copy of the spun-up state (for run_alone)
+
+    @property
+    def n_cells(self) -> int:
+        return self.dom.n_cells
+
+
+@dataclass
+class Request:
+    rid: int
+    basin: int
+    gamma: np.ndarray
+    horizon: int                 # hourly steps
+    arrival: float = 0.0         # seconds after the start of the run
+    admitted: float | None = None
+    done: float | None = None
+    q: list = field(default_factory=list)
+
+    def discharge(self) -> np.ndarray:
+        """Outlet discharge [gauge, step] over the horizon."""
+        return np.concatenate(self.q, axis=1)[:, :self.horizon]
+
+    @property
+    def latency(self) -> float:
+        return (self.done - self.arrival) if self.done is not None else math.nan
+
+
+def context_bytes(basin: Basin, members: int, chunk: int, chunk_bytes: float = 8e9) -> int:
+    """Device footprint of a context with `members` slots (the library's
+    allocations: parameters, states, two runoff chunk slots, routing chunk
+    series, restart snapshot, forcing window, MPR tables)."""
+    N, H, L = basin.dom.n_cells, basin.dom.n_horizons, basin.dom.n_nodes
+    planes = 16 + 24 + 5 * H
+    tc = max(1, min(chunk, int(chunk_bytes // (2 * members * N * 8))))
+    b = members * (planes + 5 + H) * N * 8                # parameters + states
+    b += 2 * tc * members * N * 8                          # runoff chunk slots
+    b += 3 * members * tc * L * 8 + 8 * members * L * 8    # routing series + states + C1/C2
+    b += ((5 + H) * N + 4 * L) * 8                         # restart snapshot
+    b += 3 * chunk * N * 8                                 # forcing window
+    b += basin.l0.n_cells0 * 24 + members * 64 * 1024      # L0 slots, MPR tables
+    return int(b)
+
+
+class Server:
+    """Continuous-batching request loop over a catalogue of basins."""
+
+    def __init__(self, basins: list[Basin], hbm_budget: float = 150e9, chunk: int = 240, max_slots: int = 16,
+                 proc_sm: int = 1, proc_pet: int = 0, spinup_steps: int = 90 * 24, gamma_spinup=None,
+                 autotune: bool = False):
+        import torch
+        self.torch = torch
+        self.basins = basins
+        self.budget = hbm_budget
+        self.chunk = chunk
+        self.max_slots = max_slots
+        self.proc_sm, self.proc_pet = proc_sm, proc_pet
+        self.ctx: dict[int, dict] = {}          # basin -> {g, slots, tt0, bytes}
+        self.used = 0
+        self.waiting: list[Request] = []
+        self.finished: list[Request] = []
+        self.iterations = 0
+        self.cell_steps = 0
+        self.autotune = autotune
+        self.tuned: dict[str, dict] = {}
+        for b in basins:
+            if not b.window:
+                f = synth.make_forcing(b.dom, chunk, seed=2)
+                b.window = tuple(torch.from_numpy(f[k]).cuda() for k in ("pre", "temp", "pet"))
+            if b.restart is None:
+                b.restart = self._spin_up(b, spinup_steps, gamma_spinup)
+
+    # ---- basin set-up ----
+    def _spin_up(self, b: Basin, steps: int, gamma) -> dict:
+        """Default states advanced `steps` hourly steps with the namelist
+        parameters: the warm start every request of the basin begins from."""
+        g = MhmGpu(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=1)
+        try:
+            g.mpr_setup(b.l0)
+            gam = gamma if gamma is not None else gparams.default_gamma(self.proc_sm, self.proc_pet, 1, b.l0.n_geo)
+            g.mpr(gam)
+            g.init_states(0)
+            for c in range(math.ceil(steps / self.chunk)):   # steps == 0: default states
+                n = min(self.chunk, steps - c * self.chunk)
+                tt0 = 1 + c * self.chunk
+                g.set_meteo(tt0, *[w[:n] for w in b.window], on_device=True)
+                g.run(tt0, n)
+            # states only: the Muskingum coefficients of a run come from its
+            # own parameter vector (mhm_mpr), not from the spin-up
+            return {k: v for k, v in g.get_state(0).items() if k not in ("C1", "C2")}
+        finally:
+            g.close()
+
+    def _open(self, bi: int, members: int) -> bool:
+        b = self.basins[bi]
+        need = context_bytes(b, members, self.chunk)
+        if self.used + need > self.budget:
+            return False
+        g = MhmGpu(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=members, read_states=True)
+        g.mpr_setup(b.l0)
+        g.snapshot_alloc(1)
+        g.set_state(b.restart, 0)
+        g.snapshot_save(0, 0)
+        g.set_meteo(1, *b.window, on_device=True)
+        if self.autotune:
+            # time the variants on the basin's first chunk with the namelist
+            # parameters and the warm start in every slot (states restored after)
+            g.mpr(np.tile(gparams.default_gamma(self.proc_sm, self.proc_pet, 1, b.l0.n_geo), (members, 1)))
+            for m in range(members):
+                g.snapshot_load(0, m)
+            t = g.autotune(1, self.chunk)
+            self.tuned[b.name] = {k: t[k] for k in ("cell_blocks_per_sm", "route_sub_steps")}
+        self.ctx[bi] = {"g": g, "slots": [None] * members, "tt0": np.zeros(members, np.int32), "bytes": need,
+                        "q": np.zeros((members, len(b.dom.gauge_node), self.chunk))}
+        self.used += need
+        return True
+
+    def _close(self, bi: int):
+        c = self.ctx.pop(bi)
+        c["g"].close()
+        self.used -= c["bytes"]
+
+    # ---- the loop ----
+    def submit(self, r: Request):
+        self.waiting.append(r)
+
+    def _admit(self, now: float):
+        still = []
+        for r in self.waiting:
+            if r.arrival > now:
+                still.append(r)
+                continue
+            c = self.ctx.get(r.basin)
+            if c is None:
+                want = min(self.max_slots, max(1, sum(1 for w in self.waiting
+                                                      if w.basin == r.basin and w.arrival <= now)))
+                if not self._open(r.basin, want):
+                    # make room: retire contexts without active slots
+                    for bi in [k for k, v in self.ctx.items() if all(s is None for s in v["slots"])]:
+                        self._close(bi)
+                    if not self._open(r.basin, want):
+                        still.append(r)
+                        continue
+                c = self.ctx[r.basin]
+            try:
+                slot = c["slots"].index(None)
+            except ValueError:
+                still.append(r)
+                continue
+            g = c["g"]
+            g.mpr(r.gamma, member0=slot)
+            g.snapshot_load(0, slot)
+            c["slots"][slot] = r
+            c["tt0"][slot] = 1
+            r.admitted = now
+        self.waiting = still
+
+    def step(self, now: float) -> bool:
+        """One iteration; returns False when there is nothing to do."""
+        self._admit(now)
+        active = [(bi, c) for bi, c in self.ctx.items() if any(s is not None for s in c["slots"])]
+        if not active:
+            return False
+        for bi, c in active:                       # enqueue every context's chunk ...
+            tt0 = np.where([s is not None for s in c["slots"]], c["tt0"], 0).astype(np.int32)
+            c["tt0_now"] = tt0
+            c["g"].run_members_async(tt0, self.chunk, c["q"])
+        t_done = None
+        for bi, c in active:                       # ... then wait for all of them
+            c["g"].sync()
+            t_done = time.perf_counter()
+            n = self.basins[bi].n_cells
+            for m, r in enumerate(c["slots"]):
+                if r is None or c["tt0_now"][m] <= 0:
+                    continue
+                r.q.append(c["q"][m].copy())
+                self.cell_steps += n * self.chunk
+                c["tt0"][m] += self.chunk
+                if c["tt0"][m] - 1 >= r.horizon:
+                    r.done = t_done - self._t0
+                    self.finished.append(r)
+                    c["slots"][m] = None
+        self.iterations += 1
+        return True
+
+    def serve(self, requests: list[Request], timeout_s: float = 600.0) -> dict:
+        """Run until every request is finished; arrivals follow their
+        `arrival` offsets in wall-clock time."""
+        for r in requests:
+            self.submit(r)
+        self._t0 = time.perf_counter()
+        while (self.waiting or any(any(s is not None for s in c["slots"]) for c in self.ctx.values())):
+            now = time.perf_counter() - self._t0
+            if now > timeout_s:
+                raise TimeoutError("serving loop did not drain in time")
+            if not self.step(now):
+                nxt = min((r.arrival for r in self.waiting), default=now)
+                time.sleep(max(0.0, min(0.05, nxt - now)))
+        wall = time.perf_counter() - self._t0
+        for bi in list(self.ctx):
+            self._close(bi)
+        return summarize(self.finished, wall, self.cell_steps)
+
+    def close(self):
+        for bi in list(self.ctx):
+            self._close(bi)
+
+
+def summarize(done: list[Request], wall: float, cell_steps: int) -> dict:
+    lat = np.array([r.latency for r in done])
+    return {"requests": len(done), "wall_s": wall, "throughput": cell_steps / wall,
+            "p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_s": float(np.percentile(lat, 99)) if lat.size else None}
+
+
+def run_alone(basin: Basin, r: Request, chunk: int, proc_sm: int = 1, proc_pet: int = 0,
+              g: MhmGpu | None = None) -> np.ndarray:
+    """The request on its own: one-member context, the ordinary mhm_run path,
+    same warm start and forcing window.  Returns [gauge, step]."""
+    own = g is None
+    if own:
+        g = MhmGpu(basin.dom, proc_soilmoist=proc_sm, proc_pet=proc_pet, n_members=1, read_states=True)
+        g.mpr_setup(basin.l0)
+    try:
+        g.mpr(r.gamma)
+        g.set_state(basin.restart, 0)
+        qs = []
+        for c in range(math.ceil(r.horizon / chunk)):
+            tt0 = 1 + c * chunk
+            g.set_meteo(tt0, *basin.window, on_device=True)
+            qs.append(g.run(tt0, chunk)[0])
+        return np.concatenate(qs, axis=1)[:, :r.horizon]
+    finally:
+        if own:
+            g.close()
+
+
+def serve_plain(basins: list[Basin], requests: list[Request], chunk: int, proc_sm: int = 1,
+                proc_pet: int = 0) -> dict:
+    """The one-run-at-a-time path: requests in arrival order, each on a
+    one-member context of its basin (contexts kept per basin)."""
+    ctxs: dict[int, MhmGpu] = {}
+    t0 = time.perf_counter()
+    cell_steps = 0
+    try:
+        for r in sorted(requests, key=lambda q: q.arrival):
+            now = time.perf_counter() - t0
+            if r.arrival > now:
+                time.sleep(r.arrival - now)
+            b = basins[r.basin]
+            if r.basin not in ctxs:
+                g = MhmGpu(b.dom, proc_soilmoist=proc_sm, proc_pet=proc_pet, n_members=1, read_states=True)
+                g.mpr_setup(b.l0)
+                ctxs[r.basin] = g
+            r.q = [run_alone(b, r, chunk, proc_sm, proc_pet, g=ctxs[r.basin])]
+            r.done = time.perf_counter() - t0
+            cell_steps += b.n_cells * chunk * math.ceil(r.horizon / chunk)
+        wall = time.perf_counter() - t0
+    finally:
+        for g in ctxs.values():
+            g.close()
+    return summarize(requests, wall, cell_steps)
+
+
+def make_catalogue(n: int, seed: int = 11, n_min: float = 1e3, n_max: float = 1e6, l0_factor: int = 2,
+                   h_min: int = 2, h_max: int = 6) -> list[Basin]:
+    """Basins with cell counts log-uniform in [n_min, n_max] (square-ish L1
+    grids), h_min..h_max soil horizons, their own fractal DEM / D8 network."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        cells = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        nr = max(8, int(round(math.sqrt(cells))))
+        nc = max(8, int(round(cells / nr)))
+        H = int(rng.integers(h_min, h_max + 1))
+        dom = synth.make_domain(nr, nc, H, l11_factor=4 if nr * nc > 4e4 else 2, seed=100 + i, dem_kind="fractal",
+                                fractal_beta=3.0, tilt=0.001)
+        l0 = synth.make_l0(dom, l0_factor, seed=200 + i)
+        out.append(Basin(name=f"basin{i}_{nr}x{nc}_H{H}", dom=dom, l0=l0))
+    return out
+
+
+def make_requests(basins: list[Basin], n: int, rate: float, seed: int = 12, h_min_days: int = 30,
+                  h_max_days: int = 365, proc_sm: int = 1, proc_pet: int = 0) -> list[Request]:
+    """Poisson arrivals at `rate` per second; each request a basin of the
+    catalogue, a parameter vector within the namelist bounds and a horizon
+    of h_min..h_max days hourly."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for i in range(n):
+        bi = int(rng.integers(0, len(basins)))
+        g = gparams.random_gammas(1, proc_sm, proc_pet, 1, basins[bi].l0.n_geo, seed=int(rng.integers(1 << 30)))[0]
+        days = int(rng.integers(h_min_days, h_max_days + 1))
+        reqs.append(Request(rid=i, basin=bi, gamma=g, horizon=24 * days, arrival=float(t[i])))
+    return reqs
