@@ -135,6 +135,12 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
  * the reference's L1_* arrays. */
 int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
 
+/* Floodplain impervious fraction of the links [nLinks] for the land-cover
+ * scene that starts (L11_nLinkFracFPimp(:, iLC) of src/mRM/mo_mrm_routing.f90
+ * follows the scene of the current year); the next mhm_set_routing_params /
+ * mhm_mpr computes C1/C2 with it. */
+int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp);
+
 /* Muskingum coefficients C1/C2 of `member` from the five routing parameters
  * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device). */
 int mhm_set_routing_params(mhm_ctx *ctx, int32_t member, const double *rout_param5);
@@ -253,7 +259,9 @@ int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t 
  * generate_soil_database (src/MPR/mo_soil_database.f90:387-518) and
  * L0_variable_init (src/MPR/mo_mpr_startup.f90:237-337).  L0 cell arrays are
  * packed column-major over mask0 like the reference's level-0 arrays; all
- * class ids are 1-based. */
+ * class ids are 1-based.  Slope, aspect and LAI are taken as read_data leaves
+ * them (src/MPR/mo_read_wrapper.f90:282-283, 335-336: slope >= 0.01,
+ * aspect >= 1, LAI within [1e-10, 30]). */
 typedef struct {
     int32_t n_cells0;          /* level0%nCells                                  */
     int32_t nrows0, ncols0;    /* level0 grid                                    */

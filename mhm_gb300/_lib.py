@@ -84,7 +84,7 @@ EXPORTS = [
     "mhm_mpr_setup", "mhm_gamma_layout", "mhm_mpr", "mhm_mpr_get_aux", "mhm_get_eff_params",
     "mhm_soil_weights", "mhm_slope_emp", "mhm_mpr_noalloc",
     "mhm_run_members_async", "mhm_snapshot_alloc", "mhm_snapshot_save", "mhm_snapshot_load", "mhm_autotune",
-    "mhm_enable_fluxes", "mhm_get_fluxes",
+    "mhm_enable_fluxes", "mhm_get_fluxes", "mhm_set_link_fpimp",
 ]
 
 _LIB = None
@@ -147,6 +147,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_snapshot_alloc.argtypes = [vp, C.c_int32]
     L.mhm_autotune.argtypes = [vp, C.c_int32, C.c_int32, _ip, _ip, _dp]
     L.mhm_enable_fluxes.argtypes = [vp, C.c_int32]
+    L.mhm_set_link_fpimp.argtypes = [vp, _dp]
     L.mhm_get_fluxes.argtypes = [vp, _dp, _dp]
     L.mhm_snapshot_save.argtypes = [vp, C.c_int32, C.c_int32]
     L.mhm_snapshot_load.argtypes = [vp, C.c_int32, C.c_int32]

@@ -566,6 +566,18 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
     return MHM_OK;
 }
 
+int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
+{
+    if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still use the old fractions
+    if (ctx->n_links == 0) return MHM_OK;
+    CK(cudaMemcpyAsync(ctx->ffp.p, ffp_imp, (size_t)ctx->n_links * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "fpimp");
+    CK(cudaStreamSynchronize(ctx->stream), "fpimp sync");
+    return MHM_OK;
+}
+
 int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 {
     if (!ctx || !p) return MHM_ERR_INVALID;

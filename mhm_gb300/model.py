@@ -130,6 +130,11 @@ class MhmGpu:
         a = np.ascontiguousarray(p5, np.float64)
         self._check(self.L.mhm_set_routing_params(self.ctx, member, _d(a)), "mhm_set_routing_params")
 
+    def set_link_fpimp(self, ffp):
+        """Floodplain impervious fraction of the links for a new land-cover scene."""
+        a = np.ascontiguousarray(ffp, np.float64)
+        self._check(self.L.mhm_set_link_fpimp(self.ctx, _d(a)), "mhm_set_link_fpimp")
+
     def init_states(self, member: int = 0):
         hd = np.ascontiguousarray(self.dom.horizon_depth, np.float64)
         self._check(self.L.mhm_init_states(self.ctx, member, _d(hd)), "mhm_init_states")

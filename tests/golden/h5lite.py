@@ -29,6 +29,12 @@ class H5File:
         if self.b[:8] != SIG:
             raise ValueError("not an HDF5 file")
         ver = self.b[8]
+        if ver in (2, 3):
+            if self.b[9] != 8 or self.b[10] != 8:
+                raise NotImplementedError("offset/length sizes other than 8")
+            self.base = self.u64(12)
+            self.root = self.u64(36)            # root group object header address
+            return
         if ver not in (0, 1):
             raise NotImplementedError(f"superblock version {ver}")
         if self.b[13] != 8 or self.b[14] != 8:

@@ -1,0 +1,146 @@
+#!/usr/bin/env python3
+"""Build tests/golden/case00_run.npz: everything besides the parameter
+regionalisation that the reference's regression case check/case_00 feeds its
+time loop, and what the loop produced.
+
+Inputs (from the reference tree at REF): daily meteo (test_domain
+pre/tavg/pet netCDF-4, L2 = L1 = 24 km) for the simulated period 1990-01-01
+.. 1991-06-30 (181 warm-up days + the evaluation year), the L11 network mRM
+built (L11_fromN/toN/netPerm/length/slope, the floodplain impervious
+fraction per land-cover scene, cell areas, the gauge node) from
+b1_mRM_restart_001.nc, and case_00's mhm.nml meteo tables.  Outputs: the
+daily simulated discharge of b1_daily_discharge.out and the final states of
+both restart files.  Cell arrays are packed column-major over mHM's (x, y)
+L1 mask, i.e. in the row-major order of the north-first grids.
+
+Also writes case10_gold.npz and case12_gold.npz: check/case_10 and case_12
+run the same inputs with soil-moisture cases 3 and 4 and the LAI-based PET
+correction (processCase(5) = -1); their parameter vectors (from their
+mhm_parameter.nml), L1 parameters, final states and daily discharge.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import h5lite  # noqa: E402
+
+REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+TD = REF / "test_domain" / "input"
+CASE = REF / "check" / "case_00"
+
+# case_00 mhm.nml: &nightdayratio, &panevapo
+FNIGHT_PET = [0.1] * 12
+FNIGHT_PREC = [0.46, 0.5, 0.52, 0.51, 0.48, 0.5, 0.49, 0.48, 0.52, 0.56, 0.5, 0.47]
+FNIGHT_TEMP = [-0.76, -1.3, -1.88, -2.38, -2.72, -2.75, -2.74, -3.04, -2.44, -1.6, -0.94, -0.53]
+EVAP_COEFF = [1.3, 1.2, 0.72, 0.75, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.5]
+FILE_START = (1989, 1, 1)     # meteo time axis: days since 1989-01-01
+SIM_START = (1990, 1, 1)      # eval_Per start 1990-07-01 minus warming_days 181
+SIM_DAYS = 546                # .. 1991-06-30
+WARMING_DAYS = 181
+SCENE2_FROM_DAY = 365         # land-cover scene 1991 from 1991-01-01 on
+
+
+def julday(y, m, d):
+    a = (14 - m) // 12
+    yy, mm = y + 4800 - a, m + 12 * a - 3
+    return d + (153 * mm + 2) // 5 + 365 * yy + yy // 4 - yy // 100 + yy // 400 - 32045
+
+
+def main():
+    mrm = h5lite.H5File(str(CASE / "output_save" / "b1_mRM_restart_001.nc"))
+    mhm = h5lite.H5File(str(CASE / "output_save" / "b1_mHM_restart_001.nc"))
+    mask1 = mrm.read("L1_domain_mask").astype(bool)          # [y][x], north first
+    mask11 = mrm.read("L11_domain_mask").astype(bool)
+    assert np.array_equal(mask1, mask11)
+    n = int(mask1.sum())
+    off = julday(*SIM_START) - julday(*FILE_START)
+    met = {}
+    for key, rel in (("pre", "pre/pre.nc"), ("temp", "tavg/tavg.nc"), ("pet", "pet/pet.nc")):
+        f = h5lite.H5File(str(TD / "meteo" / rel))
+        a = f.read({"temp": "tavg"}.get(key, key))
+        t = f.read("time")
+        assert t[off] == off and a.shape[1:] == mask1.shape
+        met[key] = np.ascontiguousarray(a[off:off + SIM_DAYS][:, mask1])
+    n_links = int(mrm.read("L11_fromN").size) - 1
+    ffp = mrm.read("L11_nLinkFracFPimp")                      # [scene][y][x], link i at packed position i
+    q = np.loadtxt(CASE / "output_save" / "b1_daily_discharge.out", skiprows=1)
+    gold_states = {}
+    for name in ("L1_Inter", "L1_snowPack", "L1_sealSTW", "L1_unsatSTW", "L1_satSTW"):
+        gold_states[name] = mhm.read(name)[mask1]
+    sm = mhm.read("L1_soilMoist")                             # [horizon][y][x]
+    gold_states["L1_soilMoist"] = np.stack([sm[h][mask1] for h in range(sm.shape[0])])
+    for name in ("L11_qOUT", "L11_Qmod", "L11_C1", "L11_C2"):
+        gold_states[name] = mrm.read(name)[mask11]
+    for name in ("L11_qTIN", "L11_qTR"):                      # [IT][y][x]
+        a = mrm.read(name)
+        gold_states[name] = np.stack([a[i][mask11] for i in range(a.shape[0])])
+    np.savez_compressed(
+        HERE / "case00_run.npz",
+        pre=met["pre"], temp=met["temp"], pet=met["pet"], jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
+        warming_days=WARMING_DAYS, scene2_from_day=SCENE2_FROM_DAY,
+        from_n=mrm.read("L11_fromN").astype(np.int32), to_n=mrm.read("L11_toN").astype(np.int32),
+        net_perm=mrm.read("L11_netPerm").astype(np.int32), r_order=mrm.read("L11_rOrder").astype(np.int32),
+        length=mrm.read("L11_length")[:n_links], slope=mrm.read("L11_slope")[:n_links],
+        ffp_imp=np.stack([ffp[s][mask11][:n_links] for s in range(ffp.shape[0])]),
+        gauge_node=mrm.read("gaugeNodeList").astype(np.int32),
+        l1_l11_id=mrm.read("L1_L11_Id")[mask1].astype(np.int32),
+        l11_l1_id=mrm.read("L11_L1_Id")[mask11].astype(np.int32),
+        l1_area_km2=mrm.read("L1_domain_cellarea")[mask1], l11_area_km2=mrm.read("L11_domain_cellarea")[mask11],
+        latitude=mrm.read("L1_domain_lat")[mask1],
+        evap_coeff=np.array(EVAP_COEFF), fnight_pet=np.array(FNIGHT_PET), fnight_prec=np.array(FNIGHT_PREC),
+        fnight_temp=np.array(FNIGHT_TEMP), gold_q_daily=q[:, 5], gold_q_dmy=q[:, 1:4].astype(np.int32),
+        **{"gold_" + k: v for k, v in gold_states.items()})
+    print("wrote", HERE / "case00_run.npz", "cells", n, "links", n_links, "days", SIM_DAYS)
+
+
+# ---- further check cases on the same inputs (only processCase differs) ----
+import make_case00_mpr as mpr_fix  # noqa: E402
+
+CASES = {"case_10": (3, -1), "case_12": (4, -1)}   # processCase(3), processCase(5); routing 1
+PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "karstLoss", "kfastFlow",
+               "kSlowFlow", "kBaseFlow", "kPerco", "tempThresh", "unsatThresh", "sealedThresh", "maxInter",
+               "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "petLAIcorFactor",
+               "jarvis_thresh_c1")
+
+
+def case_golds(case: str, proc_sm: int, proc_pet: int):
+    cdir = REF / "check" / case
+    mrm = h5lite.H5File(str(cdir / "output_save" / "b1_mRM_restart_001.nc"))
+    mhm = h5lite.H5File(str(cdir / "output_save" / "b1_mHM_restart_001.nc"))
+    mask1 = mhm.read("L1_domain_mask").astype(bool)
+    names = mhm.group()
+    gold = {}
+    for name in PARAM_NAMES:
+        if "L1_" + name not in names:
+            continue
+        a = mhm.read("L1_" + name)
+        if a.ndim == 2:
+            gold["p_" + name] = a[mask1][None]
+        else:   # leading dims: [scene][(horizon|month)] then the grid
+            lead = a.shape[:-2]
+            gold["p_" + name] = a.reshape(-1, *a.shape[-2:])[:, mask1].reshape(*lead, -1)
+    for name in ("L1_Inter", "L1_snowPack", "L1_sealSTW", "L1_unsatSTW", "L1_satSTW"):
+        gold["s_" + name] = mhm.read(name)[mask1]
+    sm = mhm.read("L1_soilMoist")
+    gold["s_L1_soilMoist"] = np.stack([sm[h][mask1] for h in range(sm.shape[0])])
+    for name in ("L11_qOUT", "L11_Qmod", "L11_C1", "L11_C2"):
+        gold["s_" + name] = mrm.read(name)[mask1]
+    q = np.loadtxt(cdir / "output_save" / "b1_daily_discharge.out", skiprows=1)
+    blocks = ["interception1", "snow1", f"soilmoisture{proc_sm}", "directRunoff1",
+              {-1: "PETminus1", 0: "PET0", 1: "PET1"}[proc_pet], "interflow1", "percolation1", "routing1",
+              "geoparameter"]
+    gamma = mpr_fix.namelist_values(cdir / "mhm_parameter.nml", blocks)
+    np.savez_compressed(HERE / f"{case.replace('_', '')}_gold.npz", gamma=np.array(gamma), proc_sm=proc_sm,
+                        proc_pet=proc_pet, q_daily=q[:, 5], **gold)
+    print("wrote", HERE / f"{case.replace('_', '')}_gold.npz", len(gamma), sorted(gold))
+
+
+if __name__ == "__main__":
+    main()
+    for c, (sm_case, pet_case) in CASES.items():
+        case_golds(c, sm_case, pet_case)

@@ -1,0 +1,204 @@
+"""The reference's own regression case pins the whole hot path end to end.
+
+check/case_00, case_10 and case_12 (test_domain, 24 km L1 = L11, 2 soil
+horizons; soil-moisture cases 1, 3 and 4; PET input corrected by aspect
+(case_00) or by LAI (case_10, 12); hourly steps
+with daily forcing disaggregated by the day/night ratios, PET input with
+aspect correction, Muskingum routing, land-cover scene 1981 for 1990 and
+1991 from 1991-01-01): 181 warm-up days from 1990-01-01, then the
+evaluation year.  Fixtures: tests/golden/case00_mpr.npz (regionalisation
+inputs) and case00_run.npz (forcing, the network mRM built, the
+reference's daily discharge output and final restart states; made by
+tests/golden/make_case00_run.py).
+
+Checked, for the oracle (libm and hmath builds) and the device: all 365
+daily discharges printed in b1_daily_discharge.out equal ours rounded to its
+7 decimals, and every final state of b1_mHM/b1_mRM_restart_001.nc (cell
+storages, soil moisture, routing states, C1/C2) is bit-identical for the
+libm build and within 1e-12 (a last-bit difference at most) for the hmath
+build and the device, which also equals the hmath build bit for bit."""
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from mhm_gb300 import params
+from oracle import oracle
+
+import test_case00_mpr as mpr_case
+
+FIX = Path(__file__).resolve().parent / "golden" / "case00_run.npz"
+H = 2
+Q_DECIMALS = 7           # the discharge file prints 7 decimals
+
+
+def load_run():
+    z = np.load(FIX)
+    n = int(z["l1_area_km2"].size)
+    doms = []
+    for scene in range(2):
+        doms.append(SimpleNamespace(
+            n_cells=n, n_horizons=H, n_nodes=n, n_outlets=1, timestep=1, jul_start=int(z["jul_start"]),
+            evap_coeff=z["evap_coeff"], fday_prec=1.0 - z["fnight_prec"], fnight_prec=z["fnight_prec"],
+            fday_pet=1.0 - z["fnight_pet"], fnight_pet=z["fnight_pet"], fday_temp=-1.0 * z["fnight_temp"],
+            fnight_temp=z["fnight_temp"], l1_area_km2=z["l1_area_km2"], l1_l11_id=z["l1_l11_id"],
+            l11_area_km2=z["l11_area_km2"], l11_l1_id=z["l11_l1_id"], net_perm=z["net_perm"],
+            from_n=z["from_n"], to_n=z["to_n"], length=z["length"], slope=z["slope"],
+            ffp_imp=np.ascontiguousarray(z["ffp_imp"][scene]), gauge_node=z["gauge_node"], latitude=z["latitude"],
+            horizon_depth=np.array([200.0, 1000.0])))
+    forcing = {"pre": z["pre"], "temp": z["temp"], "pet": z["pet"]}
+    return z, doms, forcing
+
+
+def daily_means(q_steps, warming_days):
+    """sum(Q(iS:iE)) / 24 over each evaluation day, summed in step order
+    (src/mRM/mo_mrm_write.f90:138-149)."""
+    days = q_steps[warming_days * 24:].reshape(-1, 24)
+    return np.cumsum(days, axis=1)[:, -1] / 24.0
+
+
+# mHM() reads these with land-cover index 1 whatever the scene
+# (src/mHM/mo_mhm_interface_run.f90:439-451), and mpr() rewrites index 1 in
+# every pass of its scene loop: a multi-scene run uses the values of the
+# LAST scene throughout (maxInter and sealedThresh do not depend on the scene)
+SCENE_INDEPENDENT = ("unsatThresh", "karstLoss", "sealedThresh", "jarvis_thresh_c1")
+
+
+GOLD_DIR = Path(__file__).resolve().parent / "golden"
+# check case -> (processCase(3), processCase(5)); all on the test_domain inputs
+CASES = {"case_00": (1, 0), "case_10": (3, -1), "case_12": (4, -1)}
+
+
+def case_setup(case):
+    """(gamma, proc_sm, proc_pet, golds) of a check case: golds has the daily
+    discharge "q", final states "s_*" and L1 parameters "p_*"."""
+    if case == "case_00":
+        z = np.load(FIX)
+        gold = {"q": z["gold_q_daily"]}
+        gold.update({"s_" + k[5:]: z[k] for k in z.files if k.startswith("gold_L")})
+        return mpr_case.load_case()[2], 1, 0, gold
+    z = np.load(GOLD_DIR / f"{case.replace('_', '')}_gold.npz")
+    gold = {"q": z["q_daily"]}
+    gold.update({k: z[k] for k in z.files if k[:2] in ("s_", "p_")})
+    return z["gamma"], int(z["proc_sm"]), int(z["proc_pet"]), gold
+
+
+def regionalised(kind, gamma, proc_sm=1, proc_pet=0):
+    l0_for, _, _, n1 = mpr_case.load_case()
+    off = params.layout(proc_sm, proc_pet, 1, 10)
+    out = []
+    for scene in range(2):
+        r = oracle.oracle_mpr(n1, H, l0_for(scene), gamma, off, proc_sm, proc_pet, kind)
+        out.append({k: v for k, v in r.items() if k not in ("Wd", "slope_emp", "horizon_depth")})
+    for k in SCENE_INDEPENDENT:
+        out[0][k] = out[-1][k]
+    return out, gamma[off[7]:off[7] + 5]
+
+
+def check_states(g, st, rtol=0.0):
+    gold = {"interc": g["s_L1_Inter"], "snowpack": g["s_L1_snowPack"], "sealSTW": g["s_L1_sealSTW"],
+            "unsatSTW": g["s_L1_unsatSTW"], "satSTW": g["s_L1_satSTW"],
+            "soilMoist": g["s_L1_soilMoist"].reshape(-1), "qOUT": g["s_L11_qOUT"], "Qmod": g["s_L11_Qmod"],
+            "C1": g["s_L11_C1"][:-1], "C2": g["s_L11_C2"][:-1]}
+    bad = {}
+    for k, want in gold.items():
+        got = np.asarray(st[k]).reshape(-1)[: want.size]
+        err = float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-300)))
+        if not (np.array_equal(got, want) or err <= rtol):
+            bad[k] = err
+    return bad
+
+
+# The libm oracle calls the C library's exp/log/pow as the reference's build
+# did and reproduces its states bit for bit; the hmath build (the device's
+# functions, <= 1 ulp from the C library's) may differ in the last bit.
+HMATH_RTOL = 1e-12
+
+
+@pytest.mark.parametrize("case", ["case_10", "case_12"])
+def test_oracle_mpr_reproduces_cases_10_12(case):
+    gamma, proc_sm, proc_pet, gold = case_setup(case)
+    l0_for, _, _, n1 = mpr_case.load_case()
+    off = params.layout(proc_sm, proc_pet, 1, 10)
+    names = dict(mpr_case.NAMES, petLAIcorFactor="petLAIcorFactor", jarvis_thresh_c1="jarvis_thresh_c1")
+    for scene in range(2):
+        r = oracle.oracle_mpr(n1, H, l0_for(scene), gamma, off, proc_sm, proc_pet, "hmath")
+        for gname, ename in names.items():
+            if "p_" + gname not in gold:
+                continue
+            want = mpr_case.gold_for({gname: gold["p_" + gname]}, gname, scene)
+            if gname == "petLAIcorFactor":
+                want = gold["p_" + gname][scene].reshape(-1)
+            if gname == "jarvis_thresh_c1":
+                want = gold["p_" + gname][0] if scene == 1 else None
+            if want is not None:
+                assert np.array_equal(r[ename], want), (case, scene, gname)
+
+
+@pytest.mark.parametrize("kind", ["libm", "hmath"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_oracle_reproduces_case_discharge_and_states(case, kind):
+    z, doms, forcing = load_run()
+    gamma, proc_sm, proc_pet, gold = case_setup(case)
+    p, rp = regionalised(kind, gamma, proc_sm, proc_pet)
+    n_steps = int(z["sim_days"]) * 24
+    s2 = int(z["scene2_from_day"]) * 24
+    r1 = oracle.OracleRun(doms[0], p[0], rout_param=rp, proc_sm=proc_sm, proc_pet=proc_pet, hourly=False, kind=kind)
+    q1, _, _ = r1.run(forcing, 1, 1, s2)
+    r2 = oracle.OracleRun(doms[1], p[1], rout_param=rp, proc_sm=proc_sm, proc_pet=proc_pet, hourly=False, kind=kind)
+    for k, v in r1.state.items():          # states carry over into the new land-cover scene
+        if k not in ("C1", "C2"):
+            np.copyto(r2.state[k], v)
+    q2, _, _ = r2.run(forcing, 1, s2 + 1, n_steps - s2)
+    q = np.concatenate([q1[:, 0], q2[:, 0]])
+    qd = daily_means(q, int(z["warming_days"]))
+    assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), (case, kind, np.abs(qd - gold["q"]).max())
+    st = dict(r2.state)
+    st["soilMoist"] = st.pop("SM")
+    st["unsatSTW"], st["satSTW"] = st.pop("unsat"), st.pop("sat")
+    bad = check_states(gold, st, 0.0 if kind == "libm" else HMATH_RTOL)
+    assert not bad, (case, bad)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", list(CASES))
+def test_gpu_reproduces_case_discharge_and_states(case):
+    from mhm_gb300.model import MhmGpu
+    z, doms, forcing = load_run()
+    l0_for, _, _, n1 = mpr_case.load_case()
+    gamma, proc_sm, proc_pet, gold = case_setup(case)
+    n_steps = int(z["sim_days"]) * 24
+    s2 = int(z["scene2_from_day"]) * 24
+    g = MhmGpu(doms[0], proc_soilmoist=proc_sm, proc_pet=proc_pet, hourly=False, n_members=1)
+    try:
+        g.mpr_setup(l0_for(1))            # the last scene's scene-independent parameters
+        g.mpr(gamma)
+        last = g.get_eff_params(0)
+        g.mpr_setup(l0_for(0))
+        g.mpr(gamma)
+        p0 = g.get_eff_params(0)
+        for k in SCENE_INDEPENDENT:
+            p0[k] = last[k]
+        g.set_eff_params(p0)
+        g.init_states(0)
+        g.set_meteo(1, forcing["pre"], forcing["temp"], forcing["pet"])
+        q1 = g.run(1, s2)[0, 0]
+        g.mpr_setup(l0_for(1))            # land-cover scene 1991: new parameters, states kept
+        g.set_link_fpimp(doms[1].ffp_imp)
+        g.mpr(gamma)                      # (its scene-independent values are the ones already used)
+        q2 = g.run(s2 + 1, n_steps - s2)[0, 0]
+        st = g.get_state(0)
+    finally:
+        g.close()
+    q = np.concatenate([q1, q2])
+    qd = daily_means(q, int(z["warming_days"]))
+    assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), np.abs(qd - gold["q"]).max()
+    bad = check_states(gold, st, HMATH_RTOL)
+    assert not bad, bad
+    # and the device equals the oracle's hmath build bit for bit
+    p, rp = regionalised("hmath", gamma, proc_sm, proc_pet)
+    r1 = oracle.OracleRun(doms[0], p[0], rout_param=rp, proc_sm=proc_sm, proc_pet=proc_pet, hourly=False,
+                          kind="hmath")
+    o1, _, _ = r1.run(forcing, 1, 1, s2)
+    assert np.array_equal(o1[:, 0], q1)
