@@ -197,7 +197,7 @@ def run_gpu(args) -> dict:
     pre, temp, pet = device_forcing(dom, chunk, seed=2 + rank, device=device)
     stream = torch.cuda.ExternalStream(g.stream, device=device)
     g.set_meteo(1, pre, temp, pet, on_device=True)
-    tune = g.autotune(1, chunk)   # register variant x routing sub-chunk, states restored
+    tune = None if args.no_autotune else g.autotune(1, chunk)   # register variant x routing sub-chunk
 
     G = len(dom.gauge_node)
     qbufs = [np.zeros((1, G, chunk)) for _ in range(2)]
@@ -259,7 +259,7 @@ def run_gpu(args) -> dict:
     for h, d in zip(host, (pre, temp, pet)):
         h.copy_(d)
     hnp = [h.numpy() for h in host]
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, min(args.steps, 8))
     step(args.warmup + args.steps, on_device=False, host=hnp)  # warm the staging buffers
     g.sync()
     barrier()
@@ -351,7 +351,7 @@ def run_ensemble(args, device, plain_members: int = 8) -> dict:
     dom = synth.make_domain(E["nrows"], E["ncols"], E["H"], E["l11_factor"], seed=1, dem_kind="fractal",
                             fractal_beta=3.0, tilt=0.001)
     l0 = synth.make_l0(dom, E["l0_factor"], seed=4)
-    M, chunk, N = E["members"], E["chunk"], dom.n_cells
+    M, chunk, N = (args.ensemble_members or E["members"]), E["chunk"], dom.n_cells
     gam = gparams.random_gammas(M, 1, 0, 1, l0.n_geo, seed=3)
     pre, temp, pet = device_forcing(dom, chunk, seed=2, device=device)
     G = len(dom.gauge_node)
@@ -381,12 +381,15 @@ def run_ensemble(args, device, plain_members: int = 8) -> dict:
     for m in range(M):
         g.init_states(m)
     g.set_meteo(1, pre, temp, pet, on_device=True)
-    tune = g.autotune(1, 48)
+    tune = None if args.no_autotune else g.autotune(1, 48)
     qb = [np.zeros((M, G, chunk)) for _ in range(2)]
     timed(g, qb, 2, 0)                      # warm-up
     ms_b = timed(g, qb, K, 2)
     g.close()
     vb = float(M) * N * chunk * K / (ms_b * 1e-3)
+    if args.ensemble_no_plain:
+        return {"workload": f"calibration ensemble: L1 {E['nrows']}x{E['ncols']} ({N} cells), {M} parameter sets",
+                "value": vb, "unit": UNIT, "members": M, "ms_batched": ms_b, "autotune_batched": tune}
     # plain: one member per run, one after another
     p = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=1, device=device.index)
     p.mpr_setup(l0)
@@ -394,7 +397,7 @@ def run_ensemble(args, device, plain_members: int = 8) -> dict:
     p.mpr(gam[0])
     p.init_states(0)
     p.set_meteo(1, pre, temp, pet, on_device=True)
-    tune_p = p.autotune(1, 48)
+    tune_p = None if args.no_autotune else p.autotune(1, 48)
     timed(p, qp, 2, 0)                      # warm-up
     ms_p, mpr_p = 0.0, 0.0
     for m in range(plain_members):
@@ -542,6 +545,11 @@ def main():
     ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--ensemble-only", action="store_true", help="only the batched-ensemble measurement")
+    ap.add_argument("--ensemble-members", type=int, default=0, help="members of the ensemble (default 256)")
+    ap.add_argument("--ensemble-no-plain", action="store_true", help="skip the one-set-at-a-time comparison")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the kernel variant of MHM_CELL_OCC / MHM_ROUTE_SUB (for profiling)")
     ap.add_argument("--serve", action="store_true", help="measure the serving loop instead (p50/p99 latency)")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0, 500.0])
     ap.add_argument("--serve-requests", type=int, default=24)
@@ -556,6 +564,11 @@ def main():
         return
     if args.uneven:
         print(json.dumps(run_uneven(args)))
+        return
+    if args.ensemble_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_ensemble(args, torch.device("cuda", 0))))
         return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:

@@ -66,7 +66,9 @@ typedef struct {
     int32_t timestep;            /* model time step [h] (mhm.nml timestep)     */
     int32_t proc_soilmoist;      /* processMatrix(3,1): 1..4                   */
     int32_t proc_pet;            /* processMatrix(5,1): -1, 0 or 1             */
-    int32_t proc_routing;        /* processMatrix(8,1): 0 or 1                 */
+    int32_t proc_routing;        /* processMatrix(8,1): 0, 1 (Muskingum) or 2
+                                    (Muskingum with a routing time step chosen
+                                    from a constant celerity)                  */
     int32_t n_tstep_forcing_day; /* 24 (hourly forcing) or 1 (daily forcing)   */
     int32_t jul_start;           /* simPer%julStart (Julian day number)        */
     int32_t map_flag;            /* routing resolution >= hydrology resolution */
@@ -142,7 +144,14 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp);
 
 /* Muskingum coefficients C1/C2 of `member` from the five routing parameters
- * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device). */
+ * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device).  With
+ * routing case 2 rout_param5[0] is the streamflow celerity [m s-1]
+ * (mrm_update_param, src/mRM/mo_mrm_mpr.f90:241-329): the routing time step is
+ * the largest of the reference's allowed steps not above the shortest link's
+ * travel time; shorter than the model step, each step's runoff is routed
+ * that many times and the step's discharge is their mean; longer, runoff is
+ * summed over that many model steps, routed once and the result stands for
+ * each of them (then every mhm_run must cover whole routing steps). */
 int mhm_set_routing_params(mhm_ctx *ctx, int32_t member, const double *rout_param5);
 
 /* Default initial states (fluxes_states_default_init,

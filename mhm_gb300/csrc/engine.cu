@@ -27,6 +27,7 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
                               int32_t stride, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
 cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
+cudaError_t launch_qmod_step(const QmodStepArgs &a, cudaStream_t s);
 cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
 cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double TS, const double *length,
                             const double *slope, const double *ffp, const int32_t *link_pos, double *C1,
@@ -136,6 +137,9 @@ struct mhm_ctx {
     size_t chunk_bytes = (size_t)8 << 30;
     int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
     int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
+    // routing case 2: per-member routing time step [s] and the link lengths
+    std::vector<double> ts_rout, length_h;
+    DevBuf<double> qmod_sub;
     // member mode (mhm_run_members_async) and device-resident state snapshots
     DevBuf<StepInfo> steps_all;
     int64_t steps_all_filled = 0;
@@ -250,6 +254,62 @@ namespace {
 
 // processMatrix(:, 2) of src/MPR/mo_mpr_read_config.f90:390-990 (and the
 // routing block set there for mRM), accumulated into start offsets
+// Routing time steps [s] the adaptive routing can choose
+// (src/mRM/mo_mrm_constants.F90:42-46)
+constexpr double kGivenTS[19] = {60.0,    120.0,   180.0,   240.0,   300.0,   360.0,   600.0,
+                                 720.0,   900.0,   1200.0,  1800.0,  3600.0,  7200.0,  10800.0,
+                                 14400.0, 21600.0, 28800.0, 43200.0, 86400.0};
+
+// FORCES locate (in-tree copy pre-proc/mtCLIM/mo_utils.f90:1329-1346): index
+// (1-based) of the nearest table value, minus one when it lies above y (LE
+// with relative-epsilon equality)
+int locate_ts(double y)
+{
+    int c = 0;
+    double best = std::fabs(kGivenTS[0] - y);
+    for (int i = 1; i < 19; ++i)
+        if (std::fabs(kGivenTS[i] - y) < best) {
+            best = std::fabs(kGivenTS[i] - y);
+            c = i;
+        }
+    const double a = kGivenTS[c], eps = 2.220446049250313e-16;
+    const bool le = !(((eps * std::fabs(y) - std::fabs(a - y)) < 0.0) && (a > y));
+    return le ? c + 1 : c;
+}
+
+} // namespace
+
+// Routing case 2 for one member (mrm_update_param, src/mRM/mo_mrm_mpr.f90:
+// 241-329): K = length / celerity per link, TSrout from the smallest K,
+// Muskingum coefficients with xi = 0 (written at the links' positions).
+static int set_case2_member(mhm_ctx *ctx, int32_t m, double celerity)
+{
+    const size_t L = ctx->L;
+    const int nl = ctx->n_links;
+    if (nl == 0) return MHM_OK;
+    if (!(celerity > 0.0)) return fail(ctx, MHM_ERR_INVALID, "streamflow celerity must be positive");
+    const double xi = std::fabs(0.0); // rout_space_weight
+    double kmin = HUGE_VAL;
+    for (int i = 0; i < nl; ++i) kmin = std::min(kmin, ctx->length_h[i] / celerity);
+    int ind = locate_ts(kmin);
+    if (ind < 1) ind = 1;
+    const double ts = kGivenTS[ind - 1];
+    std::vector<double> c1(L, 0.0), c2(L, 0.0);
+    for (int i = 0; i < nl; ++i) {
+        const double K = ctx->length_h[i] / celerity;
+        const double a = ts / (K * (1.0 - xi) + 0.5 * ts);
+        c1[ctx->net.link_pos[i]] = a;
+        c2[ctx->net.link_pos[i]] = 1.0 - a * K / ts;
+    }
+    CK(cudaMemcpyAsync(ctx->C1.p + m * L, c1.data(), L * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "C1");
+    CK(cudaMemcpyAsync(ctx->C2.p + m * L, c2.data(), L * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "C2");
+    CK(cudaStreamSynchronize(ctx->stream), "C1/C2 sync");
+    ctx->ts_rout[m] = ts;
+    return MHM_OK;
+}
+
+namespace {
+
 bool gamma_layout(int32_t proc_sm, int32_t proc_pet, int32_t proc_rout, int32_t n_geo, GammaOffsets &o)
 {
     int32_t n_sm, n_pet, n_rout;
@@ -324,7 +384,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     if (d->timestep < 1 || 24 % d->timestep != 0) return bad("timestep must divide 24 hours");
     if (d->proc_soilmoist < 1 || d->proc_soilmoist > 4) return bad("proc_soilmoist must be 1..4");
     if (d->proc_pet < -1 || d->proc_pet > 1) return bad("proc_pet must be -1, 0 or 1 (2, 3 unsupported)");
-    if (d->proc_routing != 0 && d->proc_routing != 1) return bad("proc_routing must be 0 or 1");
+    if (d->proc_routing < 0 || d->proc_routing > 2) return bad("proc_routing must be 0, 1 or 2");
     if (d->n_tstep_forcing_day != 24 && d->n_tstep_forcing_day != 1)
         return bad("n_tstep_forcing_day must be 24 or 1");
     if (d->jul_start < 2299161) return bad("jul_start before the Gregorian reform is not supported");
@@ -355,7 +415,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
             ctx->tab.fnight_temp[i] = d->fnight_temp[i];
         }
     }
-    if (ctx->proc_rout == 1) {
+    if (ctx->proc_rout >= 1) {
         if (d->n_nodes < 1 || !d->l1_l11_id || !d->net_perm || !d->from_n || !d->to_n)
             return bad("routing arrays missing");
         if (!d->map_flag && (!d->l11_l1_id || !d->l11_area_km2)) return bad("L11_L1_Id/areas missing");
@@ -433,7 +493,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         cudaMemsetAsync(ctx->states.p, 0, ctx->states.n * sizeof(double), ctx->stream);
     }
     if (ok && ctx->proc_pet == 1) ok = ck(upload(ctx->latitude, d->latitude, N, ctx->stream), "latitude");
-    if (ok && ctx->proc_rout == 1) {
+    if (ok && ctx->proc_rout >= 1) {
         const LevelNetwork &net = ctx->net;
         // L1 cells of each node in ascending cell order, by position
         std::vector<int32_t> cnt(L + 1, 0), cells(N);
@@ -471,6 +531,8 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
             ctx->ss_max = mx;
         }
         ok = ok && ck(ctx->rout_p5.ensure(5 * M), "p5");
+        ctx->ts_rout.assign(M, 0.0);
+        if (ctx->n_links > 0) ctx->length_h.assign(d->length, d->length + ctx->n_links);
         for (auto *b : {&ctx->C1, &ctx->C2, &ctx->qtin1, &ctx->qtr1, &ctx->qout_last, &ctx->qmod_last}) {
             ok = ok && ck(b->ensure(M * L), "routing state");
             if (ok) cudaMemsetAsync(b->p, 0, M * L * sizeof(double), ctx->stream);
@@ -617,6 +679,7 @@ int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
     if (!ctx || !p5) return MHM_ERR_INVALID;
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (ctx->proc_rout == 2) return set_case2_member(ctx, m, p5[0]); // p5[0]: streamflow celerity [m s-1]
     if (ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
     if (ctx->n_links == 0) return MHM_OK;
     const size_t L = ctx->L;
@@ -653,7 +716,7 @@ int mhm_init_states(mhm_ctx *ctx, int32_t m, const double *hd)
     CK(cudaMemcpyAsync(ctx->states.p + (size_t)m * ns * N, s.data(), s.size() * sizeof(double),
                        cudaMemcpyHostToDevice, ctx->stream),
        "states");
-    if (ctx->proc_rout == 1) {
+    if (ctx->proc_rout >= 1) {
         const size_t L = ctx->L;
         for (auto *b : {&ctx->qtin1, &ctx->qtr1, &ctx->qout_last, &ctx->qmod_last})
             CK(cudaMemsetAsync(b->p + m * L, 0, L * sizeof(double), ctx->stream), "routing states");
@@ -748,13 +811,35 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     const size_t per_step = M * N * sizeof(double);
     int32_t Tc = (int32_t)std::max<size_t>(1, std::min<size_t>((size_t)n_steps, ctx->chunk_bytes / (2 * per_step)));
     if (!on_device) Tc = std::max<int32_t>(stride, Tc / stride * stride); // whole forcing rows per chunk
+    // routing case 2: routing time step shorter than the model step -> R routing
+    // passes per step; longer -> one pass per window of F steps
+    int32_t R = 1, F = 1;
+    if (ctx->proc_rout == 2 && ctx->L > 1) {
+        const double ts = ctx->ts_rout[0];
+        for (size_t m = 1; m < M; ++m)
+            if (ctx->ts_rout[m] != ts)
+                return fail(ctx, MHM_ERR_UNSUPPORTED, "members with different routing time steps");
+        if (!(ts > 0.0)) return fail(ctx, MHM_ERR_INVALID, "routing parameters not set");
+        const double f = ts / ((double)ctx->timestep * 3600.0);
+        if (f < 1.0)
+            R = std::max<int32_t>(1, (int32_t)std::lround(1.0 / f));
+        else
+            F = std::max<int32_t>(1, (int32_t)std::lround(f));
+        if (F > 1) {
+            if (members) return fail(ctx, MHM_ERR_UNSUPPORTED, "per-member steps with a multi-step routing window");
+            if ((tt0 - 1) % F != 0 || n_steps % F != 0)
+                return fail(ctx, MHM_ERR_INVALID,
+                            "runs must cover whole routing steps of " + std::to_string(F) + " model steps");
+            Tc = std::max<int32_t>(F, Tc / F * F);
+        }
+    }
     if (ctx->tc_cap < Tc) {
         // growing the per-chunk buffers: no older work may still use them
         CK(cudaStreamSynchronize(ctx->stream), "sync");
         CK(cudaStreamSynchronize(ctx->route_stream), "sync");
         CK(cudaStreamSynchronize(ctx->copy_stream), "sync");
         for (int s = 0; s < 2; ++s) CK(ctx->tro[s].ensure((size_t)Tc * M * N), "total runoff chunk");
-        if (ctx->proc_rout == 1) {
+        if (ctx->proc_rout >= 1) {
             CK(ctx->qout.ensure(M * (size_t)Tc * L), "qout chunk");
             CK(ctx->qtr.ensure(M * (size_t)Tc * L), "qtr chunk");
             CK(ctx->qmod.ensure(M * (size_t)Tc * L), "qmod chunk");
@@ -765,11 +850,19 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         ctx->stage_rows = max_rows;
         ctx->tc_cap = Tc;
     }
+    if ((R > 1 || F > 1) && ctx->proc_rout >= 1) {
+        const size_t need_rt = M * (size_t)ctx->tc_cap * R * L;
+        if (ctx->qtr.n < need_rt || ctx->qmod_sub.n < need_rt) {
+            CK(cudaStreamSynchronize(ctx->route_stream), "sync");
+            CK(ctx->qtr.ensure(need_rt), "qtr routing steps");
+            CK(ctx->qmod_sub.ensure(need_rt), "qmod routing steps");
+        }
+    }
     if (!on_device)
         for (int k = 0; k < 5; ++k)
             if (need[k])
                 for (int s = 0; s < 2; ++s) CK(ctx->stage[k][s].ensure((size_t)ctx->stage_rows * N), "forcing staging");
-    if (ctx->proc_rout == 1 && ctx->G > 0 && q_gauge) {
+    if (ctx->proc_rout >= 1 && ctx->G > 0 && q_gauge) {
         // one device gauge buffer per call in flight: ring of 2
         const int gs = (int)(ctx->call_seq & 1);
         if (ctx->qg_cap[gs] < M * (size_t)ctx->G * n_steps) {
@@ -927,14 +1020,15 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         // ---- routing of this chunk on route_stream ----
         cudaStream_t rs = ctx->route_stream;
         CK(cudaStreamWaitEvent(rs, ctx->ev_cell_done[slot], 0), "wait cell");
-        if (ctx->proc_rout == 1) {
+        if (ctx->proc_rout >= 1) {
             AccArgs acc{};
             acc.n_cells = ctx->N;
             acc.n_nodes = ctx->L;
             acc.n_members = ctx->M;
-            acc.n_steps = nT;
+            acc.n_steps = nT / F;
             acc.map_flag = ctx->map_flag;
-            acc.TST = 3600.0 * ctx->timestep;
+            acc.win = F;
+            acc.TST = 3600.0 * (ctx->timestep * F);
             acc.tro = ctx->tro[slot].p;
             acc.l1_area = ctx->l1_area.p;
             acc.node_cell_ptr = ctx->node_cell_ptr.p;
@@ -951,12 +1045,15 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             }
         }
         CK(cudaEventRecord(ctx->ev_acc_done[slot], rs), "record acc done");
-        if (ctx->proc_rout != 1) continue;
+        if (ctx->proc_rout < 1) continue;
         RouteArgs r{};
+        const int32_t n_rsteps = nT * R / F; // routing steps of the chunk
         r.n_nodes = ctx->L;
         r.n_members = ctx->M;
-        r.n_steps = nT;
-        r.sub = std::min(ctx->route_sub, nT);
+        r.n_steps = n_rsteps;
+        r.rdiv = R;
+        r.n_qsteps = nT / F;
+        r.sub = std::min(ctx->route_sub, n_rsteps);
         r.pos_level = ctx->pos_level.p;
         r.up_ptr = ctx->up_ptr.p;
         r.up_pos = ctx->up_pos.p;
@@ -965,7 +1062,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         r.C2 = ctx->C2.p;
         r.qout = ctx->qout.p;
         r.qtr = ctx->qtr.p;
-        r.qmod = ctx->qmod.p;
+        r.qmod = (R > 1 || F > 1) ? ctx->qmod_sub.p : ctx->qmod.p;
         r.qtin1 = ctx->qtin1.p;
         r.qtr1 = ctx->qtr1.p;
         r.member_step0 = members ? ctx->member_s0_cur : nullptr;
@@ -973,13 +1070,26 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             Bracket br(ctx, 2, rs);
             // wavefront: tick k advances sub-chunk k - l of level l
             const int D = ctx->net.n_levels;
-            const int n_sub = (nT + r.sub - 1) / r.sub;
+            const int n_sub = (n_rsteps + r.sub - 1) / r.sub;
             for (int k = 0; k < D + n_sub - 1; ++k) {
                 const int lo = std::max(0, k - n_sub + 1), hi = std::min(k, D - 1);
                 r.tick = k;
                 r.pos_begin = ctx->net.level_ptr[lo];
                 r.pos_end = ctx->net.level_ptr[hi + 1];
                 CK(launch_route_tick(r, rs), "route launch");
+                g_launches++;
+            }
+            if (R > 1 || F > 1) {
+                QmodStepArgs qs{};
+                qs.n_members = ctx->M;
+                qs.n_steps = nT;
+                qs.n_nodes = ctx->L;
+                qs.rdiv = R;
+                qs.win = F;
+                qs.qmod_sub = ctx->qmod_sub.p;
+                qs.qmod = ctx->qmod.p;
+                qs.member_step0 = r.member_step0;
+                CK(launch_qmod_step(qs, rs), "qmod step launch");
                 g_launches++;
             }
             br.done();
@@ -1008,7 +1118,8 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             // qOUT and Qmod of the last step (restart fields)
             for (size_t m = 0; m < M; ++m) {
                 if (members && ctx->member_s0_h[m] < 0) continue; // idle member keeps its restart fields
-                CK(cudaMemcpyAsync(ctx->qout_last.p + m * L, ctx->qout.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
+                const size_t nq = (size_t)(nT / F); // qOUT rows: one per routing step of the window mode
+                CK(cudaMemcpyAsync(ctx->qout_last.p + m * L, ctx->qout.p + (m * nq + (nq - 1)) * L, L * sizeof(double),
                                    cudaMemcpyDeviceToDevice, rs),
                    "qout last");
                 CK(cudaMemcpyAsync(ctx->qmod_last.p + m * L, ctx->qmod.p + (m * nT + (nT - 1)) * L, L * sizeof(double),
@@ -1018,7 +1129,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         }
     }
     ctx->chunk_seq += nchunks;
-    if (q_gauge && ctx->proc_rout == 1 && ctx->G > 0) {
+    if (q_gauge && ctx->proc_rout >= 1 && ctx->G > 0) {
         auto &st = ctx->qg_stage[(int)(ctx->call_seq & 1)];
         const size_t bytes = M * (size_t)ctx->G * n_steps * sizeof(double);
         if (int rc = finish_gauge_stage(ctx, st)) return rc; // the call two back used this slot
@@ -1154,7 +1265,7 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
     const size_t N = ctx->N, M = ctx->M, L = ctx->L, ns = n_state_planes(ctx->H);
     // every trial starts from the same states: keep a device copy
     DevBuf<double> keep;
-    const bool rout = ctx->proc_rout == 1 && L > 0;
+    const bool rout = ctx->proc_rout >= 1 && L > 0;
     const size_t n_cells_st = M * ns * N, n_rt = rout ? 4 * M * L : 0;
     CK(keep.ensure(n_cells_st + n_rt), "autotune state copy");
     double *const rt[4] = {ctx->qtin1.p, ctx->qtr1.p, ctx->qout_last.p, ctx->qmod_last.p};
@@ -1262,7 +1373,7 @@ int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
     if (st->soilMoist)
         CK(cudaMemcpy(st->soilMoist, S + (size_t)S_SM * N, (size_t)H * N * sizeof(double), cudaMemcpyDeviceToHost),
            "SM");
-    if (ctx->proc_rout == 1) {
+    if (ctx->proc_rout >= 1) {
         std::vector<double> buf(L);
         auto by_node = [&](const double *dev, double *out, size_t off) -> int {
             CK(cudaMemcpy(buf.data(), dev + m * L, L * sizeof(double), cudaMemcpyDeviceToHost), "routing state");
@@ -1308,7 +1419,7 @@ int mhm_set_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
     if (st->soilMoist)
         CK(cudaMemcpy(S + (size_t)S_SM * N, st->soilMoist, (size_t)H * N * sizeof(double), cudaMemcpyHostToDevice),
            "SM");
-    if (ctx->proc_rout == 1) {
+    if (ctx->proc_rout >= 1) {
         std::vector<double> buf(L);
         auto to_pos = [&](const double *in, double *dev) -> int {
             for (size_t v = 0; v < L; ++v) buf[ctx->net.pos_of_node[v]] = in[v];
@@ -1346,7 +1457,7 @@ int mhm_get_var(mhm_ctx *ctx, int32_t m, const char *name, double *out)
     else if (n == "L11_QMOD") st.Qmod = out;
     else if (n == "L11_QOUT") st.qOUT = out;
     else return fail(ctx, MHM_ERR_INVALID, "unknown variable " + n);
-    if ((st.Qmod || st.qOUT) && ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
+    if ((st.Qmod || st.qOUT) && ctx->proc_rout < 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
     return mhm_get_state(ctx, m, &st);
 }
 
@@ -1526,6 +1637,9 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
             g_launches++;
         }
     }
+    if (ctx->proc_rout == 2)
+        for (int32_t i = 0; i < n; ++i)
+            if (int rc = set_case2_member(ctx, member0 + i, gammas[(size_t)i * n_gamma + off.routing])) return rc;
     CK(cudaStreamSynchronize(s), "mpr sync");
     return MHM_OK;
 }
@@ -1555,6 +1669,7 @@ int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n
     if (!ctx || !gamma) return MHM_ERR_INVALID;
     if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
     if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (ctx->proc_rout == 2) return fail(ctx, MHM_ERR_UNSUPPORTED, "routing case 2: use mhm_mpr");
     const MprSetup &m = ctx->mpr;
     GammaOffsets off{};
     if (!gamma_layout(ctx->proc_sm, ctx->proc_pet, ctx->proc_rout, m.n_geo, off))

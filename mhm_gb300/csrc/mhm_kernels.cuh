@@ -81,9 +81,10 @@ struct CellArgs {
 };
 
 struct AccArgs {
-    int32_t n_cells, n_nodes, n_members, n_steps;
-    int32_t map_flag, pad_;
-    double TST;                  // HourSecs * timestep
+    int32_t n_cells, n_nodes, n_members, n_steps;   // n_steps: routing steps written to qout
+    int32_t map_flag;
+    int32_t win;                 // model steps summed per routing step (adaptive routing, else 1)
+    double TST;                  // HourSecs * routing timestep
     const double *tro;           // [n_steps][M][n_cells]
     const double *l1_area;       // [n_cells]
     const int32_t *node_cell_ptr; // [n_nodes+1] by level position
@@ -106,11 +107,26 @@ struct RouteArgs {
     const int32_t *up_pos;      // upstream positions in rank order
     const int8_t *pos_flags;    // bit0: is link (has C1/C2), bit1: add qOUT
     const double *C1, *C2;      // [M][n_nodes] by position
-    const double *qout;         // [M][n_steps][n_nodes]
+    // routing step s reads qOUT row s / rdiv of [M][n_qsteps][n_nodes]: with an
+    // adaptive routing step shorter than the model step the model step's qOUT
+    // is routed rdiv times
+    int32_t rdiv, n_qsteps;
+    const double *qout;
     double *qtr;                // [M][n_steps][n_nodes] routed outflow series
     double *qmod;               // [M][n_steps][n_nodes] (if write_qmod)
     double *qtin1, *qtr1;       // [M][n_nodes] state (previous step)
     const int32_t *member_step0; // member mode: < 0 marks an idle member (skipped)
+};
+
+// Per-model-step L11 discharge from the routing steps (adaptive routing):
+// rdiv > 1: the mean of the step's rdiv routing passes, ((0 + Q_1) + Q_2 ...)
+// / rdiv (src/mRM/mo_mrm_routing.f90:238-277); win > 1: the routing step's
+// value for each of its win model steps (src/mHM/mo_mhm_interface_run.f90:603-608)
+struct QmodStepArgs {
+    int32_t n_members, n_steps, n_nodes, rdiv, win;
+    const double *qmod_sub;     // [M][n_steps * rdiv / win][n_nodes]
+    double *qmod;               // [M][n_steps][n_nodes]
+    const int32_t *member_step0;
 };
 
 struct GaugeArgs {

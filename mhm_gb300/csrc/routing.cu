@@ -29,18 +29,28 @@ __global__ void __launch_bounds__(256) runoff_acc_kernel(const AccArgs a)
     const int m = (int)(tm % a.n_members);
     const int t = (int)(tm / a.n_members);
     if (a.member_step0 && a.member_step0[m] < 0) return; // idle member
-    const double *row = a.tro + (size_t)tm * a.n_cells;
+    // runoff of cell k for routing step t: the model step's value, or with a
+    // routing step of `win` model steps their sum from 0 in step order
+    // (RunToRout, src/mHM/mo_mhm_interface_run.f90:489-490)
+    const size_t row_stride = (size_t)a.n_members * a.n_cells;
+    const double *row = a.tro + ((size_t)t * a.win * a.n_members + m) * a.n_cells;
+    auto run = [&](int k) -> double {
+        if (a.win == 1) return __ldg(row + k);
+        double r = 0.0;
+        for (int j = 0; j < a.win; ++j) r = r + __ldg(row + j * row_stride + k);
+        return r;
+    };
     double q;
     if (a.map_flag) {
         double acc = 0.0;
         const int b = __ldg(a.node_cell_ptr + pos), e = __ldg(a.node_cell_ptr + pos + 1);
         for (int j = b; j < e; ++j) {
             const int k = __ldg(a.node_cells + j);
-            acc = acc + __ldg(row + k) * __ldg(a.l1_area + k);
+            acc = acc + run(k) * __ldg(a.l1_area + k);
         }
         q = acc * 1000.0 / a.TST;
     } else {
-        q = __ldg(row + __ldg(a.pos_l11_l1 + pos)) * __ldg(a.pos_area + pos) * 1000.0 / a.TST;
+        q = run(__ldg(a.pos_l11_l1 + pos)) * __ldg(a.pos_area + pos) * 1000.0 / a.TST;
     }
     a.qout[((size_t)m * a.n_steps + t) * L + pos] = q;
 }
@@ -81,9 +91,10 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
             if (t < nt) qtin[t] = qtin[t] + __ldcg(up + (size_t)t * L);
     }
     if (add_qout) {
+        const double *qo = a.qout + (size_t)m * a.n_qsteps * L + pos;
 #pragma unroll
         for (int t = 0; t < SUB; ++t)
-            if (t < nt) qtin[t] = qtin[t] + __ldcg(a.qout + base + (size_t)t * L + pos);
+            if (t < nt) qtin[t] = qtin[t] + __ldcg(qo + (size_t)((t0 + t) / a.rdiv) * L);
     }
     double qtin1 = a.qtin1[ms + pos];
     double qtr1 = a.qtr1[ms + pos];
@@ -104,6 +115,28 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
     }
     a.qtin1[ms + pos] = qtin1;
     a.qtr1[ms + pos] = qtr1;
+}
+
+__global__ void qmod_step_kernel(const QmodStepArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t L = a.n_nodes;
+    if (gid >= (int64_t)a.n_members * a.n_steps * L) return;
+    const int pos = (int)(gid % L);
+    const int64_t mt = gid / L;
+    const int t = (int)(mt % a.n_steps), m = (int)(mt / a.n_steps);
+    if (a.member_step0 && a.member_step0[m] < 0) return;
+    const int64_t n_sub = (int64_t)a.n_steps * a.rdiv / a.win;
+    const double *q = a.qmod_sub + (size_t)m * n_sub * L + pos;
+    double v;
+    if (a.rdiv > 1) {
+        double acc = 0.0;
+        for (int r = 0; r < a.rdiv; ++r) acc = acc + q[(size_t)(t * a.rdiv + r) * L];
+        v = acc / (double)a.rdiv;
+    } else {
+        v = q[(size_t)(t / a.win) * L];
+    }
+    a.qmod[((size_t)m * a.n_steps + t) * L + pos] = v;
 }
 
 // GaugeDischarge(gaugeIndexList) = L11_Qmod(gaugeNodeList), mo_mrm_routing.f90:299-301
@@ -160,6 +193,14 @@ cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s)
     else if (a.sub <= 8) route_tick_kernel<8><<<grid, 128, 0, s>>>(a);
     else if (a.sub <= 16) route_tick_kernel<16><<<grid, 128, 0, s>>>(a);
     else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_qmod_step(const QmodStepArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_members * a.n_steps * a.n_nodes;
+    if (n == 0) return cudaSuccess;
+    qmod_step_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

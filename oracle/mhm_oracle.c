@@ -709,6 +709,47 @@ void ora_default_states(const ora_domain *d, const double *horizon_depth, ora_st
  * do_time_step (src/mHM/mo_mhm_interface_run.f90:341-638) = meteo getters
  * (src/meteo/mo_meteo_handler.f90:915-1285) + mHM() (src/mHM/mo_mhm.f90:229-521)
  * + mRM_routing (src/mRM/mo_mrm_routing.f90:104-303, processCase 1). */
+/* src/mRM/mo_mrm_constants.F90:42-46 */
+static const double GIVEN_TS[19] = {60.0,   120.0,  180.0,   240.0,   300.0,   360.0,   600.0,
+                                    720.0,  900.0,  1200.0,  1800.0,  3600.0,  7200.0,  10800.0,
+                                    14400.0, 21600.0, 28800.0, 43200.0, 86400.0};
+
+/* FORCES locate (in-tree copy pre-proc/mtCLIM/mo_utils.f90:1329-1346): the
+ * index (1-based) of the nearest table value, minus one when that value is
+ * above y (LE with the relative-epsilon equality) */
+static int ora_locate(const double *x, int n, double y)
+{
+    int c = 0;
+    double best = fabs(x[0] - y);
+    for (int i = 1; i < n; ++i)
+        if (fabs(x[i] - y) < best) {
+            best = fabs(x[i] - y);
+            c = i;
+        }
+    return ora_le(x[c], y) ? c + 1 : c;
+}
+
+double ora_update_param_case2(double celerity, const double *length, int nLinks, double *C1, double *C2)
+{
+    const double xi = fabs(0.0); /* rout_space_weight */
+    double kmin = HUGE_VAL;
+    for (int i = 0; i < nLinks; ++i) {
+        double K = length[i] / celerity;
+        if (K < kmin)
+            kmin = K;
+    }
+    int ind = ora_locate(GIVEN_TS, 19, kmin);
+    if (ind < 1)
+        ind = 1;
+    const double ts = GIVEN_TS[ind - 1];
+    for (int i = 0; i < nLinks; ++i) {
+        double K = length[i] / celerity;
+        C1[i] = ts / (K * (1.0 - xi) + 0.5 * ts);
+        C2[i] = 1.0 - C1[i] * K / ts;
+    }
+    return ts;
+}
+
 int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
             int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff_out, double *qmod_out,
             int nthreads)
@@ -742,6 +783,30 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
     if (d->proc_rout == 1 && !d->read_states && L > 1)
         ora_reg_rout(d->rout_param, d->length, d->slope, d->ffp_imp, nLinks, (double)d->timestep,
                      s->C1, s->C2);
+    /* routing case 2: one routing time step for the run (mrm_init_param / mrm_update_param) and
+     * tsRoutFactor = TSrout / (timestep * HourSecs) (src/mHM/mo_mhm_interface_run.f90:480-511) */
+    double ts_factor = 1.0;
+    int rout_loop = 1, win = 1;
+    if (d->proc_rout == 2 && L > 1) {
+        const double tsrout = ora_update_param_case2(d->rout_param[0], d->length, nLinks, s->C1, s->C2);
+        ts_factor = tsrout / ((double)d->timestep * 3600.0);
+        if (ts_factor < 1.0) {
+            rout_loop = (int)lround(1.0 / ts_factor);
+            if (rout_loop < 1)
+                rout_loop = 1;
+        } else {
+            win = (int)lround(ts_factor);
+            if (!s->run_to_rout || (tt0 - 1) % win != 0 || nT % win != 0) {
+                free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
+                return -4; /* runs must cover whole routing steps */
+            }
+        }
+    }
+    double *qacc = (double *)malloc(sizeof(double) * (size_t)L);
+    if (!qacc) {
+        free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
+        return -2;
+    }
 
     for (int32_t it = 0; it < nT; ++it) {
         const int32_t tt = tt0 + it;
@@ -833,7 +898,7 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
         if (total_runoff_out)
             memcpy(total_runoff_out + (size_t)it * N, tro, sizeof(double) * (size_t)N);
 
-        /* mRM_routing, processCase 1 (mo_mrm_routing.f90:104-303): rout_loop = 1 */
+        /* mRM_routing, processCase 1 (mo_mrm_routing.f90:104-303): rout_loop = 1; case 2 below */
         if (d->proc_rout == 1) {
             ora_L11_runoff_acc(N, L, tro, d->l1_area_km2, d->l1_l11_id, d->l11_area_km2, d->l11_l1_id,
                                d->timestep, d->map_flag, s->qOUT);
@@ -851,8 +916,50 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
                     q_gauge[(size_t)it * d->nGauges + g] = s->Qmod[d->gauge_node[g] - 1];
             if (qmod_out)
                 memcpy(qmod_out + (size_t)it * L, s->Qmod, sizeof(double) * (size_t)L);
+        } else if (d->proc_rout == 2) {
+            int route_now = 1, ts_rout = d->timestep;
+            const double *run = tro;
+            if (win > 1) { /* accumulate until the routing step is complete (:489-511) */
+                for (int k = 0; k < N; ++k)
+                    s->run_to_rout[k] = s->run_to_rout[k] + tro[k];
+                route_now = (tt % win) == 0;
+                ts_rout = d->timestep * win;
+                run = s->run_to_rout;
+            }
+            if (route_now) {
+                ora_L11_runoff_acc(N, L, run, d->l1_area_km2, d->l1_l11_id, d->l11_area_km2, d->l11_l1_id,
+                                   ts_rout, d->map_flag, s->qOUT);
+                if (L > 1) {
+                    for (int i = 0; i < L; ++i)
+                        qacc[i] = 0.0;
+                    for (int r = 0; r < rout_loop; ++r) { /* mo_mrm_routing.f90:238-277 */
+                        ora_L11_routing(L, nLinks, d->net_perm, d->from_n, d->to_n, s->C1, s->C2, s->qOUT,
+                                        s->qTIN, s->qTR, s->Qmod);
+                        for (int i = 0; i < L; ++i)
+                            qacc[i] = qacc[i] + s->Qmod[i];
+                    }
+                    for (int i = 0; i < L; ++i)
+                        s->Qmod[i] = qacc[i] / (double)rout_loop;
+                } else {
+                    s->Qmod[0] = s->qOUT[0];
+                }
+                if (win > 1)
+                    for (int k = 0; k < N; ++k)
+                        s->run_to_rout[k] = 0.0;
+                /* the routed value stands for every model step of the routing step
+                 * (mRM_runoff copy-back, src/mHM/mo_mhm_interface_run.f90:603-608) */
+                for (int j = 0; j < win; ++j) {
+                    const int32_t jt = it - j;
+                    if (q_gauge)
+                        for (int g = 0; g < d->nGauges; ++g)
+                            q_gauge[(size_t)jt * d->nGauges + g] = s->Qmod[d->gauge_node[g] - 1];
+                    if (qmod_out)
+                        memcpy(qmod_out + (size_t)jt * L, s->Qmod, sizeof(double) * (size_t)L);
+                }
+            }
         }
     }
+    free(qacc);
     free(cal);
     free(pet_calc);
     free(temp_calc);

@@ -98,12 +98,17 @@ int ora_L11_set_network_topology(int nrows, int ncols, const int32_t *id2d /*[nc
 void ora_L11_routing_order(int nNodes, int nOutlets, const int32_t *fromN, const int32_t *toN,
                            int32_t *netPerm, int32_t *rOrder);
 
+/* Routing case 2 (mrm_update_param, src/mRM/mo_mrm_mpr.f90:241-329): K = length /
+ * celerity per link, the routing time step TSrout [s] = given_TS(locate(given_TS,
+ * min K)), C1/C2 with xi = 0.  Returns TSrout. */
+double ora_update_param_case2(double celerity, const double *length, int nLinks, double *C1, double *C2);
+
 /* ---- whole-domain run (the mhm_eval time loop for one domain) ---- */
 typedef struct {
     int32_t nCells, nH, nNodes, nOutlets, timestep;
     int32_t proc_sm;      /* processMatrix(3,1): 1..4 */
     int32_t proc_pet;     /* processMatrix(5,1): -1, 0, 1 */
-    int32_t proc_rout;    /* processMatrix(8,1): 0 or 1 */
+    int32_t proc_rout;    /* processMatrix(8,1): 0, 1 or 2 */
     int32_t nTstepForcingDay; /* 24 (hourly) or 1 (daily) */
     int32_t read_states;  /* 1: states (and C1/C2) come from a restart */
     int32_t jul_start;    /* simPer%julStart */
@@ -120,7 +125,7 @@ typedef struct {
     const int32_t *l11_l1_id;                 /* [nNodes] */
     const int32_t *net_perm, *from_n, *to_n;  /* [nNodes] (valid 1..nLinks) */
     const double *length, *slope, *ffp_imp;   /* [nLinks] */
-    const double *rout_param;                 /* [5] */
+    const double *rout_param;                 /* [5] (case 1) or [1] celerity [m s-1] (case 2) */
     const int32_t *gauge_node;                /* [nGauges] */
     const double *latitude;                   /* [nCells] degrees */
 } ora_domain;
@@ -139,6 +144,8 @@ typedef struct {
     double *qTIN, *qTR;   /* [2][nNodes] column-major (nNodes, 2) */
     double *qOUT, *Qmod;  /* [nNodes] */
     double *C1, *C2;      /* [nNodes] (links 1..nLinks used) */
+    double *run_to_rout;  /* [nCells] routing case 2 with a routing step of several
+                             model steps: runoff summed since the last routing (or NULL) */
 } ora_state;
 
 /* Forcing rows: row r of pre/temp/pet/tmin/tmax is [r][nCells]; the row used at

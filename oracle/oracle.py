@@ -52,7 +52,8 @@ class OraParams(C.Structure):
     _fields_ = [(n, _dp) for n in PARAM_FIELDS]
 
 
-STATE_FIELDS = ["interc", "snowpack", "sealSTW", "SM", "unsat", "sat", "qTIN", "qTR", "qOUT", "Qmod", "C1", "C2"]
+STATE_FIELDS = ["interc", "snowpack", "sealSTW", "SM", "unsat", "sat", "qTIN", "qTR", "qOUT", "Qmod", "C1", "C2",
+                "run_to_rout"]
 
 
 class OraState(C.Structure):
@@ -144,6 +145,8 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_L11_set_network_topology.argtypes = [C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, _ip]
     L.ora_L11_set_network_topology.restype = C.c_int
     L.ora_L11_routing_order.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.ora_update_param_case2.argtypes = [d, _dp, C.c_int, _dp, _dp]
+    L.ora_update_param_case2.restype = d
     L.ora_run.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
                           C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int]
     L.ora_default_states.argtypes = [C.POINTER(OraDomain), _dp, C.POINTER(OraState)]
@@ -193,7 +196,7 @@ class OracleRun:
             setattr(d, n, _d(k(getattr(dom, n))))
         for n in ("l1_l11_id", "l11_l1_id", "net_perm", "from_n", "to_n", "gauge_node"):
             setattr(d, n, _i(k(getattr(dom, n), np.int32)))
-        rp = k(rout_param if rout_param is not None else np.zeros(5))
+        rp = k(np.resize(np.asarray(rout_param if rout_param is not None else np.zeros(5), np.float64), 5))
         d.rout_param = _d(rp)
         self.d = d
         p = OraParams()
@@ -206,7 +209,7 @@ class OracleRun:
         self.state = {"interc": np.zeros(N), "snowpack": np.zeros(N), "sealSTW": np.zeros(N),
                       "SM": np.zeros(H * N), "unsat": np.zeros(N), "sat": np.zeros(N),
                       "qTIN": np.zeros(2 * Ln), "qTR": np.zeros(2 * Ln), "qOUT": np.zeros(Ln),
-                      "Qmod": np.zeros(Ln), "C1": np.zeros(Ln), "C2": np.zeros(Ln)}
+                      "Qmod": np.zeros(Ln), "C1": np.zeros(Ln), "C2": np.zeros(Ln), "run_to_rout": np.zeros(N)}
         self.s = OraState(**{n: _d(self.state[n]) for n in STATE_FIELDS})
         hd = k(dom.horizon_depth)
         self.L.ora_default_states(C.byref(self.d), _d(hd), C.byref(self.s))

@@ -13,10 +13,12 @@ daily simulated discharge of b1_daily_discharge.out and the final states of
 both restart files.  Cell arrays are packed column-major over mHM's (x, y)
 L1 mask, i.e. in the row-major order of the north-first grids.
 
-Also writes case10_gold.npz and case12_gold.npz: check/case_10 and case_12
-run the same inputs with soil-moisture cases 3 and 4 and the LAI-based PET
-correction (processCase(5) = -1); their parameter vectors (from their
-mhm_parameter.nml), L1 parameters, final states and daily discharge.
+Also writes case10_gold.npz, case12_gold.npz and case09_gold.npz: check/
+case_10 and case_12 run the same inputs with soil-moisture cases 3 and 4 and
+the LAI-based PET correction (processCase(5) = -1), case_09 with
+Hargreaves-Samani PET (daily tmin/tmax) and adaptive routing case 2; their
+parameter vectors (from their mhm_parameter.nml), L1 parameters, final
+states and daily discharge.
 """
 from __future__ import annotations
 
@@ -66,6 +68,12 @@ def main():
         t = f.read("time")
         assert t[off] == off and a.shape[1:] == mask1.shape
         met[key] = np.ascontiguousarray(a[off:off + SIM_DAYS][:, mask1])
+    # daily minimum / maximum temperature (Hargreaves-Samani PET): days since 1933-12-31
+    for key in ("tmin", "tmax"):
+        f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
+        a, t = f.read(key), f.read("time")
+        o = int(np.nonzero(t == julday(*SIM_START) - julday(1933, 12, 31))[0][0])
+        met[key] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
     n_links = int(mrm.read("L11_fromN").size) - 1
     ffp = mrm.read("L11_nLinkFracFPimp")                      # [scene][y][x], link i at packed position i
     q = np.loadtxt(CASE / "output_save" / "b1_daily_discharge.out", skiprows=1)
@@ -81,7 +89,8 @@ def main():
         gold_states[name] = np.stack([a[i][mask11] for i in range(a.shape[0])])
     np.savez_compressed(
         HERE / "case00_run.npz",
-        pre=met["pre"], temp=met["temp"], pet=met["pet"], jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
+        pre=met["pre"], temp=met["temp"], pet=met["pet"], tmin=met["tmin"], tmax=met["tmax"],
+        jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
         warming_days=WARMING_DAYS, scene2_from_day=SCENE2_FROM_DAY,
         from_n=mrm.read("L11_fromN").astype(np.int32), to_n=mrm.read("L11_toN").astype(np.int32),
         net_perm=mrm.read("L11_netPerm").astype(np.int32), r_order=mrm.read("L11_rOrder").astype(np.int32),
@@ -101,14 +110,15 @@ def main():
 # ---- further check cases on the same inputs (only processCase differs) ----
 import make_case00_mpr as mpr_fix  # noqa: E402
 
-CASES = {"case_10": (3, -1), "case_12": (4, -1)}   # processCase(3), processCase(5); routing 1
+# processCase(3), processCase(5), processCase(8)
+CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2)}
 PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "karstLoss", "kfastFlow",
                "kSlowFlow", "kBaseFlow", "kPerco", "tempThresh", "unsatThresh", "sealedThresh", "maxInter",
                "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "petLAIcorFactor",
                "jarvis_thresh_c1")
 
 
-def case_golds(case: str, proc_sm: int, proc_pet: int):
+def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
     cdir = REF / "check" / case
     mrm = h5lite.H5File(str(cdir / "output_save" / "b1_mRM_restart_001.nc"))
     mhm = h5lite.H5File(str(cdir / "output_save" / "b1_mHM_restart_001.nc"))
@@ -132,15 +142,21 @@ def case_golds(case: str, proc_sm: int, proc_pet: int):
         gold["s_" + name] = mrm.read(name)[mask1]
     q = np.loadtxt(cdir / "output_save" / "b1_daily_discharge.out", skiprows=1)
     blocks = ["interception1", "snow1", f"soilmoisture{proc_sm}", "directRunoff1",
-              {-1: "PETminus1", 0: "PET0", 1: "PET1"}[proc_pet], "interflow1", "percolation1", "routing1",
-              "geoparameter"]
+              {-1: "PETminus1", 0: "PET0", 1: "PET1"}[proc_pet], "interflow1", "percolation1",
+              f"routing{proc_rout}", "geoparameter"]
     gamma = mpr_fix.namelist_values(cdir / "mhm_parameter.nml", blocks)
+    extra = {}
+    if proc_rout == 2:
+        # link lengths as mRM sets them up for adaptive routing (cut at their 40th
+        # percentile, src/mRM/mo_mrm_net_startup.f90:1441-1447) and the routing step
+        n_links = int(mrm.read("L11_fromN").size) - 1
+        extra = dict(length=mrm.read("L11_length")[:n_links], ts_rout=float(mrm.read("L11_TSrout")[0]))
     np.savez_compressed(HERE / f"{case.replace('_', '')}_gold.npz", gamma=np.array(gamma), proc_sm=proc_sm,
-                        proc_pet=proc_pet, q_daily=q[:, 5], **gold)
+                        proc_pet=proc_pet, proc_rout=proc_rout, q_daily=q[:, 5], **gold, **extra)
     print("wrote", HERE / f"{case.replace('_', '')}_gold.npz", len(gamma), sorted(gold))
 
 
 if __name__ == "__main__":
     main()
-    for c, (sm_case, pet_case) in CASES.items():
-        case_golds(c, sm_case, pet_case)
+    for c, procs in CASES.items():
+        case_golds(c, *procs)
