@@ -228,6 +228,60 @@ int mhm_get_outputs(mhm_ctx *ctx, double *total_runoff, double *qmod);
 int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on);
 int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss);
 
+/* Aggregated per-cell flux/state outputs, the mHM_Fluxes_States file's
+ * variables (replaces mHM_OutputDataset / mHM_updateDataset / writeTimestep,
+ * src/mHM/mo_write_fluxes_states.f90:48-438 and src/common/mo_nc_output.f90:
+ * 140-262, driven from mhm_interface_run_write_output,
+ * src/mHM/mo_mhm_interface_run.f90:641-742).
+ *
+ * flags[i] = outputFlxState(i+1) of mhm_outputs.nml: 1 interception,
+ * 2 snowpack, 3 SWC_L<h>, 4 SM_L<h>, 5 SM_Lall, 6 sealedSTW, 7 unsatSTW,
+ * 8 satSTW, 9 PET, 10 aET, 11 Q, 12 QD, 13 QIf, 14 QIs, 15 QB, 16 recharge,
+ * 17 soil_infil_L<h>, 18 neutrons (refused: process 10 is not built),
+ * 19 aET_L<h>, 20 preEffect, 21 Qsm.  Per-horizon variables give one plane
+ * per horizon.  Planes follow the file's variable order (1, 2, 3, 4, 5, 6, 7,
+ * 8, 9, 10, ..., 17, 19, 20, 21).  States (1-8) are written as the mean over
+ * the interval, fluxes as its sum, in mm (per step) like the reference.
+ *
+ * Steps tt <= warming_steps add nothing; step tt closes an interval when
+ * timestep_model_outputs > 0 divides tt - warming_steps, when the next step
+ * starts a new day / month / year (-1 / -2 / -3), and always at
+ * tt == n_time_steps (0: only then).  The device keeps up to max_slots
+ * closed intervals, [slot][plane][member][n_cells]; a run that would close
+ * more than the free slots is refused: read them first.  Enabling again (or
+ * with cfg == NULL, off) clears sums and slots.  Runs with per-member steps
+ * (mhm_run_members_async) refuse aggregated outputs. */
+typedef struct {
+    int32_t timestep_model_outputs; /* > 0: every n steps; 0: at the end; -1 daily; -2 monthly; -3 yearly */
+    int32_t max_slots;              /* closed intervals held on the device between reads */
+    int64_t warming_steps;          /* warmingDays * steps per day */
+    int64_t n_time_steps;           /* steps of the simulation period */
+    int32_t flags[21];              /* outputFlxState(1..21); Qrouted: flags[0] (flags[1] river temperature refused) */
+    int32_t pad_;
+} mhm_output_config;
+int mhm_enable_flux_state_outputs(mhm_ctx *ctx, const mhm_output_config *cfg);
+/* Copies the closed intervals ([n_slots][n_planes][member][n_cells]) and the
+ * model step that closed each, then frees the slots.  out == NULL: only
+ * *n_slots (and *n_planes) are set. */
+int mhm_read_flux_state_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots,
+                                int32_t *n_planes);
+/* mRM's Qrouted output: the L11 discharge of every node, mean over each
+ * interval (mRM_OutputDataset / mRM_updateDataset,
+ * src/mRM/mo_mrm_write_fluxes_states.f90:48-140), same interval rules with
+ * timeStep_model_outputs_mrm; out is [n_slots][member][n_nodes] in L11 node
+ * order.  Needs routing. */
+int mhm_enable_routed_outputs(mhm_ctx *ctx, const mhm_output_config *cfg);
+int mhm_read_routed_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots);
+/* The reference writes a step's outputs after advancing its calendar, so the
+ * last step before a land-cover scene change is weighted with the NEXT
+ * scene's fSealed (QD, QIf, QIs, QB, recharge, aET, soil_infil, aET_L) and
+ * soilMoistSat (SM_L, SM_Lall) (src/mHM/mo_mhm_interface_run.f90:621-629,
+ * 698-727).  Outputs of model step tt of `member` use these values
+ * (fsealed [n_cells], soil_moist_sat [n_horizons][n_cells]) instead of the
+ * member's current parameters; tt < 1 clears the override. */
+int mhm_set_output_weights(mhm_ctx *ctx, int32_t member, int64_t tt, const double *fsealed,
+                           const double *soil_moist_sat);
+
 /* Restart state of one member (host buffers). */
 int mhm_get_state(mhm_ctx *ctx, int32_t member, const mhm_restart *st);
 int mhm_set_state(mhm_ctx *ctx, int32_t member, const mhm_restart *st);

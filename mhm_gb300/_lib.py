@@ -75,6 +75,14 @@ class L0Desc(C.Structure):
     ]
 
 
+class OutputConfig(C.Structure):
+    """mhm_output_config: aggregated flux/state (or Qrouted) outputs."""
+    _fields_ = [
+        ("timestep_model_outputs", C.c_int32), ("max_slots", C.c_int32), ("warming_steps", C.c_int64),
+        ("n_time_steps", C.c_int64), ("flags", C.c_int32 * 21), ("pad_", C.c_int32),
+    ]
+
+
 EXPORTS = [
     "mhm_ctx_create", "mhm_ctx_destroy", "mhm_last_error", "mhm_ctx_stream", "mhm_set_eff_params",
     "mhm_set_routing_params", "mhm_init_states", "mhm_set_forcing", "mhm_run", "mhm_enable_outputs",
@@ -85,6 +93,8 @@ EXPORTS = [
     "mhm_soil_weights", "mhm_slope_emp", "mhm_mpr_noalloc",
     "mhm_run_members_async", "mhm_snapshot_alloc", "mhm_snapshot_save", "mhm_snapshot_load", "mhm_autotune",
     "mhm_enable_fluxes", "mhm_get_fluxes", "mhm_set_link_fpimp",
+    "mhm_enable_flux_state_outputs", "mhm_read_flux_state_outputs", "mhm_enable_routed_outputs",
+    "mhm_read_routed_outputs", "mhm_set_output_weights",
 ]
 
 _LIB = None
@@ -150,6 +160,12 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_set_link_fpimp.argtypes = [vp, _dp]
     L.mhm_get_fluxes.argtypes = [vp, _dp, _dp]
     L.mhm_snapshot_save.argtypes = [vp, C.c_int32, C.c_int32]
+    i64p = C.POINTER(C.c_int64)
+    L.mhm_enable_flux_state_outputs.argtypes = [vp, C.POINTER(OutputConfig)]
+    L.mhm_enable_routed_outputs.argtypes = [vp, C.POINTER(OutputConfig)]
+    L.mhm_read_flux_state_outputs.argtypes = [vp, _dp, i64p, C.c_int32, _ip, _ip]
+    L.mhm_read_routed_outputs.argtypes = [vp, _dp, i64p, C.c_int32, _ip]
+    L.mhm_set_output_weights.argtypes = [vp, C.c_int32, C.c_int64, _dp, _dp]
     L.mhm_snapshot_load.argtypes = [vp, C.c_int32, C.c_int32]
     _LIB = L
     return L

@@ -51,4 +51,18 @@ MHM_HD StepDate step_date(int32_t jul_start, int32_t timestep, int64_t tt)
     return s;
 }
 
+// Day flag of step tt and whether step tt + 1 starts a new day, month or year
+// (is_new_day / is_new_month / is_new_year after datetimeinfo_increment,
+// src/common/mo_common_datetime_type.f90:106-133); bits as StepFlags.
+MHM_HD int32_t step_dflags(int32_t jul_start, int32_t timestep, int64_t tt)
+{
+    const StepDate sd = step_date(jul_start, timestep, tt);
+    const StepDate nx = step_date(jul_start, timestep, tt + 1);
+    int32_t fl = (sd.hour > 6 && sd.hour <= 18) ? 1 : 0; // isday, src/meteo/mo_meteo_handler.f90:1048
+    if (nx.day != sd.day) fl |= 2;
+    if (nx.month != sd.month) fl |= 4;
+    if (nx.year != sd.year) fl |= 8;
+    return fl;
+}
+
 } // namespace mhm

@@ -8,7 +8,7 @@ namespace mhm {
 cudaError_t launch_cell_chain_o6(const CellArgs &a, int H, cudaStream_t s);
 cudaError_t launch_cell_chain_o8(const CellArgs &a, int H, cudaStream_t s);
 
-// Calendar of steps tt0 .. tt0+n-1: forcing row, month, day flag, day of year.
+// Calendar of steps tt0 .. tt0+n-1: forcing row, month, day flags, day of year.
 __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
                                   int32_t stride)
 {
@@ -19,7 +19,7 @@ __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32
     StepInfo si;
     si.row = (int32_t)((tt + stride - 1) / stride); // iMeteoTS, mo_meteo_handler.f90:575-620
     si.month = (int8_t)sd.month;
-    si.isday = (int8_t)(sd.hour > 6 && sd.hour <= 18); // mo_meteo_handler.f90:1048
+    si.dflags = (int8_t)step_dflags(jul_start, timestep, tt);
     si.doy = (int16_t)sd.doy;
     steps[i] = si;
 }
@@ -36,7 +36,8 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
 cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s)
 {
     if (H < 1 || H > kMaxHorizons) return cudaErrorInvalidValue;
-    if (a.flux_aet) return launch_cell_chain_variant<4, true>(a, H, s); // flux outputs: one variant
+    // per-step fluxes or aggregated outputs: one variant
+    if (a.flux_aet || a.out.n_planes > 0) return launch_cell_chain_variant<4, true>(a, H, s);
     switch (occ) {
     case 6: return launch_cell_chain_o6(a, H, s);
     case 8: return launch_cell_chain_o8(a, H, s);

@@ -157,6 +157,24 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     double rad = 0.0;
     const size_t out_stride = (size_t)a.n_members * N;
     double *tro = a.tro + (size_t)m * N + k;
+    // aggregated flux/state outputs (flux variant): running sums in device
+    // memory, one [member][cell] plane per output variable
+    const OutArgs &o = a.out;
+    double *oacc = nullptr;
+    int ocnt = 0, oslot = 0;
+    int64_t ott_w = -1;
+    if constexpr (FLUX) {
+        if (o.n_planes > 0) {
+            oacc = o.acc + (size_t)m * N + k;
+            ocnt = o.cnt0;
+            oslot = o.slot0;
+            if (o.tt_w) ott_w = o.tt_w[m];
+        }
+    }
+    auto oadd = [&](int plane, double x) {
+        double *q = oacc + (size_t)plane * out_stride;
+        *q = *q + x; // OutputVariable%data = data + value, src/common/mo_nc_output.f90:140-149
+    };
 
     for (int t = 0; t < a.n_steps; ++t) {
         const StepInfo si = steps[t];
@@ -167,6 +185,18 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             if (a.proc_pet == -1) petlai = par(P_PETLAI + month - 1);
         }
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
+        // output weights: write_output runs after the calendar has advanced, so
+        // it reads fSealed / soilMoistSat of the NEXT step's land-cover scene
+        // (src/mHM/mo_mhm_interface_run.f90:621-629, 698-727)
+        bool oon = false, ow = false;
+        double ofs = 0.0, ofns = 0.0;
+        if constexpr (FLUX) {
+            const int64_t tt = o.tt_base + t;
+            oon = oacc != nullptr && tt > o.warm_steps;
+            ow = oon && tt == ott_w;
+            ofs = ow ? o.w_fsealed[(size_t)m * N + k] : c.fsealed;
+            ofns = 1.0 - ofs; // run_cfg%L1_fNotSealed = 1 - L1_fSealed (:239)
+        }
         // ---- meteo for the step (mo_meteo_handler.f90:915-1285) ----
         double pv;
         if (a.proc_pet == 0) {
@@ -189,9 +219,10 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             const int mi = month - 1;
             const double nd = a.nTstepDay;
             if (nd > 1.0) {
-                pet = 2.0 * pv * (si.isday ? a.tab.fday_pet[mi] : a.tab.fnight_pet[mi]) / nd;
-                temp = __ldg(a.temp + f) + (si.isday ? a.tab.fday_temp[mi] : a.tab.fnight_temp[mi]);
-                prec = 2.0 * __ldg(a.pre + f) * (si.isday ? a.tab.fday_prec[mi] : a.tab.fnight_prec[mi]) / nd;
+                const bool isday = (si.dflags & SF_ISDAY) != 0;
+                pet = 2.0 * pv * (isday ? a.tab.fday_pet[mi] : a.tab.fnight_pet[mi]) / nd;
+                temp = __ldg(a.temp + f) + (isday ? a.tab.fday_temp[mi] : a.tab.fnight_temp[mi]);
+                prec = 2.0 * __ldg(a.pre + f) * (isday ? a.tab.fday_prec[mi] : a.tab.fnight_prec[mi]) / nd;
             } else {
                 pet = pv;
                 temp = __ldg(a.temp + f);
@@ -221,13 +252,12 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             }
         }
         // ---- snow_accum_melt, mo_snow_accum_melt.f90:70-158 ----
-        double prec_effect;
+        double prec_effect, melt;
         {
             const bool warm = hm_gt(temp, c.tthresh);
             double rain = warm ? throughfall : 0.0;
             double snowf = warm ? 0.0 : throughfall;
             double dd = (dd_thr_ok && hm_le(prec, c.dd_thr)) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
-            double melt;
             if (warm) {
                 if (hm_gt0(c.snow)) {
                     double aux = dd * (temp - c.tthresh);
@@ -325,12 +355,18 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 if (hm_lt(smh, kEps)) smh = kEps;
                 hs(HS_SM, h) = smh;
                 if (hm_gt0(aet)) aet_above = aet_above + aet;
-                if constexpr (FLUX) aet_soil = aet_soil + aet;
+                if constexpr (FLUX) {
+                    aet_soil = aet_soil + aet;
+                    if (oon) { // soil_infil_L<h>, aET_L<h> (mo_write_fluxes_states.f90:414-426)
+                        if (o.plane[OF_INFIL] >= 0) oadd(o.plane[OF_INFIL] + h, infil * ofns);
+                        if (o.plane[OF_AET_L] >= 0) oadd(o.plane[OF_AET_L] + h, aet * ofns);
+                    }
+                }
             }
             infil_last = infil;
         }
         // ---- runoff_unsat_zone, mo_runoff.f90:74-154 ----
-        double fast = 0.0, slow = 0.0, base;
+        double fast = 0.0, slow = 0.0, base, perc;
         {
             c.unsat = c.unsat + infil_last;
             if (hm_gt(c.unsat, c.uthresh)) {
@@ -345,7 +381,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 slow = hm_lt(x, y) ? x : y;
             }
             c.unsat = c.unsat - slow;
-            double perc = c.kps * c.unsat;
+            perc = c.kps * c.unsat;
             if (hm_gt(c.unsat, perc)) {
                 c.unsat = c.unsat - perc;
                 c.sat = c.sat + perc * c.karst;
@@ -355,9 +391,11 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 c.unsat = 0.0;
             }
             if constexpr (FLUX) {
-                const size_t o = (size_t)t * out_stride + (size_t)m * N + k;
-                a.flux_aet[o] = aet_can + c.fsealed * aet_sealed_act + (1.0 - c.fsealed) * aet_soil;
-                a.flux_loss[o] = (1.0 - c.fsealed) * (perc - perc * c.karst);
+                if (a.flux_aet) {
+                    const size_t fo = (size_t)t * out_stride + (size_t)m * N + k;
+                    a.flux_aet[fo] = aet_can + c.fsealed * aet_sealed_act + (1.0 - c.fsealed) * aet_soil;
+                    a.flux_loss[fo] = (1.0 - c.fsealed) * (perc - perc * c.karst);
+                }
             }
         }
         // ---- runoff_sat_zone, mo_runoff.f90:191-212 ----
@@ -369,7 +407,56 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             c.sat = 0.0;
         }
         // ---- L1_total_runoff, mo_runoff.f90:248-274 ----
-        tro[(size_t)t * out_stride] = ((base + slow + fast) * (1.0 - c.fsealed)) + (runoff_sealed * c.fsealed);
+        const double q_total = ((base + slow + fast) * (1.0 - c.fsealed)) + (runoff_sealed * c.fsealed);
+        tro[(size_t)t * out_stride] = q_total;
+        if constexpr (FLUX) {
+            // mHM_updateDataset, src/mHM/mo_write_fluxes_states.f90:283-438
+            if (oon) {
+                const int8_t *pl = o.plane;
+                if (pl[OF_INTERC] >= 0) oadd(pl[OF_INTERC], c.interc);
+                if (pl[OF_SNOW] >= 0) oadd(pl[OF_SNOW], c.snow);
+                if (pl[OF_SWC] >= 0)
+                    for (int h = 0; h < H; ++h) oadd(pl[OF_SWC] + h, hs(HS_SM, h));
+                if (pl[OF_SM] >= 0 || pl[OF_SM_ALL] >= 0) {
+                    double ssm = 0.0, ssat = 0.0;
+                    for (int h = 0; h < H; ++h) {
+                        const double sat_h = ow ? o.w_sms[((size_t)m * H + h) * N + k] : hs(HS_SMS, h);
+                        if (pl[OF_SM] >= 0) oadd(pl[OF_SM] + h, hs(HS_SM, h) / sat_h);
+                        ssm = ssm + hs(HS_SM, h);
+                        ssat = ssat + sat_h;
+                    }
+                    if (pl[OF_SM_ALL] >= 0) oadd(pl[OF_SM_ALL], ssm / ssat);
+                }
+                if (pl[OF_SEAL] >= 0) oadd(pl[OF_SEAL], c.seal);
+                if (pl[OF_UNSAT] >= 0) oadd(pl[OF_UNSAT], c.unsat);
+                if (pl[OF_SAT] >= 0) oadd(pl[OF_SAT], c.sat);
+                if (pl[OF_PET] >= 0) oadd(pl[OF_PET], pet);
+                if (pl[OF_AET] >= 0) oadd(pl[OF_AET], aet_soil * ofns + aet_can + aet_sealed_act * ofs);
+                if (pl[OF_Q] >= 0) oadd(pl[OF_Q], q_total);
+                if (pl[OF_QD] >= 0) oadd(pl[OF_QD], runoff_sealed * ofs);
+                if (pl[OF_QIF] >= 0) oadd(pl[OF_QIF], fast * ofns);
+                if (pl[OF_QIS] >= 0) oadd(pl[OF_QIS], slow * ofns);
+                if (pl[OF_QB] >= 0) oadd(pl[OF_QB], base * ofns);
+                if (pl[OF_RECHARGE] >= 0) oadd(pl[OF_RECHARGE], perc * ofns);
+                if (pl[OF_PRE_EFFECT] >= 0) oadd(pl[OF_PRE_EFFECT], prec_effect);
+                if (pl[OF_QSM] >= 0) oadd(pl[OF_QSM], melt);
+                ++ocnt; // OutputVariable%counter
+                const int64_t tt = o.tt_base + t;
+                if (out_writeout(o.interval, tt - o.warm_steps, tt, o.n_tt, si.dflags)) {
+                    // writeVariableTimestep, src/common/mo_nc_output.f90:158-175
+                    double *dst = o.out + (size_t)oslot * o.n_planes * out_stride + (size_t)m * N + k;
+                    for (int v = 0; v < o.n_planes; ++v) {
+                        double *q = oacc + (size_t)v * out_stride;
+                        const double x = *q;
+                        if (oslot < o.max_slots)
+                            dst[(size_t)v * out_stride] = ((o.avg_mask >> v) & 1) ? x / (double)ocnt : x;
+                        *q = 0.0;
+                    }
+                    ++oslot;
+                    ocnt = 0;
+                }
+            }
+        }
     }
 
     S[(size_t)S_INTERC * N] = c.interc;

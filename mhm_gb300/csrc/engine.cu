@@ -29,6 +29,7 @@ cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
 cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
 cudaError_t launch_qmod_step(const QmodStepArgs &a, cudaStream_t s);
 cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
+cudaError_t launch_qrouted(const QroutArgs &a, cudaStream_t s);
 cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double TS, const double *length,
                             const double *slope, const double *ffp, const int32_t *link_pos, double *C1,
                             double *C2, cudaStream_t s);
@@ -72,6 +73,18 @@ struct DevBuf {
 struct TimedLaunch {
     int kind;
     cudaEvent_t a, b;
+};
+
+// One aggregated output set (mHM's outputFlxState or mRM's Qrouted): the
+// interval schedule, the host's view of the device counters after all
+// enqueued work, and the device running sums / written intervals.
+struct OutSet {
+    bool on = false;
+    int32_t interval = 0, max_slots = 0, n_planes = 0;
+    int64_t warm = 0, n_tt = 0;
+    int32_t slots = 0, cnt = 0;      // intervals written (not yet read), steps in the open interval
+    std::vector<int64_t> slot_tt;    // model step that closed each written interval
+    DevBuf<double> acc, out;
 };
 
 struct ForcingSrc {
@@ -122,6 +135,12 @@ struct mhm_ctx {
     // outputs
     int32_t out_tro = 0, out_qmod = 0, out_flux = 0;
     DevBuf<double> flux_d[2];
+    // aggregated flux/state outputs and Qrouted
+    OutSet fso, qro;
+    int8_t fs_plane[kOutFlags + 1];
+    uint64_t fs_avg = 0;
+    DevBuf<int64_t> w_tt;
+    DevBuf<double> w_fs, w_sms;
     std::vector<double> host_aet, host_loss;
     std::vector<double> host_tro, host_qmod;
     int32_t last_steps = 0;
@@ -180,6 +199,28 @@ int cuda_fail(mhm_ctx *c, cudaError_t e, const char *what)
         cudaError_t e_ = (call);                                                                                   \
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what);                                                    \
     } while (0)
+
+// Host replica of the device interval bookkeeping over steps tt_a .. tt_a+n-1
+// (same calendar and writeout rule as the kernels); with `commit` the set's
+// counters and closing steps advance, else only the written count is returned.
+int32_t out_advance(OutSet &o, int32_t jul_start, int32_t timestep, int64_t tt_a, int64_t n, bool commit)
+{
+    int32_t cnt = o.cnt, wrote = 0;
+    for (int64_t tt = tt_a; tt < tt_a + n; ++tt) {
+        if (tt <= o.warm) continue;
+        ++cnt;
+        if (out_writeout(o.interval, tt - o.warm, tt, o.n_tt, step_dflags(jul_start, timestep, tt))) {
+            ++wrote;
+            cnt = 0;
+            if (commit) o.slot_tt.push_back(tt);
+        }
+    }
+    if (commit) {
+        o.cnt = cnt;
+        o.slots += wrote;
+    }
+    return wrote;
+}
 
 template <class T>
 cudaError_t upload(DevBuf<T> &b, const T *host, size_t n, cudaStream_t s)
@@ -350,6 +391,36 @@ bool gamma_layout(int32_t proc_sm, int32_t proc_pet, int32_t proc_rout, int32_t 
     return true;
 }
 
+} // namespace
+
+namespace {
+// Copies the written intervals to the caller and frees the device slots.
+int read_outset(mhm_ctx *ctx, OutSet &o, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots,
+                bool by_node)
+{
+    if (!o.on) return fail(ctx, MHM_ERR_INVALID, "these outputs are not enabled");
+    if (int rc = mhm_sync(ctx)) return rc;
+    if (n_slots) *n_slots = o.slots;
+    if (!out) return MHM_OK; // query only
+    if (o.slots > max_slots) return fail(ctx, MHM_ERR_INVALID, "buffer holds fewer intervals than were written");
+    const size_t per = (size_t)o.n_planes * ctx->M * (by_node ? (size_t)ctx->L : (size_t)ctx->N);
+    if (o.slots > 0)
+        CK(cudaMemcpy(out, o.out.p, (size_t)o.slots * per * sizeof(double), cudaMemcpyDeviceToHost), "outputs");
+    if (by_node) { // routing-level positions -> L11 node order
+        const size_t L = ctx->L;
+        std::vector<double> row(L);
+        for (size_t r = 0; r < (size_t)o.slots * ctx->M; ++r) {
+            double *q = out + r * L;
+            for (size_t v = 0; v < L; ++v) row[v] = q[ctx->net.pos_of_node[v]];
+            std::memcpy(q, row.data(), L * sizeof(double));
+        }
+    }
+    if (slot_tt)
+        for (int32_t i = 0; i < o.slots; ++i) slot_tt[i] = o.slot_tt[i];
+    o.slots = 0;
+    o.slot_tt.clear();
+    return MHM_OK;
+}
 } // namespace
 
 extern "C" {
@@ -788,6 +859,14 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     const bool members = member_tt0 != nullptr;
     if (members && (stride != 1 || ctx->ntfd != 24))
         return fail(ctx, MHM_ERR_UNSUPPORTED, "per-member steps need hourly steps with hourly forcing");
+    if (members && (ctx->fso.on || ctx->qro.on))
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "aggregated outputs with per-member steps");
+    for (OutSet *o : {&ctx->fso, &ctx->qro}) {
+        if (!o->on) continue;
+        const int32_t w = out_advance(*o, ctx->jul_start, ctx->timestep, tt0, n_steps, false);
+        if (o->slots + w > o->max_slots)
+            return fail(ctx, MHM_ERR_INVALID, "output intervals would exceed the device slots: read the outputs first");
+    }
     // member mode reads the first n_steps rows of the device forcing window
     const int32_t first_row = members ? ctx->forc[0].row0 : (tt0 + stride - 1) / stride;
     const int32_t last_row = members ? ctx->forc[0].row0 + n_steps - 1 : (tt0 + n_steps - 1 + stride - 1) / stride;
@@ -996,6 +1075,25 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             a.flux_aet = ctx->flux_d[0].p;
             a.flux_loss = ctx->flux_d[1].p;
         }
+        if (ctx->fso.on) {
+            OutArgs &o = a.out;
+            o.n_planes = ctx->fso.n_planes;
+            o.interval = ctx->fso.interval;
+            o.warm_steps = ctx->fso.warm;
+            o.n_tt = ctx->fso.n_tt;
+            o.tt_base = (int64_t)tt0 + s0;
+            o.slot0 = ctx->fso.slots;
+            o.cnt0 = ctx->fso.cnt;
+            o.max_slots = ctx->fso.max_slots;
+            std::memcpy(o.plane, ctx->fs_plane, sizeof(o.plane));
+            o.avg_mask = ctx->fs_avg;
+            o.acc = ctx->fso.acc.p;
+            o.out = ctx->fso.out.p;
+            o.tt_w = ctx->w_tt.p;
+            o.w_fsealed = ctx->w_fs.p;
+            o.w_sms = ctx->w_sms.p;
+            out_advance(ctx->fso, ctx->jul_start, ctx->timestep, (int64_t)tt0 + s0, nT, true);
+        }
         {
             Bracket br(ctx, 0, ctx->stream);
             CK(launch_cell_chain(a, H, ctx->cell_occ, ctx->stream), "cell chain launch");
@@ -1114,8 +1212,32 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
                 CK(cudaMemcpyAsync(ctx->host_qmod.data() + (m * n_steps + s0) * L, ctx->qmod.p + m * (size_t)nT * L,
                                    (size_t)nT * L * sizeof(double), cudaMemcpyDeviceToHost, rs),
                    "qmod D2H");
-        if (c == nchunks - 1) {
-            // qOUT and Qmod of the last step (restart fields)
+        if (ctx->qro.on) {
+            QroutArgs qa{};
+            qa.n_members = ctx->M;
+            qa.n_steps = nT;
+            qa.n_nodes = ctx->L;
+            qa.win = F;
+            qa.interval = ctx->qro.interval;
+            qa.slot0 = ctx->qro.slots;
+            qa.cnt0 = ctx->qro.cnt;
+            qa.max_slots = ctx->qro.max_slots;
+            qa.warm_steps = ctx->qro.warm;
+            qa.n_tt = ctx->qro.n_tt;
+            qa.tt_base = (int64_t)tt0 + s0;
+            qa.jul_start = ctx->jul_start;
+            qa.timestep = ctx->timestep;
+            qa.qmod = ctx->qmod.p;
+            qa.qmod_prev = ctx->qmod_last.p;
+            qa.acc = ctx->qro.acc.p;
+            qa.out = ctx->qro.out.p;
+            CK(launch_qrouted(qa, rs), "Qrouted launch");
+            g_launches++;
+            out_advance(ctx->qro, ctx->jul_start, ctx->timestep, (int64_t)tt0 + s0, nT, true);
+        }
+        if (c == nchunks - 1 || ctx->qro.on) {
+            // qOUT and Qmod of the chunk's last step (restart fields; the
+            // Qrouted output of the next chunk starts from this Qmod)
             for (size_t m = 0; m < M; ++m) {
                 if (members && ctx->member_s0_h[m] < 0) continue; // idle member keeps its restart fields
                 const size_t nq = (size_t)(nT / F); // qOUT rows: one per routing step of the window mode
@@ -1282,6 +1404,8 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
     };
     const int32_t out_t = ctx->out_tro, out_q = ctx->out_qmod, out_f = ctx->out_flux;
     ctx->out_tro = ctx->out_qmod = ctx->out_flux = 0;
+    const bool fso_on = ctx->fso.on, qro_on = ctx->qro.on; // trials add nothing to the outputs
+    ctx->fso.on = ctx->qro.on = false;
     const int32_t occ0 = ctx->cell_occ, sub0 = ctx->route_sub;
     int rc = copy_states(true);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1320,6 +1444,8 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
     ctx->out_tro = out_t;
     ctx->out_qmod = out_q;
     ctx->out_flux = out_f;
+    ctx->fso.on = fso_on;
+    ctx->qro.on = qro_on;
     if (int r2 = copy_states(false)) rc = rc ? rc : r2;
     if (int r3 = mhm_sync(ctx)) rc = rc ? rc : r3;
     if (occ_out) *occ_out = ctx->cell_occ;
@@ -1356,6 +1482,120 @@ int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss)
     if (aet) std::memcpy(aet, ctx->host_aet.data(), ctx->host_aet.size() * sizeof(double));
     if (loss) std::memcpy(loss, ctx->host_loss.data(), ctx->host_loss.size() * sizeof(double));
     return MHM_OK;
+}
+
+int mhm_enable_flux_state_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    OutSet &o = ctx->fso;
+    o.on = false;
+    o.acc.release();
+    o.out.release();
+    o.slots = o.cnt = 0;
+    o.slot_tt.clear();
+    if (!cfg) return MHM_OK;
+    if (cfg->max_slots < 1) return fail(ctx, MHM_ERR_INVALID, "max_slots >= 1 required");
+    if (cfg->flags[OF_NEUTRONS - 1])
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "neutron output (process 10) is not part of this build");
+    // planes in the order of mHM_OutputDataset, src/mHM/mo_write_fluxes_states.f90:82-262
+    static const int order[kOutFlags] = {OF_INTERC, OF_SNOW, OF_SWC, OF_SM, OF_SM_ALL, OF_SEAL, OF_UNSAT,
+                                         OF_SAT, OF_NEUTRONS, OF_PET, OF_AET, OF_Q, OF_QD, OF_QIF, OF_QIS,
+                                         OF_QB, OF_RECHARGE, OF_INFIL, OF_AET_L, OF_PRE_EFFECT, OF_QSM};
+    int n = 0;
+    uint64_t avg = 0;
+    for (int i = 0; i <= kOutFlags; ++i) ctx->fs_plane[i] = -1;
+    for (int f : order) {
+        if (!cfg->flags[f - 1]) continue;
+        const bool per_h = f == OF_SWC || f == OF_SM || f == OF_INFIL || f == OF_AET_L;
+        const bool state = f <= OF_SAT; // states are written as interval means (avg = .true.)
+        ctx->fs_plane[f] = (int8_t)n;
+        for (int j = 0; j < (per_h ? ctx->H : 1); ++j, ++n)
+            if (state) avg |= (uint64_t)1 << n;
+    }
+    if (n == 0) return MHM_OK;
+    const size_t MN = (size_t)ctx->M * ctx->N;
+    CK(cudaSetDevice(ctx->device), "set device");
+    CK(o.acc.ensure((size_t)n * MN), "output sums");
+    CK(o.out.ensure((size_t)cfg->max_slots * n * MN), "output intervals");
+    CK(cudaMemsetAsync(o.acc.p, 0, (size_t)n * MN * sizeof(double), ctx->stream), "output sums");
+    if (!ctx->w_tt.p) {
+        std::vector<int64_t> none(ctx->M, -1);
+        CK(upload(ctx->w_tt, none.data(), none.size(), ctx->stream), "output weights");
+        CK(ctx->w_fs.ensure(MN), "output weights");
+        CK(ctx->w_sms.ensure(MN * ctx->H), "output weights");
+        CK(cudaStreamSynchronize(ctx->stream), "sync");
+    }
+    ctx->fs_avg = avg;
+    o.n_planes = n;
+    o.interval = cfg->timestep_model_outputs;
+    o.max_slots = cfg->max_slots;
+    o.warm = cfg->warming_steps;
+    o.n_tt = cfg->n_time_steps;
+    o.on = true;
+    return MHM_OK;
+}
+
+int mhm_enable_routed_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc;
+    OutSet &o = ctx->qro;
+    o.on = false;
+    o.acc.release();
+    o.out.release();
+    o.slots = o.cnt = 0;
+    o.slot_tt.clear();
+    if (!cfg || !cfg->flags[0]) return MHM_OK;
+    if (ctx->proc_rout < 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
+    if (cfg->flags[1]) return fail(ctx, MHM_ERR_UNSUPPORTED, "river temperature (process 11) is not part of this build");
+    if (cfg->max_slots < 1) return fail(ctx, MHM_ERR_INVALID, "max_slots >= 1 required");
+    const size_t ML = (size_t)ctx->M * ctx->L;
+    CK(cudaSetDevice(ctx->device), "set device");
+    CK(o.acc.ensure(ML), "Qrouted sums");
+    CK(o.out.ensure((size_t)cfg->max_slots * ML), "Qrouted intervals");
+    CK(cudaMemsetAsync(o.acc.p, 0, ML * sizeof(double), ctx->stream), "Qrouted sums");
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    o.n_planes = 1;
+    o.interval = cfg->timestep_model_outputs;
+    o.max_slots = cfg->max_slots;
+    o.warm = cfg->warming_steps;
+    o.n_tt = cfg->n_time_steps;
+    o.on = true;
+    return MHM_OK;
+}
+
+int mhm_set_output_weights(mhm_ctx *ctx, int32_t m, int64_t tt, const double *fsealed, const double *soil_moist_sat)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (!ctx->fso.on) return fail(ctx, MHM_ERR_INVALID, "flux/state outputs are not enabled");
+    if (tt >= 1 && (!fsealed || !soil_moist_sat)) return fail(ctx, MHM_ERR_INVALID, "weights missing");
+    if (int rc = mhm_sync(ctx)) return rc;
+    const size_t N = ctx->N;
+    if (tt >= 1) {
+        CK(cudaMemcpy(ctx->w_fs.p + m * N, fsealed, N * sizeof(double), cudaMemcpyHostToDevice), "weights");
+        CK(cudaMemcpy(ctx->w_sms.p + (size_t)m * ctx->H * N, soil_moist_sat, (size_t)ctx->H * N * sizeof(double),
+                      cudaMemcpyHostToDevice),
+           "weights");
+    }
+    const int64_t v = tt >= 1 ? tt : -1;
+    CK(cudaMemcpy(ctx->w_tt.p + m, &v, sizeof(int64_t), cudaMemcpyHostToDevice), "weights");
+    return MHM_OK;
+}
+
+int mhm_read_flux_state_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots,
+                                int32_t *n_planes)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (n_planes) *n_planes = ctx->fso.on ? ctx->fso.n_planes : 0;
+    return read_outset(ctx, ctx->fso, out, slot_tt, max_slots, n_slots, false);
+}
+
+int mhm_read_routed_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    return read_outset(ctx, ctx->qro, out, slot_tt, max_slots, n_slots, true);
 }
 
 int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)

@@ -37,12 +37,52 @@ enum StatePlane : int { S_INTERC = 0, S_SNOW, S_SEAL, S_UNSAT, S_SAT, S_SM };
 __host__ __device__ constexpr int n_state_planes(int H) { return S_SM + H; }
 
 // One model step: forcing row (0-based within the device forcing window),
-// calendar month (1..12), day flag and day of year.
+// calendar month (1..12), day flags and day of year.
+enum StepFlags : int { SF_ISDAY = 1, SF_DAY_END = 2, SF_MONTH_END = 4, SF_YEAR_END = 8 };
 struct StepInfo {
     int32_t row;
     int8_t month;
-    int8_t isday;
+    int8_t dflags;  // SF_ISDAY: 6 < hour <= 18; SF_*_END: the next step starts a new day / month / year
     int16_t doy;
+};
+
+// Aggregated flux/state outputs (outputFlxState of mhm_outputs.nml), indexes
+// 1..21 of the reference's list; planes in the reference's write order.
+constexpr int kOutFlags = 21;
+enum OutFlag : int {
+    OF_INTERC = 1, OF_SNOW, OF_SWC, OF_SM, OF_SM_ALL, OF_SEAL, OF_UNSAT, OF_SAT, OF_PET, OF_AET, OF_Q, OF_QD,
+    OF_QIF, OF_QIS, OF_QB, OF_RECHARGE, OF_INFIL, OF_NEUTRONS, OF_AET_L, OF_PRE_EFFECT, OF_QSM
+};
+// Output of step tt (tindex = tt - warming steps > 0) closes an interval:
+// src/common/mo_common_datetime_type.f90:157-185
+__host__ __device__ inline bool out_writeout(int interval, int64_t tindex, int64_t tt, int64_t n_tt, int dflags)
+{
+    if (interval < -3) return false; // no output at all
+    if (tt == n_tt) return true;     // the last step closes any open interval
+    if (interval > 0) return tindex % interval == 0;
+    if (interval == -1) return (dflags & SF_DAY_END) != 0;
+    if (interval == -2) return (dflags & SF_MONTH_END) != 0;
+    if (interval == -3) return (dflags & SF_YEAR_END) != 0;
+    return false; // 0: only the last step
+}
+
+struct OutArgs {
+    int32_t n_planes;        // 0: outputs off
+    int32_t interval;        // timeStep_model_outputs
+    int64_t warm_steps;      // no output for tt <= warm_steps
+    int64_t n_tt;            // last step of the simulation period
+    int64_t tt_base;         // absolute step of the chunk's step 0
+    int32_t slot0, cnt0;     // slots written before this chunk, steps in the open interval
+    int32_t max_slots;       // slots of `out` (writes past it are dropped; the host refuses such runs)
+    int8_t plane[kOutFlags + 1]; // first plane of flag f (1-based), -1 if off
+    uint64_t avg_mask;       // planes written as a mean over the interval (states)
+    double *acc;             // [n_planes][M][n_cells] running sums
+    double *out;             // [slots][n_planes][M][n_cells]
+    // outputs of step tt_w[m] weighted with these fSealed / soilMoistSat
+    // instead of the member's parameters (the next land-cover scene's)
+    const int64_t *tt_w;     // [M]
+    const double *w_fsealed; // [M][n_cells]
+    const double *w_sms;     // [M][H][n_cells]
 };
 
 struct MonthTables {
@@ -78,6 +118,7 @@ struct CellArgs {
     // actual ET (canopy + sealed + soil, area weighted) and the percolation
     // lost to (or, karstLoss > 1, gained from) outside the cell
     double *flux_aet, *flux_loss;
+    OutArgs out;        // aggregated flux/state outputs (flux variant only)
 };
 
 struct AccArgs {
@@ -127,6 +168,21 @@ struct QmodStepArgs {
     const double *qmod_sub;     // [M][n_steps * rdiv / win][n_nodes]
     double *qmod;               // [M][n_steps][n_nodes]
     const int32_t *member_step0;
+};
+
+// mRM's Qrouted output: per model step the L11 discharge state (with a routing
+// step of `win` model steps it changes only at the last step of each window),
+// aggregated as a mean over the output interval
+// (src/mRM/mo_mrm_write_fluxes_states.f90:130-133, src/common/mo_nc_output.f90:140-175)
+struct QroutArgs {
+    int32_t n_members, n_steps, n_nodes, win, interval;
+    int32_t slot0, cnt0, max_slots;
+    int64_t warm_steps, n_tt, tt_base;
+    int32_t jul_start, timestep; // calendar (interval ends)
+    const double *qmod;          // [M][n_steps][n_nodes]
+    const double *qmod_prev;     // [M][n_nodes] discharge state before the chunk
+    double *acc;                 // [M][n_nodes]
+    double *out;                 // [slots][M][n_nodes]
 };
 
 struct GaugeArgs {

@@ -11,6 +11,7 @@
 // rank order, then the node's own qOUT), so results are bit-identical.
 #include <cstdint>
 
+#include "calendar.h"
 #include "mhm_kernels.cuh"
 
 namespace mhm {
@@ -139,6 +140,40 @@ __global__ void qmod_step_kernel(const QmodStepArgs a)
     a.qmod[((size_t)m * a.n_steps + t) * L + pos] = v;
 }
 
+// mRM's Qrouted output (mRM_updateDataset / writeTimestep, called every model
+// step after the warm-up: src/mHM/mo_mhm_interface_run.f90:651-668).  One
+// thread per (member, node) walks the chunk's steps; with a routing step of
+// `win` model steps the discharge state changes only at a window's last step.
+__global__ void qrouted_kernel(const QroutArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t L = a.n_nodes;
+    if (gid >= (int64_t)a.n_members * L) return;
+    const int pos = (int)(gid % L);
+    const int m = (int)(gid / L);
+    const size_t ML = (size_t)a.n_members * L;
+    const double *q = a.qmod + (size_t)m * a.n_steps * L + pos;
+    double acc = a.acc[(size_t)m * L + pos];
+    int cnt = a.cnt0, slot = a.slot0;
+    for (int t = 0; t < a.n_steps; ++t) {
+        const int64_t tt = a.tt_base + t;
+        if (tt <= a.warm_steps) continue;
+        double v;
+        if (a.win == 1 || (t + 1) % a.win == 0) v = q[(size_t)t * L];
+        else if (t >= a.win) v = q[(size_t)((t / a.win) * a.win - 1) * L];
+        else v = a.qmod_prev[(size_t)m * L + pos];
+        acc = acc + v;
+        ++cnt;
+        if (out_writeout(a.interval, tt - a.warm_steps, tt, a.n_tt, step_dflags(a.jul_start, a.timestep, tt))) {
+            if (slot < a.max_slots) a.out[(size_t)slot * ML + (size_t)m * L + pos] = acc / (double)cnt; // a mean
+            acc = 0.0;
+            cnt = 0;
+            ++slot;
+        }
+    }
+    a.acc[(size_t)m * L + pos] = acc;
+}
+
 // GaugeDischarge(gaugeIndexList) = L11_Qmod(gaugeNodeList), mo_mrm_routing.f90:299-301
 __global__ void gauge_gather_kernel(const GaugeArgs a)
 {
@@ -201,6 +236,14 @@ cudaError_t launch_qmod_step(const QmodStepArgs &a, cudaStream_t s)
     const int64_t n = (int64_t)a.n_members * a.n_steps * a.n_nodes;
     if (n == 0) return cudaSuccess;
     qmod_step_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_qrouted(const QroutArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_members * a.n_nodes;
+    if (n == 0 || a.n_steps == 0) return cudaSuccess;
+    qrouted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -1,15 +1,15 @@
-"""Minimal reader for the netCDF-4 (HDF5) files of the reference's regression
-outputs (TEST INFRASTRUCTURE: used only to turn the reference's restart
-goldens into fixtures).
+"""Minimal reader for netCDF-4 (HDF5) files as the reference writes them:
+its restart files (mHM and mRM), flux/state outputs and input grids.
 
 Written from the published HDF5 file-format specification, covering what
-netCDF-C writes with HDF5's default (earliest) library bounds: superblock
-version 0/1, version-1 object headers with continuation blocks, groups as
-symbol tables (version-1 B-tree of symbol-table nodes plus a local heap),
-dataspace / datatype (little-endian fixed and floating point) / layout
-(version 3: contiguous, compact, chunked with a version-1 B-tree index) /
-filter pipeline (deflate, shuffle, fletcher32) messages.  Anything else
-raises NotImplementedError.
+netCDF-C writes with HDF5's default (earliest) library bounds and newer
+layouts: superblock version 0/1/2, version-1 and version-2 object headers
+with continuation blocks, groups as symbol tables (version-1 B-tree of
+symbol-table nodes plus a local heap) or as link messages / dense link
+storage (fractal heap), dataspace / datatype (little-endian fixed and
+floating point) / layout (version 3: contiguous, compact, chunked with a
+version-1 B-tree index) / filter pipeline (deflate, shuffle, fletcher32)
+messages.  Anything else raises NotImplementedError.
 """
 from __future__ import annotations
 

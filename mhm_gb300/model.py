@@ -15,7 +15,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib
+from . import _lib, outputs
 from .synth import Domain
 
 _dp = C.POINTER(C.c_double)
@@ -275,6 +275,57 @@ class MhmGpu:
         self._check(self.L.mhm_get_fluxes(self.ctx, _d(aet), _d(loss)), "mhm_get_fluxes")
         return aet, loss
 
+    def enable_flux_state_outputs(self, flags, interval: int, warming_steps: int, n_time_steps: int,
+                                  max_slots: int = 32):
+        """Aggregated per-cell outputs (outputFlxState flags: 21 ints, or indexes /
+        names for outputs.flags_from) closed at timeStep_model_outputs `interval`."""
+        flags = list(flags) if len(flags) == 21 and all(f in (0, 1) for f in flags) else outputs.flags_from(flags)
+        cfg = _lib.OutputConfig(timestep_model_outputs=interval, max_slots=max_slots, warming_steps=warming_steps,
+                                n_time_steps=n_time_steps)
+        for i, f in enumerate(flags):
+            cfg.flags[i] = int(f)
+        self._check(self.L.mhm_enable_flux_state_outputs(self.ctx, C.byref(cfg)), "mhm_enable_flux_state_outputs")
+        self._fs_names = outputs.plane_names(flags, self.dom.n_horizons)
+        self._fs_slots = max_slots
+
+    def read_flux_state_outputs(self) -> tuple[list[str], np.ndarray, np.ndarray]:
+        """(plane names, closed intervals [slot][plane][member][cell], the model
+        step closing each slot); frees the device slots."""
+        n = C.c_int32()
+        npl = C.c_int32()
+        self._check(self.L.mhm_read_flux_state_outputs(self.ctx, None, None, 0, C.byref(n), C.byref(npl)),
+                    "mhm_read_flux_state_outputs")
+        out = np.zeros((n.value, npl.value, self.n_members, self.dom.n_cells))
+        tt = np.zeros(max(n.value, 1), np.int64)
+        self._check(self.L.mhm_read_flux_state_outputs(self.ctx, _d(out), tt.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                       n.value, C.byref(n), C.byref(npl)),
+                    "mhm_read_flux_state_outputs")
+        return self._fs_names, out, tt[: n.value]
+
+    def enable_routed_outputs(self, interval: int, warming_steps: int, n_time_steps: int, max_slots: int = 32):
+        """mRM's Qrouted output (mean L11 discharge per interval)."""
+        cfg = _lib.OutputConfig(timestep_model_outputs=interval, max_slots=max_slots, warming_steps=warming_steps,
+                                n_time_steps=n_time_steps)
+        cfg.flags[0] = 1
+        self._check(self.L.mhm_enable_routed_outputs(self.ctx, C.byref(cfg)), "mhm_enable_routed_outputs")
+
+    def read_routed_outputs(self) -> tuple[np.ndarray, np.ndarray]:
+        """(Qrouted [slot][member][node] in L11 node order, closing steps)."""
+        n = C.c_int32()
+        self._check(self.L.mhm_read_routed_outputs(self.ctx, None, None, 0, C.byref(n)), "mhm_read_routed_outputs")
+        out = np.zeros((n.value, self.n_members, self.dom.n_nodes))
+        tt = np.zeros(max(n.value, 1), np.int64)
+        self._check(self.L.mhm_read_routed_outputs(self.ctx, _d(out), tt.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                   n.value, C.byref(n)), "mhm_read_routed_outputs")
+        return out, tt[: n.value]
+
+    def set_output_weights(self, member: int, tt: int, fsealed=None, soil_moist_sat=None):
+        """Outputs of step tt weighted with these fSealed [cell] / soilMoistSat
+        [horizon][cell] (the next land-cover scene's); tt < 1 clears."""
+        fs = None if fsealed is None else np.ascontiguousarray(fsealed, np.float64)
+        sm = None if soil_moist_sat is None else np.ascontiguousarray(soil_moist_sat, np.float64)
+        self._check(self.L.mhm_set_output_weights(self.ctx, member, tt, _d(fs), _d(sm)), "mhm_set_output_weights")
+
     def autotune(self, tt0: int, n_steps: int) -> dict:
         """Pick the fastest cell-chain register variant and routing sub-chunk
         by timing n_steps from tt0 (states restored afterwards)."""
@@ -317,6 +368,38 @@ class MhmGpu:
         arrs = {k: np.ascontiguousarray(v, np.float64) for k, v in state.items()}
         st = _lib.Restart(**{k: _d(v) for k, v in arrs.items()})
         self._check(self.L.mhm_set_state(self.ctx, member, C.byref(st)), "mhm_set_state")
+
+    def load_restart(self, mhm, scene: int = 0, mrm=None, member: int = 0):
+        """Start from restart files (read_restart = .true.): the land-cover
+        scene's effective parameters and the L1 states of an mHM restart
+        (restart.MhmRestart), with an mRM restart (restart.MrmRestart) also
+        the routing states and Muskingum coefficients -- no MPR, no soil
+        moisture initialisation (src/mHM/mo_mhm_interface_run.f90:221-236).
+        Create the context with read_states=True so that step 1 keeps them."""
+        if int(mhm.mask.sum()) != self.dom.n_cells:
+            raise MhmError(f"restart has {int(mhm.mask.sum())} L1 cells, the domain {self.dom.n_cells}")
+        self.set_eff_params(mhm.eff_params(scene), member)
+        st = dict(mhm.states)
+        if mrm is not None:
+            if int(mrm.mask.sum()) != self.dom.n_nodes:
+                raise MhmError(f"restart has {int(mrm.mask.sum())} L11 nodes, the domain {self.dom.n_nodes}")
+            st.update(mrm.states)
+        self.set_state(st, member)
+
+    def write_restart(self, mhm_path, params_by_scene: list[dict], mask=None, mrm_path=None, mask11=None,
+                      network: dict | None = None, member: int = 0):
+        """Write the member's states (and the given scenes' effective
+        parameters) as an mHM restart, and its routing states as an mRM
+        restart, in the reference's layout.  mask / mask11: the L1 / L11 grids
+        ([ncols][nrows] bool, default one row of all cells)."""
+        from . import restart
+        st = self.get_state(member)
+        m1 = np.ones((1, self.dom.n_cells), bool) if mask is None else np.asarray(mask, bool)
+        restart.write_mhm_restart(mhm_path, m1, st, params_by_scene, self.dom.horizon_depth)
+        if mrm_path is not None:
+            m11 = np.ones((1, self.dom.n_nodes), bool) if mask11 is None else np.asarray(mask11, bool)
+            restart.write_mrm_restart(mrm_path, m11, {k: st[k] for k in restart.MRM_STATES.values()},
+                                      network or {}, mask1=m1)
 
     def get_variable(self, name: str, member: int = 0) -> np.ndarray:
         n = {"L1_SOILMOIST": self.dom.n_horizons * self.dom.n_cells, "L11_QMOD": self.dom.n_nodes,

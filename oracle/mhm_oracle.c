@@ -480,6 +480,14 @@ void ora_dec2date(double julian, int32_t *dd, int32_t *mm, int32_t *yy, int32_t 
 void ora_step_calendar(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
                        int32_t *hour, int32_t *doy, int32_t *day, int32_t *year)
 {
+    ora_step_calendar_ex(jul_start, timestep, nSteps, month, hour, doy, day, year, NULL);
+}
+
+/* ... and is_new_day / is_new_month / is_new_year as set by the increment that
+ * follows step tt (bits 1, 2, 3 of new_flags[tt]) */
+void ora_step_calendar_ex(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
+                          int32_t *hour, int32_t *doy, int32_t *day, int32_t *year, int32_t *new_flags)
+{
     double newTime = (double)jul_start;
     int32_t y, m, d, h = 0;
     ora_caldat((int32_t)newTime, &d, &m, &y);
@@ -492,10 +500,13 @@ void ora_step_calendar(int32_t jul_start, int32_t timestep, int32_t nSteps, int3
         if (year) year[tt] = yy;
         if (doy) doy[tt] = ora_julday(dd, mm, yy) - ora_julday(1, 1, yy) + 1;
         /* increment */
+        const int32_t pd = d, pm = m, py = y;
         h = h + timestep;
         newTime = (double)ora_julday(d, m, y) + (double)h / 24.0;
         h = h % 24;
         ora_caldat((int32_t)newTime, &d, &m, &y);
+        if (new_flags)
+            new_flags[tt] = (pd != d ? 2 : 0) | (pm != m ? 4 : 0) | (py != y ? 8 : 0);
     }
 }
 
@@ -750,9 +761,54 @@ double ora_update_param_case2(double celerity, const double *length, int nLinks,
     return ts;
 }
 
+/* ---- aggregated outputs ---- */
+
+/* variables in the order mHM_OutputDataset creates them
+ * (src/mHM/mo_write_fluxes_states.f90:82-262) */
+static const int ORA_OUT_ORDER[21] = {1, 2, 3, 4, 5, 6, 7, 8, 18, 9, 10, 11, 12, 13, 14, 15, 16, 17, 19, 20, 21};
+
+int ora_output_planes(ora_output *o, int nH)
+{
+    int n = 0;
+    for (int f = 0; f < 22; ++f)
+        o->plane[f] = -1;
+    for (int i = 0; i < 21; ++i) {
+        const int f = ORA_OUT_ORDER[i];
+        if (!o->flags[f - 1])
+            continue;
+        if (f == 18)
+            return -1; /* neutrons: process 10 */
+        o->plane[f] = n;
+        n += (f == 3 || f == 4 || f == 17 || f == 19) ? nH : 1;
+    }
+    o->n_planes = n;
+    return n;
+}
+
+/* datetimeinfo_writeout, src/common/mo_common_datetime_type.f90:157-185 */
+static int ora_writeout(int interval, int32_t tindex, int32_t tt, int32_t n_tt, int32_t new_flags)
+{
+    if (interval > 0)
+        return (tindex % interval == 0) || tt == n_tt;
+    switch (interval) {
+    case 0: return tt == n_tt;
+    case -1: return (new_flags & 2) || tt == n_tt;
+    case -2: return (new_flags & 4) || tt == n_tt;
+    case -3: return (new_flags & 8) || tt == n_tt;
+    default: return 0; /* no output at all */
+    }
+}
+
 int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
             int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff_out, double *qmod_out,
             int nthreads)
+{
+    return ora_run_ex(d, p, s, f, tt0, nT, q_gauge, total_runoff_out, qmod_out, nthreads, NULL);
+}
+
+int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
+               int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff_out, double *qmod_out,
+               int nthreads, ora_output *out)
 {
     const int N = d->nCells, H = d->nH, L = d->nNodes;
     const int nLinks = L - d->nOutlets;
@@ -760,11 +816,13 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
     const double nTstepDay_dp = 24.0 / (double)d->timestep;   /* nTstepDay = 24/timestep */
     if (tt0 < 1 || nT < 0 || H < 1 || H > 16)
         return -1;
-    int32_t *cal = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(tt0 + nT));
+    int32_t *cal = (int32_t *)malloc(sizeof(int32_t) * 4 * (size_t)(tt0 + nT));
     if (!cal)
         return -2;
     int32_t *cal_month = cal, *cal_hour = cal + (tt0 + nT), *cal_doy = cal + 2 * (tt0 + nT);
-    ora_step_calendar(d->jul_start, d->timestep, tt0 - 1 + nT, cal_month, cal_hour, cal_doy, NULL, NULL);
+    int32_t *cal_new = cal + 3 * (tt0 + nT);
+    ora_step_calendar_ex(d->jul_start, d->timestep, tt0 - 1 + nT, cal_month, cal_hour, cal_doy, NULL, NULL,
+                         cal_new);
     double *pet_calc = (double *)malloc(sizeof(double) * (size_t)N);
     double *temp_calc = (double *)malloc(sizeof(double) * (size_t)N);
     double *prec_calc = (double *)malloc(sizeof(double) * (size_t)N);
@@ -830,6 +888,19 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
         const double *tmax = f->tmax ? f->tmax + (size_t)row * N : NULL;
         const double evap_coeff = d->evap_coeff[month - 1];
         const int iLAI = month; /* timeStep_LAI_input = 0 (mo_common_datetime_type.f90:135-155) */
+        /* this step's outputs (write_output after do_time_step) */
+        const int out_on = out && out->n_planes > 0 && tt > out->warm_steps;
+        int out_write = 0, out_slot = 0;
+        double out_cnt = 0.0;
+        if (out_on) {
+            out_write = ora_writeout(out->interval, tt - out->warm_steps, tt, out->n_time_steps, cal_new[tt - 1]);
+            out_slot = out->n_slots;
+            out_cnt = (double)(out->counter + 1);
+            if (out_write && out_slot >= out->max_slots) {
+                free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro); free(qacc);
+                return -5;
+            }
+        }
         if (tt == 1 && !d->read_states) /* mo_mhm.f90:448-450 */
             for (int h = 0; h < H; ++h)
                 for (int k = 0; k < N; ++k)
@@ -884,7 +955,7 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
             }
             double runoff_sealed, aet_sealed;
             ora_soil_moisture(d->proc_sm, H, p->fSealed[k], p->sealedThresh[k], pet_k, evap_coeff, sm_sat,
-                              froots, fc, pw, beta, p->jarvis_c1[k], aet_canopy, prec_effect,
+                              froots, fc, pw, beta, p->jarvis_c1 ? p->jarvis_c1[k] : 0.0, aet_canopy, prec_effect,
                               &runoff_sealed, &s->sealSTW[k], infil, sm, aet, &aet_sealed);
             for (int h = 0; h < H; ++h)
                 s->SM[(size_t)h * N + k] = sm[h];
@@ -894,6 +965,74 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
                                   &s->unsat[k], &slow, &fast, &perc);
             ora_runoff_sat_zone(c2TSTu / p->kBaseFlow[k], &s->sat[k], &base);
             tro[k] = ora_L1_total_runoff(p->fSealed[k], fast, slow, base, runoff_sealed);
+
+            if (out_on) { /* mHM_updateDataset, src/mHM/mo_write_fluxes_states.f90:283-438 */
+                const int w = out->tt_w == tt;
+                const double fS = w ? out->w_fsealed[k] : p->fSealed[k];
+                const double fNS = 1.0 - fS; /* run_cfg%L1_fNotSealed */
+                const int *pl = out->plane;
+                double *A = out->acc;
+#define ORA_ADD(PLANE, X) (A[(size_t)(PLANE) * N + k] = A[(size_t)(PLANE) * N + k] + (X))
+                if (pl[1] >= 0) ORA_ADD(pl[1], s->interc[k]);
+                if (pl[2] >= 0) ORA_ADD(pl[2], s->snowpack[k]);
+                for (int h = 0; h < H; ++h) {
+                    const double sat_h = w ? out->w_sms[(size_t)h * N + k] : sm_sat[h];
+                    if (pl[3] >= 0) ORA_ADD(pl[3] + h, sm[h]);
+                    if (pl[4] >= 0) ORA_ADD(pl[4] + h, sm[h] / sat_h);
+                }
+                if (pl[5] >= 0) {
+                    double ssm = 0.0, ssat = 0.0;
+                    for (int h = 0; h < H; ++h) {
+                        ssm = ssm + sm[h];
+                        ssat = ssat + (w ? out->w_sms[(size_t)h * N + k] : sm_sat[h]);
+                    }
+                    ORA_ADD(pl[5], ssm / ssat);
+                }
+                if (pl[6] >= 0) ORA_ADD(pl[6], s->sealSTW[k]);
+                if (pl[7] >= 0) ORA_ADD(pl[7], s->unsat[k]);
+                if (pl[8] >= 0) ORA_ADD(pl[8], s->sat[k]);
+                if (pl[9] >= 0) ORA_ADD(pl[9], pet_k);
+                if (pl[10] >= 0) {
+                    double aet_soil = 0.0;
+                    for (int h = 0; h < H; ++h)
+                        aet_soil = aet_soil + aet[h];
+                    ORA_ADD(pl[10], aet_soil * fNS + aet_canopy + aet_sealed * fS);
+                }
+                if (pl[11] >= 0) ORA_ADD(pl[11], tro[k]);
+                if (pl[12] >= 0) ORA_ADD(pl[12], runoff_sealed * fS);
+                if (pl[13] >= 0) ORA_ADD(pl[13], fast * fNS);
+                if (pl[14] >= 0) ORA_ADD(pl[14], slow * fNS);
+                if (pl[15] >= 0) ORA_ADD(pl[15], base * fNS);
+                if (pl[16] >= 0) ORA_ADD(pl[16], perc * fNS);
+                for (int h = 0; h < H; ++h) {
+                    if (pl[17] >= 0) ORA_ADD(pl[17] + h, infil[h] * fNS);
+                    if (pl[19] >= 0) ORA_ADD(pl[19] + h, aet[h] * fNS);
+                }
+                if (pl[20] >= 0) ORA_ADD(pl[20], prec_effect);
+                if (pl[21] >= 0) ORA_ADD(pl[21], melt);
+#undef ORA_ADD
+                if (out_write) { /* writeVariableTimestep, src/common/mo_nc_output.f90:158-175 */
+                    for (int i = 0; i < 21; ++i) {
+                        const int fl = ORA_OUT_ORDER[i];
+                        if (pl[fl] < 0)
+                            continue;
+                        const int np = (fl == 3 || fl == 4 || fl == 17 || fl == 19) ? H : 1;
+                        for (int j = 0; j < np; ++j) {
+                            const size_t a = (size_t)(pl[fl] + j) * N + k;
+                            const double v = (fl <= 8) ? A[a] / out_cnt : A[a]; /* avg for the states */
+                            out->out[((size_t)out_slot * out->n_planes + pl[fl] + j) * N + k] = v;
+                            A[a] = 0.0;
+                        }
+                    }
+                }
+            }
+        }
+        if (out_on) {
+            out->counter = out_write ? 0 : out->counter + 1;
+            if (out_write) {
+                out->slot_tt[out->n_slots] = tt;
+                out->n_slots = out->n_slots + 1;
+            }
         }
         if (total_runoff_out)
             memcpy(total_runoff_out + (size_t)it * N, tro, sizeof(double) * (size_t)N);
@@ -956,6 +1095,26 @@ int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_fo
                     if (qmod_out)
                         memcpy(qmod_out + (size_t)jt * L, s->Qmod, sizeof(double) * (size_t)L);
                 }
+            }
+        }
+        /* mRM_updateDataset with the discharge state after this step
+         * (src/mRM/mo_mrm_write_fluxes_states.f90:130-133; Qrouted is a mean) */
+        if (out && out->qrouted && d->proc_rout >= 1 && tt > out->warm_steps) {
+            for (int i = 0; i < L; ++i)
+                out->acc_mrm[i] = out->acc_mrm[i] + s->Qmod[i];
+            out->counter_mrm = out->counter_mrm + 1;
+            if (ora_writeout(out->interval_mrm, tt - out->warm_steps, tt, out->n_time_steps, cal_new[tt - 1])) {
+                if (out->n_slots_mrm >= out->max_slots) {
+                    free(qacc); free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
+                    return -5;
+                }
+                for (int i = 0; i < L; ++i) {
+                    out->out_mrm[(size_t)out->n_slots_mrm * L + i] = out->acc_mrm[i] / (double)out->counter_mrm;
+                    out->acc_mrm[i] = 0.0;
+                }
+                out->slot_tt_mrm[out->n_slots_mrm] = tt;
+                out->n_slots_mrm = out->n_slots_mrm + 1;
+                out->counter_mrm = 0;
             }
         }
     }

@@ -76,6 +76,8 @@ void ora_dec2date(double julian, int32_t *dd, int32_t *mm, int32_t *yy, int32_t 
  * month[tt-1], hour, doy, day, year. */
 void ora_step_calendar(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
                        int32_t *hour, int32_t *doy, int32_t *day, int32_t *year);
+void ora_step_calendar_ex(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
+                          int32_t *hour, int32_t *doy, int32_t *day, int32_t *year, int32_t *new_flags);
 
 /* ---- routing ---- */
 void ora_reg_rout(const double *param5, const double *length, const double *slope,
@@ -156,12 +158,46 @@ typedef struct {
     int32_t n_rows;
 } ora_forcing;
 
+/* Aggregated outputs of the run (mhm_interface_run_write_output,
+ * src/mHM/mo_mhm_interface_run.f90:641-742): mHM's outputFlxState variables
+ * (src/mHM/mo_write_fluxes_states.f90) and mRM's Qrouted
+ * (src/mRM/mo_mrm_write_fluxes_states.f90), summed per step after the
+ * warm-up and written at the end of each interval (src/common/mo_nc_output.f90:
+ * 140-175, src/common/mo_common_datetime_type.f90:157-185).  Counters and sums
+ * carry over between ora_run_ex calls. */
+typedef struct {
+    int32_t interval, interval_mrm;  /* timeStep_model_outputs, timeStep_model_outputs_mrm */
+    int32_t warm_steps, n_time_steps;
+    int32_t flags[21];               /* outputFlxState(1..21) (18, neutrons, not supported) */
+    int32_t qrouted;                 /* outputFlxState_mrm(1) */
+    int32_t max_slots;
+    int32_t n_planes;                /* set by ora_output_planes */
+    int32_t plane[22];               /* first plane of variable f (1-based), -1 if off */
+    int32_t counter, counter_mrm, n_slots, n_slots_mrm;
+    int32_t tt_w;                    /* step whose outputs use w_fsealed / w_sms (0: none) */
+    int32_t pad_;
+    double *acc, *out;               /* [n_planes][nCells], [max_slots][n_planes][nCells] */
+    int32_t *slot_tt;                /* [max_slots] step that closed each interval */
+    double *acc_mrm, *out_mrm;       /* [nNodes], [max_slots][nNodes] */
+    int32_t *slot_tt_mrm;
+    const double *w_fsealed, *w_sms; /* [nCells], [nH][nCells] */
+} ora_output;
+
+/* Plane layout in the order of the output file's variables; returns n_planes
+ * (or -1 for an unsupported variable). */
+int ora_output_planes(ora_output *o, int nH);
+
 /* Run steps tt = tt0 .. tt0+nT-1 (1-based, tt0 >= 1).  Outputs (any may be NULL):
  * q_gauge[nT][nGauges], total_runoff[nT][nCells], qmod[nT][nNodes].
  * nthreads <= 0: OpenMP default.  Returns 0 on success. */
 int ora_run(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
             int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff, double *qmod,
             int nthreads);
+/* ora_run plus aggregated outputs (out may be NULL); returns -5 when an
+ * interval would overflow max_slots */
+int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora_forcing *f,
+               int32_t tt0, int32_t nT, double *q_gauge, double *total_runoff, double *qmod,
+               int nthreads, ora_output *out);
 
 /* Set the reference's default initial states (mo_init_states.f90:258-345,
  * mo_mrm_init.f90:453-499).  horizon_depth[nH] in mm. */

@@ -65,6 +65,17 @@ class OraForcing(C.Structure):
                 ("forc_row0", C.c_int32), ("n_rows", C.c_int32)]
 
 
+class OraOutput(C.Structure):
+    _fields_ = [
+        ("interval", C.c_int32), ("interval_mrm", C.c_int32), ("warm_steps", C.c_int32),
+        ("n_time_steps", C.c_int32), ("flags", C.c_int32 * 21), ("qrouted", C.c_int32), ("max_slots", C.c_int32),
+        ("n_planes", C.c_int32), ("plane", C.c_int32 * 22), ("counter", C.c_int32), ("counter_mrm", C.c_int32),
+        ("n_slots", C.c_int32), ("n_slots_mrm", C.c_int32), ("tt_w", C.c_int32), ("pad_", C.c_int32),
+        ("acc", _dp), ("out", _dp), ("slot_tt", _ip), ("acc_mrm", _dp), ("out_mrm", _dp), ("slot_tt_mrm", _ip),
+        ("w_fsealed", _dp), ("w_sms", _dp),
+    ]
+
+
 class OraMprDomain(C.Structure):
     _fields_ = [
         ("nCells0", C.c_int32), ("nrows0", C.c_int32), ("ncols0", C.c_int32), ("nCells1", C.c_int32),
@@ -149,6 +160,12 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_update_param_case2.restype = d
     L.ora_run.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
                           C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int]
+    L.ora_run_ex.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
+                             C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int,
+                             C.POINTER(OraOutput)]
+    L.ora_output_planes.argtypes = [C.POINTER(OraOutput), C.c_int]
+    L.ora_output_planes.restype = C.c_int
+    L.ora_step_calendar_ex.argtypes = [C.c_int32, C.c_int32, C.c_int32, _ip, _ip, _ip, _ip, _ip, _ip]
     L.ora_default_states.argtypes = [C.POINTER(OraDomain), _dp, C.POINTER(OraState)]
     L.ora_math_kind.restype = C.c_int
     L.ora_mpr.argtypes = [C.POINTER(OraMprDomain), C.POINTER(OraGamma), C.POINTER(OraMprOut)]
@@ -214,6 +231,47 @@ class OracleRun:
         hd = k(dom.horizon_depth)
         self.L.ora_default_states(C.byref(self.d), _d(hd), C.byref(self.s))
 
+    def enable_outputs(self, interval: int, flags, warm_steps: int, n_time_steps: int, max_slots: int,
+                       interval_mrm: int | None = None, qrouted: bool = False):
+        """Aggregated outputs of the following runs: flags = outputFlxState(1..21)
+        (21 ints); Qrouted with `qrouted` at `interval_mrm`."""
+        o = OraOutput()
+        o.interval = interval
+        o.interval_mrm = interval if interval_mrm is None else interval_mrm
+        o.warm_steps, o.n_time_steps, o.max_slots = warm_steps, n_time_steps, max_slots
+        for i, f in enumerate(flags):
+            o.flags[i] = int(bool(f))
+        o.qrouted = int(qrouted)
+        N, H, Ln = self.dom.n_cells, self.dom.n_horizons, self.dom.n_nodes
+        n = self.L.ora_output_planes(C.byref(o), H)
+        if n < 0:
+            raise ValueError("unsupported output variable")
+        self.out_buf = {"acc": np.zeros(max(n, 1) * N), "out": np.zeros(max_slots * max(n, 1) * N),
+                        "slot_tt": np.zeros(max_slots, np.int32), "acc_mrm": np.zeros(Ln),
+                        "out_mrm": np.zeros(max_slots * Ln), "slot_tt_mrm": np.zeros(max_slots, np.int32)}
+        for k in ("acc", "out", "acc_mrm", "out_mrm"):
+            setattr(o, k, _d(self.out_buf[k]))
+        o.slot_tt, o.slot_tt_mrm = _i(self.out_buf["slot_tt"]), _i(self.out_buf["slot_tt_mrm"])
+        self.out = o
+
+    def set_output_weights(self, tt: int, fsealed, soil_moist_sat):
+        """Outputs of step tt weighted with these fSealed / soilMoistSat."""
+        self.out_w = (np.ascontiguousarray(fsealed, np.float64), np.ascontiguousarray(soil_moist_sat, np.float64))
+        self.out.tt_w = tt
+        self.out.w_fsealed, self.out.w_sms = _d(self.out_w[0]), _d(self.out_w[1])
+
+    def read_outputs(self):
+        """(fluxes/states [slots][planes][cells], their closing steps, Qrouted
+        [slots][nodes], its closing steps); frees the slots."""
+        o, b = self.out, self.out_buf
+        N, Ln = self.dom.n_cells, self.dom.n_nodes
+        n = o.n_planes
+        fs = b["out"][: o.n_slots * n * N].reshape(o.n_slots, n, N).copy()
+        qr = b["out_mrm"][: o.n_slots_mrm * Ln].reshape(o.n_slots_mrm, Ln).copy()
+        r = (fs, b["slot_tt"][: o.n_slots].copy(), qr, b["slot_tt_mrm"][: o.n_slots_mrm].copy())
+        o.n_slots = o.n_slots_mrm = 0
+        return r
+
     def run(self, forcing: dict, row0: int, tt0: int, n_steps: int, nthreads: int = 0,
             want_tro: bool = False, want_qmod: bool = False):
         f = OraForcing()
@@ -230,8 +288,9 @@ class OracleRun:
         q = np.zeros((n_steps, G))
         tro = np.zeros((n_steps, self.dom.n_cells)) if want_tro else None
         qm = np.zeros((n_steps, self.dom.n_nodes)) if want_qmod else None
-        rc = self.L.ora_run(C.byref(self.d), C.byref(self.p), C.byref(self.s), C.byref(f), tt0, n_steps,
-                            _d(q), _d(tro), _d(qm), nthreads)
+        out = getattr(self, "out", None)
+        rc = self.L.ora_run_ex(C.byref(self.d), C.byref(self.p), C.byref(self.s), C.byref(f), tt0, n_steps,
+                               _d(q), _d(tro), _d(qm), nthreads, C.byref(out) if out is not None else None)
         if rc != 0:
             raise RuntimeError(f"ora_run failed ({rc})")
         return q, tro, qm

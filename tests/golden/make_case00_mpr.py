@@ -32,7 +32,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
-import h5lite  # noqa: E402
+sys.path.insert(0, str(HERE.parents[1]))
+from mhm_gb300 import h5read as h5lite  # noqa: E402
 
 REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
 TD = REF / "test_domain" / "input"

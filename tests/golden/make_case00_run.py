@@ -19,9 +19,16 @@ the LAI-based PET correction (processCase(5) = -1), case_09 with
 Hargreaves-Samani PET (daily tmin/tmax) and adaptive routing case 2; their
 parameter vectors (from their mhm_parameter.nml), L1 parameters, final
 states and daily discharge.
+
+Every case also gets its aggregated outputs: the variables of
+b1_mHM_Fluxes_States.nc ("fs_<name>", [interval][cell]) and the Qrouted of
+b1_mRM_Fluxes_States.nc ("qrouted", [interval][node]) with the output
+settings of its mhm_outputs.nml / mrm_outputs.nml ("out_interval",
+"out_flags", "out_interval_mrm", "out_qrouted").
 """
 from __future__ import annotations
 
+import re
 import sys
 from pathlib import Path
 
@@ -29,7 +36,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
-import h5lite  # noqa: E402
+sys.path.insert(0, str(HERE.parents[1]))
+from mhm_gb300 import h5read as h5lite  # noqa: E402
 
 REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
 TD = REF / "test_domain" / "input"
@@ -45,6 +53,45 @@ SIM_START = (1990, 1, 1)      # eval_Per start 1990-07-01 minus warming_days 181
 SIM_DAYS = 546                # .. 1991-06-30
 WARMING_DAYS = 181
 SCENE2_FROM_DAY = 365         # land-cover scene 1991 from 1991-01-01 on
+
+
+def output_settings(cdir):
+    """timeStep_model_outputs, outputFlxState(1..21), timeStep_model_outputs_mrm
+    and outputFlxState_mrm(1) from a case's output namelists."""
+    def strip(path):
+        return "\n".join(ln.split("!")[0] for ln in path.read_text().splitlines())
+    mhm = strip(cdir / "mhm_outputs.nml")
+    mrm = strip(cdir / "mrm_outputs.nml") if (cdir / "mrm_outputs.nml").exists() else ""
+    interval = int(re.search(r"timeStep_model_outputs\s*=\s*(-?\d+)", mhm).group(1))
+    flags = np.zeros(21, np.int32)
+    for i, v in re.findall(r"outputFlxState\((\d+)\)\s*=\s*\.(TRUE|FALSE)\.", mhm, re.I):
+        flags[int(i) - 1] = v.upper() == "TRUE"
+    m = re.search(r"timeStep_model_outputs_mrm\s*=\s*(-?\d+)", mrm)
+    interval_mrm = int(m.group(1)) if m else 0
+    q = re.search(r"outputFlxState_mrm\(1\)\s*=\s*\.(TRUE|FALSE)\.", mrm, re.I)
+    return interval, flags, interval_mrm, int(bool(q and q.group(1).upper() == "TRUE"))
+
+
+def output_golds(cdir, mask):
+    """Aggregated outputs written by a case, packed over the L1 (= L11) mask."""
+    interval, flags, interval_mrm, qrouted = output_settings(cdir)
+    gold = dict(out_interval=interval, out_flags=flags, out_interval_mrm=interval_mrm, out_qrouted=qrouted)
+    fpath = cdir / "output_save" / "b1_mHM_Fluxes_States.nc"
+    if fpath.exists():
+        f = h5lite.H5File(str(fpath))
+        skip = {"easting", "northing", "easting_bnds", "northing_bnds", "lon", "lat", "time", "time_bnds", "bnds"}
+        for name in f.group():
+            if name not in skip:
+                a = f.read(name)
+                gold["fs_" + name] = np.stack([a[i][mask] for i in range(a.shape[0])])
+        gold["fs_time_bnds"] = f.read("time_bnds")
+    rpath = cdir / "output_save" / "b1_mRM_Fluxes_States.nc"
+    if rpath.exists():
+        f = h5lite.H5File(str(rpath))
+        a = f.read("Qrouted")
+        gold["qrouted"] = np.stack([a[i][mask] for i in range(a.shape[0])])
+        gold["qrouted_time_bnds"] = f.read("time_bnds")
+    return gold
 
 
 def julday(y, m, d):
@@ -77,6 +124,7 @@ def main():
     n_links = int(mrm.read("L11_fromN").size) - 1
     ffp = mrm.read("L11_nLinkFracFPimp")                      # [scene][y][x], link i at packed position i
     q = np.loadtxt(CASE / "output_save" / "b1_daily_discharge.out", skiprows=1)
+    qtext = (CASE / "output_save" / "b1_daily_discharge.out").read_text()
     gold_states = {}
     for name in ("L1_Inter", "L1_snowPack", "L1_sealSTW", "L1_unsatSTW", "L1_satSTW"):
         gold_states[name] = mhm.read(name)[mask1]
@@ -103,7 +151,9 @@ def main():
         latitude=mrm.read("L1_domain_lat")[mask1],
         evap_coeff=np.array(EVAP_COEFF), fnight_pet=np.array(FNIGHT_PET), fnight_prec=np.array(FNIGHT_PREC),
         fnight_temp=np.array(FNIGHT_TEMP), gold_q_daily=q[:, 5], gold_q_dmy=q[:, 1:4].astype(np.int32),
-        **{"gold_" + k: v for k, v in gold_states.items()})
+        gold_q_obs=q[:, 4], gold_gauge_id=int(qtext.split()[4][5:]),
+        gold_daily_text=np.frombuffer(qtext.encode(), np.uint8),
+        **{"gold_" + k: v for k, v in gold_states.items()}, **output_golds(CASE, mask1))
     print("wrote", HERE / "case00_run.npz", "cells", n, "links", n_links, "days", SIM_DAYS)
 
 
@@ -152,7 +202,8 @@ def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
         n_links = int(mrm.read("L11_fromN").size) - 1
         extra = dict(length=mrm.read("L11_length")[:n_links], ts_rout=float(mrm.read("L11_TSrout")[0]))
     np.savez_compressed(HERE / f"{case.replace('_', '')}_gold.npz", gamma=np.array(gamma), proc_sm=proc_sm,
-                        proc_pet=proc_pet, proc_rout=proc_rout, q_daily=q[:, 5], **gold, **extra)
+                        proc_pet=proc_pet, proc_rout=proc_rout, q_daily=q[:, 5], **gold, **extra,
+                        **output_golds(cdir, mask1))
     print("wrote", HERE / f"{case.replace('_', '')}_gold.npz", len(gamma), sorted(gold))
 
 

@@ -23,7 +23,7 @@ from types import SimpleNamespace
 import numpy as np
 import pytest
 
-from mhm_gb300 import params
+from mhm_gb300 import outputs, params
 from oracle import oracle
 
 import test_case00_mpr as mpr_case
@@ -54,8 +54,15 @@ def load_run():
 def daily_means(q_steps, warming_days):
     """sum(Q(iS:iE)) / 24 over each evaluation day, summed in step order
     (src/mRM/mo_mrm_write.f90:138-149)."""
-    days = q_steps[warming_days * 24:].reshape(-1, 24)
-    return np.cumsum(days, axis=1)[:, -1] / 24.0
+    return outputs.daily_discharge(q_steps, warming_days, 24)
+
+
+def check_daily_text(z, qd):
+    """b1_daily_discharge.out written from our daily discharge equals the
+    reference's file byte for byte."""
+    text = outputs.format_daily_discharge(int(z["jul_start"]) + int(z["warming_days"]), [int(z["gold_gauge_id"])],
+                                          z["gold_q_obs"], qd)
+    assert text.encode() == bytes(z["gold_daily_text"])
 
 
 # mHM() reads these with land-cover index 1 whatever the scene
@@ -164,11 +171,66 @@ def test_oracle_reproduces_case_discharge_and_states(case, kind):
     q = np.concatenate([q1[:, 0], q2[:, 0]])
     qd = daily_means(q, int(z["warming_days"]))
     assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), (case, kind, np.abs(qd - gold["q"]).max())
+    if case == "case_00":
+        check_daily_text(z, qd)
     st = dict(r2.state)
     st["soilMoist"] = st.pop("SM")
     st["unsatSTW"], st["satSTW"] = st.pop("unsat"), st.pop("sat")
     bad = check_states(gold, st, 0.0 if kind == "libm" else HMATH_RTOL)
     assert not bad, (case, bad)
+
+
+def output_golds(case):
+    """(settings, {plane name: [interval][cell]}, Qrouted [interval][node] or None)
+    of a case's b1_mHM/mRM_Fluxes_States.nc."""
+    z = np.load(FIX if case == "case_00" else GOLD_DIR / f"{case.replace('_', '')}_gold.npz")
+    cfg = dict(interval=int(z["out_interval"]), flags=[int(f) for f in z["out_flags"]],
+               interval_mrm=int(z["out_interval_mrm"]), qrouted=bool(z["out_qrouted"]))
+    fs = {k[3:]: z[k] for k in z.files if k.startswith("fs_") and k != "fs_time_bnds"}
+    return cfg, fs, (z["qrouted"] if "qrouted" in z.files else None)
+
+
+@pytest.mark.parametrize("kind", ["libm", "hmath"])
+@pytest.mark.parametrize("case", list(CASES))
+def test_oracle_reproduces_case_outputs(case, kind):
+    """b1_mHM_Fluxes_States.nc (SWC, Q, PET, aET, recharge over the evaluation
+    year) and b1_mRM_Fluxes_States.nc (Qrouted, daily means or the year's
+    mean at every node)."""
+    z, doms, forcing = load_run()
+    gamma, (proc_sm, proc_pet, proc_rout), gold = case_setup(case)
+    doms = case_domains(case, doms, gold)
+    cfg, fs_gold, qr_gold = output_golds(case)
+    p, rp = regionalised(kind, gamma, proc_sm, proc_pet, proc_rout)
+    n_steps = int(z["sim_days"]) * 24
+    s2 = int(z["scene2_from_day"]) * 24
+    warm = int(z["warming_days"]) * 24
+    kw = dict(rout_param=rp, proc_sm=proc_sm, proc_pet=proc_pet, proc_rout=proc_rout, hourly=False, kind=kind)
+    r1 = oracle.OracleRun(doms[0], p[0], **kw)
+    r1.enable_outputs(cfg["interval"], cfg["flags"], warm, n_steps, 400, cfg["interval_mrm"], cfg["qrouted"])
+    # the last step of 1990 is written with the 1991 scene's weights
+    r1.set_output_weights(s2, p[1]["fSealed"], np.reshape(p[1]["soilMoistSat"], (H, -1)))
+    r1.run(forcing, 1, 1, s2)
+    r2 = oracle.OracleRun(doms[1], p[1], **kw)
+    for k, v in r1.state.items():
+        if k not in ("C1", "C2"):
+            np.copyto(r2.state[k], v)
+    r2.out, r2.out_buf = r1.out, r1.out_buf     # the output datasets carry over
+    r2.out.tt_w = 0
+    r2.run(forcing, 1, s2 + 1, n_steps - s2)
+    fs, fs_tt, qr, qr_tt = r2.read_outputs()
+    names = outputs.plane_names(cfg["flags"], H)
+    assert sorted(names) == sorted(fs_gold)
+    assert fs.shape[0] == next(iter(fs_gold.values())).shape[0]
+    tol = 0.0 if kind == "libm" else HMATH_RTOL
+    for i, name in enumerate(names):
+        want = fs_gold[name]
+        err = np.max(np.abs(fs[:, i] - want) / np.maximum(np.abs(want), 1e-300))
+        assert np.array_equal(fs[:, i], want) or err <= tol, (case, kind, name, err)
+    if qr_gold is not None:
+        assert qr.shape == qr_gold.shape
+        err = np.max(np.abs(qr - qr_gold) / np.maximum(np.abs(qr_gold), 1e-300))
+        assert np.array_equal(qr, qr_gold) or err <= tol, (case, kind, "Qrouted", err)
+    assert fs_tt[-1] == n_steps
 
 
 @pytest.mark.gpu
@@ -206,6 +268,8 @@ def test_gpu_reproduces_case_discharge_and_states(case):
     q = np.concatenate([q1, q2])
     qd = daily_means(q, int(z["warming_days"]))
     assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), np.abs(qd - gold["q"]).max()
+    if case == "case_00":
+        check_daily_text(z, qd)
     bad = check_states(gold, st, HMATH_RTOL)
     assert not bad, bad
     # and the device equals the oracle's hmath build bit for bit
@@ -217,3 +281,55 @@ def test_gpu_reproduces_case_discharge_and_states(case):
         assert np.allclose(o1[:, 0], q1, rtol=1e-12, atol=0)
     else:
         assert np.array_equal(o1[:, 0], q1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", list(CASES))
+def test_gpu_reproduces_case_outputs(case):
+    """The device's aggregated outputs against b1_mHM_Fluxes_States.nc and
+    b1_mRM_Fluxes_States.nc."""
+    from mhm_gb300.model import MhmGpu
+    z, doms, forcing = load_run()
+    l0_for, _, _, n1 = mpr_case.load_case()
+    gamma, (proc_sm, proc_pet, proc_rout), gold = case_setup(case)
+    doms = case_domains(case, doms, gold)
+    cfg, fs_gold, qr_gold = output_golds(case)
+    n_steps = int(z["sim_days"]) * 24
+    s2 = int(z["scene2_from_day"]) * 24
+    warm = int(z["warming_days"]) * 24
+    g = MhmGpu(doms[0], proc_soilmoist=proc_sm, proc_pet=proc_pet, proc_routing=proc_rout, hourly=False,
+               n_members=1)
+    try:
+        g.mpr_setup(l0_for(1))
+        g.mpr(gamma)
+        last = g.get_eff_params(0)
+        g.mpr_setup(l0_for(0))
+        g.mpr(gamma)
+        p0 = g.get_eff_params(0)
+        for k in SCENE_INDEPENDENT:
+            p0[k] = last[k]
+        g.set_eff_params(p0)
+        g.init_states(0)
+        g.enable_flux_state_outputs(cfg["flags"], cfg["interval"], warm, n_steps, max_slots=400)
+        if cfg["qrouted"]:
+            g.enable_routed_outputs(cfg["interval_mrm"], warm, n_steps, max_slots=400)
+        # the last step of 1990 is written with the 1991 scene's weights
+        g.set_output_weights(0, s2, last["fSealed"], np.reshape(last["soilMoistSat"], (H, -1)))
+        g.set_meteo(1, forcing["pre"], forcing["temp"], forcing["pet"], forcing["tmin"], forcing["tmax"])
+        g.run(1, s2)
+        g.mpr_setup(l0_for(1))
+        g.set_link_fpimp(doms[1].ffp_imp)
+        g.mpr(gamma)
+        g.run(s2 + 1, n_steps - s2)
+        names, fs, fs_tt = g.read_flux_state_outputs()
+        qr, _ = g.read_routed_outputs() if cfg["qrouted"] else (None, None)
+    finally:
+        g.close()
+    assert sorted(names) == sorted(fs_gold) and fs_tt[-1] == n_steps
+    for i, name in enumerate(names):
+        want = fs_gold[name]
+        err = np.max(np.abs(fs[:, i, 0] - want) / np.maximum(np.abs(want), 1e-300))
+        assert np.array_equal(fs[:, i, 0], want) or err <= HMATH_RTOL, (case, name, err)
+    if qr_gold is not None:
+        err = np.max(np.abs(qr[:, 0] - qr_gold) / np.maximum(np.abs(qr_gold), 1e-300))
+        assert qr.shape[0] == qr_gold.shape[0] and (np.array_equal(qr[:, 0], qr_gold) or err <= HMATH_RTOL), err
