@@ -66,9 +66,10 @@ typedef struct {
     int32_t timestep;            /* model time step [h] (mhm.nml timestep)     */
     int32_t proc_soilmoist;      /* processMatrix(3,1): 1..4                   */
     int32_t proc_pet;            /* processMatrix(5,1): -1, 0 or 1             */
-    int32_t proc_routing;        /* processMatrix(8,1): 0, 1 (Muskingum) or 2
+    int32_t proc_routing;        /* processMatrix(8,1): 0, 1 (Muskingum), 2
                                     (Muskingum with a routing time step chosen
-                                    from a constant celerity)                  */
+                                    from a constant celerity) or 3 (from each
+                                    link's celerity)                           */
     int32_t n_tstep_forcing_day; /* 24 (hourly forcing) or 1 (daily forcing)   */
     int32_t jul_start;           /* simPer%julStart (Julian day number)        */
     int32_t map_flag;            /* routing resolution >= hydrology resolution */
@@ -153,6 +154,14 @@ int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp);
  * summed over that many model steps, routed once and the result stands for
  * each of them (then every mhm_run must cover whole routing steps). */
 int mhm_set_routing_params(mhm_ctx *ctx, int32_t member, const double *rout_param5);
+/* Routing case 3 (mrm_update_param, src/mRM/mo_mrm_mpr.f90:241-329): the
+ * celerity of each link [n_links] (m s-1) for `member`, as L11_calc_celerity
+ * derives it from the L0 river path of the link and the slope_factor
+ * parameter (src/mRM/mo_mrm_net_startup.f90:2212-2423; see
+ * mhm_gb300.routing.link_celerity).  K = length / celerity per link; the
+ * routing step and C1/C2 then follow as in case 2.  (mhm_mpr leaves case-3
+ * coefficients to this call.) */
+int mhm_set_link_celerity(mhm_ctx *ctx, int32_t member, const double *celerity);
 
 /* Default initial states (fluxes_states_default_init,
  * src/mHM/mo_init_states.f90:258-345, and fluxes_states_default_init_routing,

@@ -323,21 +323,26 @@ int locate_ts(double y)
 // Routing case 2 for one member (mrm_update_param, src/mRM/mo_mrm_mpr.f90:
 // 241-329): K = length / celerity per link, TSrout from the smallest K,
 // Muskingum coefficients with xi = 0 (written at the links' positions).
-static int set_case2_member(mhm_ctx *ctx, int32_t m, double celerity)
+// mrm_update_param (src/mRM/mo_mrm_mpr.f90:241-329): K = length / celerity
+// per link -- one celerity for routing case 2, the link's own (L11_celerity)
+// for case 3 -- the routing step from the shortest K, C1/C2 with xi = 0.
+static int set_adaptive_member(mhm_ctx *ctx, int32_t m, double celerity, const double *link_celerity)
 {
     const size_t L = ctx->L;
     const int nl = ctx->n_links;
     if (nl == 0) return MHM_OK;
-    if (!(celerity > 0.0)) return fail(ctx, MHM_ERR_INVALID, "streamflow celerity must be positive");
+    auto cel = [&](int i) { return link_celerity ? link_celerity[i] : celerity; };
+    for (int i = 0; i < nl; ++i)
+        if (!(cel(i) > 0.0)) return fail(ctx, MHM_ERR_INVALID, "streamflow celerity must be positive");
     const double xi = std::fabs(0.0); // rout_space_weight
     double kmin = HUGE_VAL;
-    for (int i = 0; i < nl; ++i) kmin = std::min(kmin, ctx->length_h[i] / celerity);
+    for (int i = 0; i < nl; ++i) kmin = std::min(kmin, ctx->length_h[i] / cel(i));
     int ind = locate_ts(kmin);
     if (ind < 1) ind = 1;
     const double ts = kGivenTS[ind - 1];
     std::vector<double> c1(L, 0.0), c2(L, 0.0);
     for (int i = 0; i < nl; ++i) {
-        const double K = ctx->length_h[i] / celerity;
+        const double K = ctx->length_h[i] / cel(i);
         const double a = ts / (K * (1.0 - xi) + 0.5 * ts);
         c1[ctx->net.link_pos[i]] = a;
         c2[ctx->net.link_pos[i]] = 1.0 - a * K / ts;
@@ -455,7 +460,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     if (d->timestep < 1 || 24 % d->timestep != 0) return bad("timestep must divide 24 hours");
     if (d->proc_soilmoist < 1 || d->proc_soilmoist > 4) return bad("proc_soilmoist must be 1..4");
     if (d->proc_pet < -1 || d->proc_pet > 1) return bad("proc_pet must be -1, 0 or 1 (2, 3 unsupported)");
-    if (d->proc_routing < 0 || d->proc_routing > 2) return bad("proc_routing must be 0, 1 or 2");
+    if (d->proc_routing < 0 || d->proc_routing > 3) return bad("proc_routing must be 0, 1, 2 or 3");
     if (d->n_tstep_forcing_day != 24 && d->n_tstep_forcing_day != 1)
         return bad("n_tstep_forcing_day must be 24 or 1");
     if (d->jul_start < 2299161) return bad("jul_start before the Gregorian reform is not supported");
@@ -699,6 +704,15 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
     return MHM_OK;
 }
 
+int mhm_set_link_celerity(mhm_ctx *ctx, int32_t m, const double *celerity)
+{
+    if (!ctx || !celerity) return MHM_ERR_INVALID;
+    if (ctx->proc_rout != 3) return fail(ctx, MHM_ERR_INVALID, "per-link celerity is routing case 3");
+    if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
+    return set_adaptive_member(ctx, m, 0.0, celerity);
+}
+
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 {
     if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
@@ -750,7 +764,9 @@ int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
     if (!ctx || !p5) return MHM_ERR_INVALID;
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
-    if (ctx->proc_rout == 2) return set_case2_member(ctx, m, p5[0]); // p5[0]: streamflow celerity [m s-1]
+    if (ctx->proc_rout == 2) return set_adaptive_member(ctx, m, p5[0], nullptr); // p5[0]: celerity [m s-1]
+    if (ctx->proc_rout == 3)
+        return fail(ctx, MHM_ERR_INVALID, "routing case 3 takes the links' celerity: mhm_set_link_celerity");
     if (ctx->proc_rout != 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
     if (ctx->n_links == 0) return MHM_OK;
     const size_t L = ctx->L;
@@ -893,7 +909,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     // routing case 2: routing time step shorter than the model step -> R routing
     // passes per step; longer -> one pass per window of F steps
     int32_t R = 1, F = 1;
-    if (ctx->proc_rout == 2 && ctx->L > 1) {
+    if (ctx->proc_rout >= 2 && ctx->L > 1) {
         const double ts = ctx->ts_rout[0];
         for (size_t m = 1; m < M; ++m)
             if (ctx->ts_rout[m] != ts)
@@ -1879,7 +1895,8 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
     }
     if (ctx->proc_rout == 2)
         for (int32_t i = 0; i < n; ++i)
-            if (int rc = set_case2_member(ctx, member0 + i, gammas[(size_t)i * n_gamma + off.routing])) return rc;
+            if (int rc = set_adaptive_member(ctx, member0 + i, gammas[(size_t)i * n_gamma + off.routing], nullptr))
+                return rc;
     CK(cudaStreamSynchronize(s), "mpr sync");
     return MHM_OK;
 }
@@ -1909,7 +1926,7 @@ int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n
     if (!ctx || !gamma) return MHM_ERR_INVALID;
     if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
     if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
-    if (ctx->proc_rout == 2) return fail(ctx, MHM_ERR_UNSUPPORTED, "routing case 2: use mhm_mpr");
+    if (ctx->proc_rout >= 2) return fail(ctx, MHM_ERR_UNSUPPORTED, "adaptive routing: use mhm_mpr");
     const MprSetup &m = ctx->mpr;
     GammaOffsets off{};
     if (!gamma_layout(ctx->proc_sm, ctx->proc_pet, ctx->proc_rout, m.n_geo, off))

@@ -130,6 +130,11 @@ class MhmGpu:
         a = np.ascontiguousarray(p5, np.float64)
         self._check(self.L.mhm_set_routing_params(self.ctx, member, _d(a)), "mhm_set_routing_params")
 
+    def set_link_celerity(self, celerity, member: int = 0):
+        """Routing case 3: each link's celerity [m s-1] (routing.link_celerity)."""
+        a = np.ascontiguousarray(celerity, np.float64)
+        self._check(self.L.mhm_set_link_celerity(self.ctx, member, _d(a)), "mhm_set_link_celerity")
+
     def set_link_fpimp(self, ffp):
         """Floodplain impervious fraction of the links for a new land-cover scene."""
         a = np.ascontiguousarray(ffp, np.float64)

@@ -740,12 +740,15 @@ static int ora_locate(const double *x, int n, double y)
     return ora_le(x[c], y) ? c + 1 : c;
 }
 
-double ora_update_param_case2(double celerity, const double *length, int nLinks, double *C1, double *C2)
+/* mrm_update_param, src/mRM/mo_mrm_mpr.f90:241-329: K = L11_length / celerity
+ * (case 2: one celerity; case 3: L11_celerity of each link) */
+double ora_update_param_links(const double *link_celerity, double celerity, const double *length, int nLinks,
+                              double *C1, double *C2)
 {
     const double xi = fabs(0.0); /* rout_space_weight */
     double kmin = HUGE_VAL;
     for (int i = 0; i < nLinks; ++i) {
-        double K = length[i] / celerity;
+        double K = length[i] / (link_celerity ? link_celerity[i] : celerity);
         if (K < kmin)
             kmin = K;
     }
@@ -754,11 +757,29 @@ double ora_update_param_case2(double celerity, const double *length, int nLinks,
         ind = 1;
     const double ts = GIVEN_TS[ind - 1];
     for (int i = 0; i < nLinks; ++i) {
-        double K = length[i] / celerity;
+        double K = length[i] / (link_celerity ? link_celerity[i] : celerity);
         C1[i] = ts / (K * (1.0 - xi) + 0.5 * ts);
         C2[i] = 1.0 - C1[i] * K / ts;
     }
     return ts;
+}
+
+double ora_update_param_case2(double celerity, const double *length, int nLinks, double *C1, double *C2)
+{
+    return ora_update_param_links(NULL, celerity, length, nLinks, C1, C2);
+}
+
+/* L11_calc_celerity, src/mRM/mo_mrm_net_startup.f90:2212-2423, for one link:
+ * the harmonic mean of slope_factor * sqrt(slope / 100) over the L0 cells of
+ * the link's river path, from its source cell to its outlet cell inclusive
+ * (slopes in percent, after the reference's lower bound of 0.1 and its
+ * outlier filter) */
+double ora_link_celerity(double slope_factor, const double *path_slope, int n)
+{
+    double s = 0.0;
+    for (int j = 0; j < n; ++j)
+        s = s + 1.0 / (slope_factor * sqrt(path_slope[j] / 100.0));
+    return (double)n / s;
 }
 
 /* ---- aggregated outputs ---- */
@@ -845,8 +866,9 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
      * tsRoutFactor = TSrout / (timestep * HourSecs) (src/mHM/mo_mhm_interface_run.f90:480-511) */
     double ts_factor = 1.0;
     int rout_loop = 1, win = 1;
-    if (d->proc_rout == 2 && L > 1) {
-        const double tsrout = ora_update_param_case2(d->rout_param[0], d->length, nLinks, s->C1, s->C2);
+    if (d->proc_rout >= 2 && L > 1) {
+        const double tsrout = ora_update_param_links(d->proc_rout == 3 ? d->link_celerity : NULL, d->rout_param[0],
+                                                     d->length, nLinks, s->C1, s->C2);
         ts_factor = tsrout / ((double)d->timestep * 3600.0);
         if (ts_factor < 1.0) {
             rout_loop = (int)lround(1.0 / ts_factor);
@@ -1055,7 +1077,7 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
                     q_gauge[(size_t)it * d->nGauges + g] = s->Qmod[d->gauge_node[g] - 1];
             if (qmod_out)
                 memcpy(qmod_out + (size_t)it * L, s->Qmod, sizeof(double) * (size_t)L);
-        } else if (d->proc_rout == 2) {
+        } else if (d->proc_rout >= 2) {
             int route_now = 1, ts_rout = d->timestep;
             const double *run = tro;
             if (win > 1) { /* accumulate until the routing step is complete (:489-511) */

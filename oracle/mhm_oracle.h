@@ -104,13 +104,16 @@ void ora_L11_routing_order(int nNodes, int nOutlets, const int32_t *fromN, const
  * celerity per link, the routing time step TSrout [s] = given_TS(locate(given_TS,
  * min K)), C1/C2 with xi = 0.  Returns TSrout. */
 double ora_update_param_case2(double celerity, const double *length, int nLinks, double *C1, double *C2);
+double ora_update_param_links(const double *link_celerity, double celerity, const double *length, int nLinks,
+                              double *C1, double *C2);
+double ora_link_celerity(double slope_factor, const double *path_slope, int n);
 
 /* ---- whole-domain run (the mhm_eval time loop for one domain) ---- */
 typedef struct {
     int32_t nCells, nH, nNodes, nOutlets, timestep;
     int32_t proc_sm;      /* processMatrix(3,1): 1..4 */
     int32_t proc_pet;     /* processMatrix(5,1): -1, 0, 1 */
-    int32_t proc_rout;    /* processMatrix(8,1): 0, 1 or 2 */
+    int32_t proc_rout;    /* processMatrix(8,1): 0, 1, 2 or 3 */
     int32_t nTstepForcingDay; /* 24 (hourly) or 1 (daily) */
     int32_t read_states;  /* 1: states (and C1/C2) come from a restart */
     int32_t jul_start;    /* simPer%julStart */
@@ -130,6 +133,7 @@ typedef struct {
     const double *rout_param;                 /* [5] (case 1) or [1] celerity [m s-1] (case 2) */
     const int32_t *gauge_node;                /* [nGauges] */
     const double *latitude;                   /* [nCells] degrees */
+    const double *link_celerity;              /* [nLinks] L11_celerity (routing case 3) */
 } ora_domain;
 
 typedef struct {

@@ -35,7 +35,7 @@ class OraDomain(C.Structure):
         ("fnight_pet", _dp), ("fday_temp", _dp), ("fnight_temp", _dp),
         ("l1_area_km2", _dp), ("l1_l11_id", _ip), ("l11_area_km2", _dp), ("l11_l1_id", _ip),
         ("net_perm", _ip), ("from_n", _ip), ("to_n", _ip), ("length", _dp), ("slope", _dp),
-        ("ffp_imp", _dp), ("rout_param", _dp), ("gauge_node", _ip), ("latitude", _dp),
+        ("ffp_imp", _dp), ("rout_param", _dp), ("gauge_node", _ip), ("latitude", _dp), ("link_celerity", _dp),
     ]
 
 
@@ -158,6 +158,10 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_L11_routing_order.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
     L.ora_update_param_case2.argtypes = [d, _dp, C.c_int, _dp, _dp]
     L.ora_update_param_case2.restype = d
+    L.ora_update_param_links.argtypes = [_dp, d, _dp, C.c_int, _dp, _dp]
+    L.ora_update_param_links.restype = d
+    L.ora_link_celerity.argtypes = [d, _dp, C.c_int]
+    L.ora_link_celerity.restype = d
     L.ora_run.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
                           C.POINTER(OraForcing), C.c_int32, C.c_int32, _dp, _dp, _dp, C.c_int]
     L.ora_run_ex.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
@@ -190,7 +194,7 @@ class OracleRun:
     """The mhm_eval time loop of one basin on the CPU (oracle)."""
 
     def __init__(self, dom, params: dict, rout_param=None, proc_sm=1, proc_pet=0, proc_rout=1,
-                 hourly=True, read_states=False, kind="hmath"):
+                 hourly=True, read_states=False, kind="hmath", link_celerity=None):
         self.L = load(kind)
         self.dom = dom
         self.keep = []
@@ -215,6 +219,8 @@ class OracleRun:
             setattr(d, n, _i(k(getattr(dom, n), np.int32)))
         rp = k(np.resize(np.asarray(rout_param if rout_param is not None else np.zeros(5), np.float64), 5))
         d.rout_param = _d(rp)
+        if link_celerity is not None:
+            d.link_celerity = _d(k(link_celerity))
         self.d = d
         p = OraParams()
         for name, arr in params.items():
