@@ -70,14 +70,16 @@ struct CellRegs {
     // states
     double interc, snow, seal, unsat, sat;
     // parameters (and parameter-only derived values)
-    double fsealed;
+    double fsealed, fnotsealed; // fnotsealed = 1 - fsealed (parameter only)
     double ddinc, ddmax_s, ddnopre_s, dd_thr;
     double tthresh, sthresh, uthresh, karst, alpha1;
     double k0s, k1s, k2s, kps; // c2TSTu / k
     double jarvis;
     double fasp, harsam, lat_rad;
 };
-enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_DEN, HS_SM, HS_PLANES };
+// (the stress denominators FC - PW / SMs - PW are recomputed per step: one
+// FP64 add, cheaper than the shared memory it would take from occupancy)
+enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, HS_PLANES };
 
 
 template <int H, int MINB, bool FLUX>
@@ -112,6 +114,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     CellRegs c;
     const double c2 = a.c2TSTu;
     c.fsealed = par(P_FSEALED);
+    c.fnotsealed = 1.0 - c.fsealed;
     c.ddinc = par(P_DDINC);
     c.ddmax_s = par(P_DDMAX) * c2;   // mo_mhm.f90:463
     c.ddnopre_s = par(P_DDNOPRE) * c2; // mo_mhm.f90:464
@@ -138,8 +141,6 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         hs(HS_FC, h) = fc;
         hs(HS_PW, h) = pw;
         hs(HS_BETA, h) = par(P_HORIZON + 4 * H + h);
-        // feddes denominator FC-PW (mo_soil_moisture.f90:358), jarvis SMs-PW (:435)
-        hs(HS_DEN, h) = feddes ? fc - pw : sms - pw;
         hs(HS_SM, h) = reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
     }
     c.interc = S[(size_t)S_INTERC * N];
@@ -231,49 +232,43 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         }
 
         // ---- canopy_interc, mo_canopy_interc.f90:75-133 ----
+        // Branches that only pick between values are written as hm_sel (an
+        // integer select of the bits): a double select or a merge of doubles
+        // after a short if/else is issued on the FP64 pipe, the bottleneck.
         double throughfall, aet_can;
         {
-            double aux = c.interc + prec;
-            if (hm_ge(aux, imax)) {
-                throughfall = aux - imax;
-                c.interc = imax;
-            } else {
-                throughfall = 0.0;
-                c.interc = aux;
-            }
-            aet_can = hm_gt(imax, kEps) ? pet * hm_pow(hm_div(c.interc, imax), kTwoThird) : 0.0;
+            const double aux = c.interc + prec;
+            const bool full = hm_ge(aux, imax);
+            throughfall = hm_sel(full, aux - imax, 0.0);
+            c.interc = hm_sel(full, imax, aux);
+            aet_can = 0.0;
+            if (hm_gt(imax, kEps)) aet_can = pet * hm_pow(hm_div(c.interc, imax), kTwoThird);
             // a negative storage gives pow() = NaN: these two tests keep IEEE NaN semantics
-            if (hm_lt_ieee(aet_can, 0.0)) aet_can = 0.0;
-            if (hm_gt_ieee(c.interc, aet_can)) {
-                c.interc = c.interc - aet_can;
-            } else {
-                aet_can = c.interc;
-                c.interc = 0.0;
-            }
+            aet_can = hm_sel(hm_lt_ieee(aet_can, 0.0), 0.0, aet_can);
+            const bool keep = hm_gt_ieee(c.interc, aet_can);
+            const double rest = c.interc - aet_can;
+            aet_can = hm_sel(keep, aet_can, c.interc);
+            c.interc = hm_sel(keep, rest, 0.0);
         }
         // ---- snow_accum_melt, mo_snow_accum_melt.f90:70-158 ----
         double prec_effect, melt;
         {
             const bool warm = hm_gt(temp, c.tthresh);
-            double rain = warm ? throughfall : 0.0;
-            double snowf = warm ? 0.0 : throughfall;
-            double dd = (dd_thr_ok && hm_le(prec, c.dd_thr)) ? c.ddnopre_s + c.ddinc * prec : c.ddmax_s;
+            const double rain = hm_sel(warm, throughfall, 0.0);
+            const double snowf = hm_sel(warm, 0.0, throughfall);
+            const bool low = dd_thr_ok && hm_le(prec, c.dd_thr);
+            const double dd = hm_sel(low, c.ddnopre_s + c.ddinc * prec, c.ddmax_s);
+            melt = 0.0;
             if (warm) {
+                double snow_left = 0.0;
                 if (hm_gt0(c.snow)) {
-                    double aux = dd * (temp - c.tthresh);
-                    if (hm_gt(aux, c.snow)) {
-                        melt = c.snow;
-                        c.snow = 0.0;
-                    } else {
-                        melt = aux;
-                        c.snow = c.snow - aux;
-                    }
-                } else {
-                    melt = 0.0;
-                    c.snow = 0.0;
+                    const double aux = dd * (temp - c.tthresh);
+                    const bool all = hm_gt(aux, c.snow);
+                    melt = hm_sel(all, c.snow, aux);
+                    snow_left = hm_sel(all, 0.0, c.snow - aux);
                 }
+                c.snow = snow_left;
             } else {
-                melt = 0.0;
                 c.snow = c.snow + snowf;
             }
             prec_effect = melt + rain;
@@ -284,28 +279,19 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         double aet_sealed_act = 0.0, aet_soil = 0.0; // for the optional flux outputs
         {
             if (sealed) {
-                double tmp = c.seal + prec_effect;
-                if (hm_gt(tmp, c.sthresh)) {
-                    runoff_sealed = tmp - c.sthresh;
-                    c.seal = c.sthresh;
-                } else {
-                    runoff_sealed = 0.0;
-                    c.seal = tmp;
-                }
-                double aet_sealed;
+                const double tmp = c.seal + prec_effect;
+                const bool over = hm_gt(tmp, c.sthresh);
+                runoff_sealed = hm_sel(over, tmp - c.sthresh, 0.0);
+                c.seal = hm_sel(over, c.sthresh, tmp);
+                double aet_sealed = DBL_MAX;
                 if (sthresh_pos) {
                     aet_sealed = (hm_div(pet, a.tab.evap[month - 1]) - aet_can) * hm_div(c.seal, c.sthresh);
-                    if (hm_lt0(aet_sealed)) aet_sealed = 0.0;
-                } else {
-                    aet_sealed = DBL_MAX;
+                    aet_sealed = hm_sel(hm_lt0(aet_sealed), 0.0, aet_sealed);
                 }
-                if (hm_gt(c.seal, aet_sealed)) {
-                    c.seal = c.seal - aet_sealed;
-                    if constexpr (FLUX) aet_sealed_act = aet_sealed;
-                } else {
-                    if constexpr (FLUX) aet_sealed_act = c.seal;
-                    c.seal = 0.0;
-                }
+                const bool keep = hm_gt(c.seal, aet_sealed);
+                const double rest = c.seal - aet_sealed;
+                if constexpr (FLUX) aet_sealed_act = hm_sel(keep, aet_sealed, c.seal);
+                c.seal = hm_sel(keep, rest, 0.0);
             }
             double infil = prec_effect; // prec_effec_soil of horizon 1
             double aet_above = 0.0;     // masked running sum of positive aet above
@@ -315,46 +301,41 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 const double pin = infil;
                 const double sms = hs(HS_SMS, h);
                 double smh = hs(HS_SM, h);
-                if (hm_gt(smh, sms)) {
-                    infil = pin;
-                } else {
-                    double frac_runoff = hm_gt(smh, kEps) ? hm_exp(hs(HS_BETA, h) * hm_log(hm_div(smh, sms))) : 0.0;
-                    double tmp = pin * (1.0 - frac_runoff);
-                    if (hm_gt(smh + tmp, sms)) {
-                        infil = pin + (smh - sms);
-                        smh = sms;
-                    } else {
-                        infil = pin - tmp;
-                        smh = smh + tmp;
-                    }
+                if (!hm_gt(smh, sms)) { // else the horizon passes its input on: infil stays pin
+                    double frac_runoff = 0.0;
+                    if (hm_gt(smh, kEps)) frac_runoff = hm_exp(hs(HS_BETA, h) * hm_log(hm_div(smh, sms)));
+                    const double tmp = pin * (1.0 - frac_runoff);
+                    const double filled = smh + tmp;
+                    const bool over = hm_gt(filled, sms);
+                    infil = hm_sel(over, pin + (smh - sms), pin - tmp);
+                    smh = hm_sel(over, sms, filled);
                 }
-                double aet = demand;
-                if (h != 0) aet = aet - aet_above;
-                double stress;
+                // demand minus the positive aet above (x - (+0) == x: no test for h == 0)
+                double aet = demand - aet_above;
                 const double froots = hs(HS_FROOTS, h), pw = hs(HS_PW, h);
+                double stress;
                 if (feddes) {
-                    if (hm_ge(smh, hs(HS_FC, h))) stress = froots;
-                    else if (hm_gt(smh, pw)) stress = hm_div(froots * (smh - pw), hs(HS_DEN, h));
-                    else stress = 0.0;
+                    const bool wet = hm_ge(smh, hs(HS_FC, h));
+                    stress = hm_sel(wet, froots, 0.0);
+                    // mo_soil_moisture.f90:358
+                    if (!wet && hm_gt(smh, pw)) stress = hm_div(froots * (smh - pw), hs(HS_FC, h) - pw);
                 } else {
-                    double th = hm_div(smh - pw, hs(HS_DEN, h));
-                    if (hm_lt0(th)) th = 0.0;
-                    if (hm_gt(th, 1.0)) th = 1.0;
-                    if (hm_ge(th, c.jarvis)) stress = froots;
-                    else if (hm_lt(th, c.jarvis)) stress = froots * hm_div(th, c.jarvis);
-                    else stress = 0.0;
+                    double th = hm_div(smh - pw, sms - pw); // mo_soil_moisture.f90:435
+                    th = hm_sel(hm_lt0(th), 0.0, th);
+                    th = hm_sel(hm_gt(th, 1.0), 1.0, th);
+                    const bool wet = hm_ge(th, c.jarvis);
+                    stress = hm_sel(wet, froots, 0.0);
+                    if (!wet && hm_lt(th, c.jarvis)) stress = froots * hm_div(th, c.jarvis);
                 }
                 aet = aet * stress;
-                if (hm_lt0(aet)) aet = 0.0;
-                if (hm_gt(smh, aet)) {
-                    smh = smh - aet;
-                } else {
-                    aet = smh - kEps;
-                    smh = kEps;
-                }
-                if (hm_lt(smh, kEps)) smh = kEps;
+                aet = hm_sel(hm_lt0(aet), 0.0, aet);
+                const bool enough = hm_gt(smh, aet);
+                const double left = smh - aet;
+                aet = hm_sel(enough, aet, smh - kEps);
+                smh = hm_sel(enough, left, kEps);
+                smh = hm_sel(hm_lt(smh, kEps), kEps, smh);
                 hs(HS_SM, h) = smh;
-                if (hm_gt0(aet)) aet_above = aet_above + aet;
+                aet_above = hm_sel(hm_gt0(aet), aet_above + aet, aet_above);
                 if constexpr (FLUX) {
                     aet_soil = aet_soil + aet;
                     if (oon) { // soil_infil_L<h>, aET_L<h> (mo_write_fluxes_states.f90:414-426)
@@ -369,45 +350,34 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         double fast = 0.0, slow = 0.0, base, perc;
         {
             c.unsat = c.unsat + infil_last;
-            if (hm_gt(c.unsat, c.uthresh)) {
-                double x = c.k0s * (c.unsat - c.uthresh);
-                double y = c.unsat - kEps;
-                fast = hm_lt(x, y) ? x : y;
-            }
-            c.unsat = c.unsat - fast;
-            if (hm_gt(c.unsat, kEps)) {
-                double x = c.k1s * hm_pow(c.unsat, c.alpha1);
-                double y = c.unsat - kEps;
-                slow = hm_lt(x, y) ? x : y;
-            }
+            if (hm_gt(c.unsat, c.uthresh)) fast = hm_min_sel(c.k0s * (c.unsat - c.uthresh), c.unsat - kEps);
+            c.unsat = c.unsat - fast; // - (+0) keeps the value when nothing flows
+            if (hm_gt(c.unsat, kEps)) slow = hm_min_sel(c.k1s * hm_pow(c.unsat, c.alpha1), c.unsat - kEps);
             c.unsat = c.unsat - slow;
             perc = c.kps * c.unsat;
-            if (hm_gt(c.unsat, perc)) {
-                c.unsat = c.unsat - perc;
-                c.sat = c.sat + perc * c.karst;
-            } else {
-                perc = c.unsat;
-                c.sat = c.sat + c.unsat * c.karst;
-                c.unsat = 0.0;
-            }
+            // if the store cannot supply kp * unsat, perc = unsat: both branches of
+            // the reference add perc * karstLoss to the saturated store
+            const bool rest = hm_gt(c.unsat, perc);
+            perc = hm_sel(rest, perc, c.unsat);
+            c.sat = c.sat + perc * c.karst;
+            c.unsat = hm_sel(rest, c.unsat - perc, 0.0);
             if constexpr (FLUX) {
                 if (a.flux_aet) {
                     const size_t fo = (size_t)t * out_stride + (size_t)m * N + k;
-                    a.flux_aet[fo] = aet_can + c.fsealed * aet_sealed_act + (1.0 - c.fsealed) * aet_soil;
-                    a.flux_loss[fo] = (1.0 - c.fsealed) * (perc - perc * c.karst);
+                    a.flux_aet[fo] = aet_can + c.fsealed * aet_sealed_act + c.fnotsealed * aet_soil;
+                    a.flux_loss[fo] = c.fnotsealed * (perc - perc * c.karst);
                 }
             }
         }
         // ---- runoff_sat_zone, mo_runoff.f90:191-212 ----
-        if (hm_gt0(c.sat)) {
-            base = c.k2s * c.sat;
-            c.sat = c.sat - base;
-        } else {
-            base = 0.0;
-            c.sat = 0.0;
+        {
+            const bool pos = hm_gt0(c.sat);
+            const double b0 = c.k2s * c.sat;
+            base = hm_sel(pos, b0, 0.0);
+            c.sat = hm_sel(pos, c.sat - b0, 0.0);
         }
         // ---- L1_total_runoff, mo_runoff.f90:248-274 ----
-        const double q_total = ((base + slow + fast) * (1.0 - c.fsealed)) + (runoff_sealed * c.fsealed);
+        const double q_total = ((base + slow + fast) * c.fnotsealed) + (runoff_sealed * c.fsealed);
         tro[(size_t)t * out_stride] = q_total;
         if constexpr (FLUX) {
             // mHM_updateDataset, src/mHM/mo_write_fluxes_states.f90:283-438

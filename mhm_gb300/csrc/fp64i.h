@@ -3,7 +3,8 @@
  *
  * GB300's FP64 pipe issues ~0.5 T thread-ops/s, and a double compare (DSETP)
  * or the refinement steps of a double division occupy it like an FMA; the
- * integer pipes are tens of times faster.  These functions return exactly
+ * integer pipes are tens of times faster.  Sign masks on a double's bits go
+ * through hm_abs_bits, or the compiler turns them back into FP64 |x|.  These functions return exactly
  * what the IEEE operations return (round-to-nearest-even), so kernels that
  * use them stay bit-identical to host code using plain C operators.
  *
@@ -20,14 +21,16 @@
 
 #include "hmath.h"
 
-/* order key: monotone in the value for non-NaN doubles, +0 and -0 -> 0 */
+/* order key: monotone in the value for non-NaN doubles, +0 and -0 -> 0
+ * (the sign-cleared bits through hm_abs_bits, which stays on the integer
+ * pipe) */
 HM_FN int64_t hm_okey(double x)
 {
-    const int64_t b = (int64_t)hm_d2b(x);
-    const int64_t m = b & 0x7fffffffffffffffLL;
-    return b < 0 ? -m : m;
+    const uint64_t u = hm_d2b(x);
+    const int64_t m = (int64_t)hm_abs_bits(u);
+    return (int64_t)u < 0 ? -m : m;
 }
-HM_FN int hm_isnan_i(double x) { return (hm_d2b(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
+HM_FN int hm_isnan_i(double x) { return hm_abs_bits(hm_d2b(x)) > 0x7ff0000000000000ULL; }
 HM_FN int hm_gt(double a, double b) { return hm_okey(a) > hm_okey(b); }
 HM_FN int hm_ge(double a, double b) { return hm_okey(a) >= hm_okey(b); }
 HM_FN int hm_lt(double a, double b) { return hm_okey(a) < hm_okey(b); }
@@ -37,8 +40,11 @@ HM_FN int hm_lt_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(
 /* x > 0, x < 0 against the constant zero */
 HM_FN int hm_gt0(double x) { return hm_okey(x) > 0; }
 HM_FN int hm_lt0(double x) { return hm_okey(x) < 0; }
+/* c ? a : b as a select of the bit patterns: a select of doubles is issued
+ * as an FP64-pipe move on this GPU (measured), an integer select is not */
+HM_FN double hm_sel(int c, double a, double b) { return hm_b2d(c ? hm_d2b(a) : hm_d2b(b)); }
 /* min/max with the selection rules of the reference's (a < b ? a : b) */
-HM_FN double hm_min_sel(double a, double b) { return hm_lt(a, b) ? a : b; }
+HM_FN double hm_min_sel(double a, double b) { return hm_sel(hm_lt(a, b), a, b); }
 
 /* reciprocal seed 1/x in float, correctly rounded on host and device */
 HM_FN float hm_frcp(float x)
@@ -67,9 +73,9 @@ HM_FN_BIG double hm_div(double a, double b)
     const uint64_t ua = hm_d2b(a), ub = hm_d2b(b);
     const uint32_t eaf = (uint32_t)(ua >> 52) & 0x7ffu, ebf = (uint32_t)(ub >> 52) & 0x7ffu;
     const uint64_t sign = (ua ^ ub) & 0x8000000000000000ULL;
-    if (ebf - 1u >= 0x7feu || (eaf - 1u >= 0x7feu && (ua << 1) != 0))
+    if (ebf - 1u >= 0x7feu || (eaf - 1u >= 0x7feu && hm_abs_bits(ua) != 0))
         return a / b; /* b zero/subnormal/inf/NaN, or a subnormal/inf/NaN */
-    if ((ua << 1) == 0)
+    if (hm_abs_bits(ua) == 0)
         return hm_b2d(sign); /* +-0 / normal */
     uint64_t Ma = (ua & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
     const uint64_t Mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;

@@ -73,6 +73,22 @@ HM_FN uint64_t hm_d2b(double d)
 #endif
 }
 
+/* The bits of |x| (sign bit cleared), as an integer.  On the device the mask
+ * is inline PTX: written in C, the compiler recognises "bits of a double AND
+ * 0x7fff..." as an FP64 absolute value and issues it on the FP64 pipe, which
+ * on this GPU is the scarce one (measured: one extra FP64 instruction per
+ * masked operand). */
+HM_FN uint64_t hm_abs_bits(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    uint64_t r;
+    asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(u));
+    return r;
+#else
+    return u & 0x7fffffffffffffffULL;
+#endif
+}
+
 /* Default tables.  Host code reads static arrays; device code reads the
  * __device__ copies unless a kernel passes its own (e.g. shared-memory) copy. */
 static const uint64_t hm_log_tab_h[3 * HM_LOG_N] = HM_LOG_TABLE_INIT;
@@ -99,7 +115,7 @@ HM_FN void hm_log_dd_t(double x, const uint64_t *ltab, double *hi_out, double *l
     int64_t kadj = 0;
     if (top - 0x00100000u >= 0x7ff00000u - 0x00100000u) {
         /* zero, subnormal, negative, inf or NaN */
-        if ((u << 1) == 0) {               /* +-0 */
+        if (hm_abs_bits(u) == 0) {               /* +-0 */
             *hi_out = -HUGE_VAL;
             *lo_out = 0.0;
             return;
@@ -393,7 +409,7 @@ HM_FN_BIG double hm_log_i(double x)
     if (top >= 0x7ff00000u) { /* +inf, NaN, or negative (sign bit set) */
         if (u == 0x7ff0000000000000ULL)
             return x;
-        if ((u << 1) == 0)
+        if (hm_abs_bits(u) == 0)
             return -HUGE_VAL; /* -0 */
         return hm_b2d(0x7ff8000000000000ULL);
     }
@@ -440,7 +456,7 @@ HM_FN_BIG double hm_exp_q64(hm_i128 X)
 HM_FN double hm_exp_i(double x)
 {
     const uint64_t u = hm_d2b(x);
-    const uint64_t a = u & 0x7fffffffffffffffULL;
+    const uint64_t a = hm_abs_bits(u);
     if (a >= 0x4087500000000000ULL) { /* |x| >= 746, inf or NaN */
         if (a > 0x7ff0000000000000ULL)
             return x;
@@ -462,7 +478,7 @@ HM_FN_BIG double hm_pow_i(double x, double y)
 {
     const uint64_t u = hm_d2b(x);
     const uint64_t uy = hm_d2b(y);
-    const uint64_t ay = uy & 0x7fffffffffffffffULL;
+    const uint64_t ay = hm_abs_bits(uy);
     if (ay == 0 || u == 0x3ff0000000000000ULL)
         return 1.0;
     const int ey = (int)(ay >> 52) - 1023;
@@ -602,7 +618,7 @@ HM_FN_BIG double hm_log_i2(double x)
     if (top >= 0x7ff00000u) {
         if (u == 0x7ff0000000000000ULL)
             return x;
-        if ((u << 1) == 0)
+        if (hm_abs_bits(u) == 0)
             return -HUGE_VAL;
         return hm_b2d(0x7ff8000000000000ULL);
     }
@@ -653,7 +669,7 @@ HM_FN_BIG double hm_exp_q64_2(int64_t Xhi, uint64_t Xlo)
 HM_FN double hm_exp_i2(double x)
 {
     const uint64_t u = hm_d2b(x);
-    const uint64_t a = u & 0x7fffffffffffffffULL;
+    const uint64_t a = hm_abs_bits(u);
     if (a >= 0x4087500000000000ULL) {
         if (a > 0x7ff0000000000000ULL)
             return x;
@@ -681,7 +697,7 @@ HM_FN_BIG double hm_pow_i2(double x, double y)
 {
     const uint64_t u = hm_d2b(x);
     const uint64_t uy = hm_d2b(y);
-    const uint64_t ay = uy & 0x7fffffffffffffffULL;
+    const uint64_t ay = hm_abs_bits(uy);
     if (ay == 0 || u == 0x3ff0000000000000ULL)
         return 1.0;
     const int ey = (int)(ay >> 52) - 1023;
