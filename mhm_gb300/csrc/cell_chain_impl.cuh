@@ -76,10 +76,16 @@ struct CellRegs {
     double k0s, k1s, k2s, kps; // c2TSTu / k
     double jarvis;
     double fasp, harsam, lat_rad;
+    uint64_t r_sthresh, r_jarvis; // reciprocals of the chunk-fixed divisors
 };
-// (the stress denominators FC - PW / SMs - PW are recomputed per step: one
-// FP64 add, cheaper than the shared memory it would take from occupancy)
-enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, HS_PLANES };
+// Every division of the step divides by a value that is fixed over the chunk
+// (SMs, the stress denominator FC - PW or SMs - PW, sealedThresh, the Jarvis
+// threshold) or over a month (interception capacity, pan-evaporation
+// coefficient): their fixed-point reciprocals (hm_recip_of) are computed once
+// and each division runs hm_div_r -- the same correctly rounded quotient as
+// hm_div at about half its integer instructions.  HS_RSMS / HS_RDEN hold the
+// reciprocals' bits.
+enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, HS_RSMS, HS_RDEN, HS_PLANES };
 
 
 template <int H, int MINB, bool FLUX>
@@ -132,6 +138,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     c.fasp = par(P_FASP);
     c.harsam = par(P_HARSAM);
     c.lat_rad = (a.proc_pet == 1) ? kDeg2Rad * __ldg(a.latitude + k) : 0.0;
+    c.r_sthresh = hm_recip_of(c.sthresh);
+    c.r_jarvis = hm_recip_of(c.jarvis);
 #pragma unroll 1
     for (int h = 0; h < H; ++h) {
         const double fr = par(P_HORIZON + h), sms = par(P_HORIZON + H + h), fc = par(P_HORIZON + 2 * H + h);
@@ -141,6 +149,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         hs(HS_FC, h) = fc;
         hs(HS_PW, h) = pw;
         hs(HS_BETA, h) = par(P_HORIZON + 4 * H + h);
+        hs(HS_RSMS, h) = hm_b2d(hm_recip_of(sms));
+        hs(HS_RDEN, h) = hm_b2d(hm_recip_of(feddes ? fc - pw : sms - pw)); // mo_soil_moisture.f90:358, :435
         hs(HS_SM, h) = reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
     }
     c.interc = S[(size_t)S_INTERC * N];
@@ -153,7 +163,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
     const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
     int cur_month = -1;
-    double imax = 0.0, petlai = 0.0;
+    double imax = 0.0, petlai = 0.0, evap = 0.0;
+    uint64_t r_imax = 0, r_evap = 0;
     int cur_doy = -1;
     double rad = 0.0;
     const size_t out_stride = (size_t)a.n_members * N;
@@ -183,6 +194,9 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         if (month != cur_month) { // iLAI = month (LUT-based LAI)
             cur_month = month;
             imax = par(P_MAXINTER + month - 1);
+            r_imax = hm_recip_of(imax);
+            evap = a.tab.evap[month - 1];
+            r_evap = hm_recip_of(evap);
             if (a.proc_pet == -1) petlai = par(P_PETLAI + month - 1);
         }
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
@@ -242,7 +256,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             throughfall = hm_sel(full, aux - imax, 0.0);
             c.interc = hm_sel(full, imax, aux);
             aet_can = 0.0;
-            if (hm_gt(imax, kEps)) aet_can = pet * hm_pow(hm_div(c.interc, imax), kTwoThird);
+            if (hm_gt(imax, kEps)) aet_can = pet * hm_pow(hm_div_r(c.interc, imax, r_imax), kTwoThird);
             // a negative storage gives pow() = NaN: these two tests keep IEEE NaN semantics
             aet_can = hm_sel(hm_lt_ieee(aet_can, 0.0), 0.0, aet_can);
             const bool keep = hm_gt_ieee(c.interc, aet_can);
@@ -285,7 +299,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 c.seal = hm_sel(over, c.sthresh, tmp);
                 double aet_sealed = DBL_MAX;
                 if (sthresh_pos) {
-                    aet_sealed = (hm_div(pet, a.tab.evap[month - 1]) - aet_can) * hm_div(c.seal, c.sthresh);
+                    aet_sealed = (hm_div_r(pet, evap, r_evap) - aet_can) * hm_div_r(c.seal, c.sthresh, c.r_sthresh);
                     aet_sealed = hm_sel(hm_lt0(aet_sealed), 0.0, aet_sealed);
                 }
                 const bool keep = hm_gt(c.seal, aet_sealed);
@@ -303,7 +317,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                 double smh = hs(HS_SM, h);
                 if (!hm_gt(smh, sms)) { // else the horizon passes its input on: infil stays pin
                     double frac_runoff = 0.0;
-                    if (hm_gt(smh, kEps)) frac_runoff = hm_exp(hs(HS_BETA, h) * hm_log(hm_div(smh, sms)));
+                    if (hm_gt(smh, kEps))
+                        frac_runoff = hm_exp(hs(HS_BETA, h) * hm_log(hm_div_r(smh, sms, hm_d2b(hs(HS_RSMS, h)))));
                     const double tmp = pin * (1.0 - frac_runoff);
                     const double filled = smh + tmp;
                     const bool over = hm_gt(filled, sms);
@@ -318,14 +333,15 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                     const bool wet = hm_ge(smh, hs(HS_FC, h));
                     stress = hm_sel(wet, froots, 0.0);
                     // mo_soil_moisture.f90:358
-                    if (!wet && hm_gt(smh, pw)) stress = hm_div(froots * (smh - pw), hs(HS_FC, h) - pw);
+                    if (!wet && hm_gt(smh, pw))
+                        stress = hm_div_r(froots * (smh - pw), hs(HS_FC, h) - pw, hm_d2b(hs(HS_RDEN, h)));
                 } else {
-                    double th = hm_div(smh - pw, sms - pw); // mo_soil_moisture.f90:435
+                    double th = hm_div_r(smh - pw, sms - pw, hm_d2b(hs(HS_RDEN, h)));
                     th = hm_sel(hm_lt0(th), 0.0, th);
                     th = hm_sel(hm_gt(th, 1.0), 1.0, th);
                     const bool wet = hm_ge(th, c.jarvis);
                     stress = hm_sel(wet, froots, 0.0);
-                    if (!wet && hm_lt(th, c.jarvis)) stress = froots * hm_div(th, c.jarvis);
+                    if (!wet && hm_lt(th, c.jarvis)) stress = froots * hm_div_r(th, c.jarvis, c.r_jarvis);
                 }
                 aet = aet * stress;
                 aet = hm_sel(hm_lt0(aet), 0.0, aet);

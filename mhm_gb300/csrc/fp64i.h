@@ -14,7 +14,8 @@
  * normal result take the integer path (float reciprocal seed, two Newton
  * steps in 64-bit fixed point, exact remainder correction, RNE); everything
  * else (subnormal, infinite, NaN, zero divisor, out-of-range results) uses
- * the native division.
+ * the native division.  hm_div_r(a, b, hm_recip_of(b)) is the same division
+ * with the divisor's reciprocal computed beforehand.
  */
 #ifndef MHM_FP64I_H
 #define MHM_FP64I_H
@@ -67,8 +68,43 @@ HM_FN uint32_t hm_f2b(float f)
 #endif
 }
 
-/* a / b, correctly rounded */
-HM_FN_BIG double hm_div(double a, double b)
+/* 64-bit fixed-point reciprocal of a divisor mantissa Mb in (2^52, 2^53):
+ * inv ~ 2^116 / Mb < 2^64 from a float seed (~24 bits) and two Newton steps
+ * y' = y (2 - Mb y / 2^116), which approach from below.  Depends on the
+ * divisor only, so a divisor that stays fixed over many divisions (a cell's
+ * soil parameters over a chunk of steps) needs it once: hm_recip_of. */
+HM_FN uint64_t hm_recip_mant(uint64_t Mb)
+{
+    const float fy = hm_frcp((float)(uint32_t)(Mb >> 29)); /* in (2^-24, 2^-23] */
+    const uint32_t fb = hm_f2b(fy);
+    const int sh = (int)((fb >> 23) & 0xffu) - 127 - 23 + 116 - 29; /* 40 or 41 */
+    const uint64_t fm = (uint64_t)((fb & 0x7fffffu) | 0x800000u);
+    uint64_t inv = (sh >= 41 && fm == 0x800000u) ? 0xffffffffffffffffULL : fm << sh;
+    for (int it = 0; it < 2; ++it) {
+        /* err = (2^116 - Mb*inv) >> 52, |err| < 2^42: bits 52..115 of the
+         * 128-bit difference, from its two limbs */
+        const uint64_t t_lo = Mb * inv, t_hi = hm_umulhi(Mb, inv);
+        const uint64_t e_lo = (uint64_t)0 - t_lo;
+        const uint64_t e_hi = ((uint64_t)1 << 52) - t_hi - (t_lo != 0);
+        const int64_t err_s = (int64_t)((e_hi << 12) | (e_lo >> 52));
+        inv = inv + (uint64_t)(hm_smulhi((int64_t)(inv >> 1), err_s) * 2);
+    }
+    return inv;
+}
+
+/* The reciprocal hm_div_r wants for divisor b (0 when b takes another path:
+ * zero, subnormal, infinite, NaN or a power of two). */
+HM_FN uint64_t hm_recip_of(double b)
+{
+    const uint64_t ub = hm_d2b(b);
+    const uint32_t ebf = (uint32_t)(ub >> 52) & 0x7ffu;
+    const uint64_t Mb = (ub & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    if (ebf - 1u >= 0x7feu || Mb == 0x0010000000000000ULL) return 0;
+    return hm_recip_mant(Mb);
+}
+
+/* a / b, correctly rounded, given inv = hm_recip_of(b) */
+HM_FN_BIG double hm_div_r(double a, double b, uint64_t inv)
 {
     const uint64_t ua = hm_d2b(a), ub = hm_d2b(b);
     const uint32_t eaf = (uint32_t)(ua >> 52) & 0x7ffu, ebf = (uint32_t)(ub >> 52) & 0x7ffu;
@@ -92,22 +128,6 @@ HM_FN_BIG double hm_div(double a, double b)
         Q = Ma << 2;
         R = 0;
     } else {
-        /* inv ~ 2^116 / Mb < 2^64: float seed (~24 bits), then two Newton
-         * steps y' = y (2 - Mb y / 2^116), which approach from below */
-        const float fy = hm_frcp((float)(uint32_t)(Mb >> 29)); /* in (2^-24, 2^-23] */
-        const uint32_t fb = hm_f2b(fy);
-        const int sh = (int)((fb >> 23) & 0xffu) - 127 - 23 + 116 - 29; /* 40 or 41 */
-        const uint64_t fm = (uint64_t)((fb & 0x7fffffu) | 0x800000u);
-        uint64_t inv = (sh >= 41 && fm == 0x800000u) ? 0xffffffffffffffffULL : fm << sh;
-        for (int it = 0; it < 2; ++it) {
-            /* err = (2^116 - Mb*inv) >> 52, |err| < 2^42: bits 52..115 of the
-             * 128-bit difference, from its two limbs */
-            const uint64_t t_lo = Mb * inv, t_hi = hm_umulhi(Mb, inv);
-            const uint64_t e_lo = (uint64_t)0 - t_lo;
-            const uint64_t e_hi = ((uint64_t)1 << 52) - t_hi - (t_lo != 0);
-            const int64_t err_s = (int64_t)((e_hi << 12) | (e_lo >> 52));
-            inv = inv + (uint64_t)(hm_smulhi((int64_t)(inv >> 1), err_s) * 2);
-        }
         /* Q ~ floor(Ma * 2^54 / Mb) in [2^54, 2^55) */
         Q = (hm_umulhi(Ma, inv) << 2) | ((Ma * inv) >> 62);
         /* exact remainder Ma*2^54 - Q*Mb; |R| < 2^57, so modulo 2^64 suffices */
@@ -132,5 +152,8 @@ HM_FN_BIG double hm_div(double a, double b)
     /* m53 in [2^52, 2^53]; a carry to 2^53 moves into the exponent field */
     return hm_b2d(sign | (((uint64_t)(e + 1022) << 52) + m53));
 }
+
+/* a / b, correctly rounded */
+HM_FN_BIG double hm_div(double a, double b) { return hm_div_r(a, b, hm_recip_of(b)); }
 
 #endif /* MHM_FP64I_H */
