@@ -87,6 +87,25 @@ struct OutSet {
     DevBuf<double> acc, out;
 };
 
+// The routing wavefront of one chunk (D + n_sub - 1 launches of
+// route_tick_kernel) captured once as a CUDA graph per argument set and
+// replayed for every chunk of that shape: the tick launches differ only in
+// tick / position range, which depend on the network and the chunk length.
+struct RouteGraph {
+    RouteArgs key{};
+    int32_t n_ticks = 0;
+    cudaGraphExec_t exec = nullptr;
+};
+
+bool same_route_shape(const RouteArgs &a, const RouteArgs &b)
+{
+    return a.n_nodes == b.n_nodes && a.n_members == b.n_members && a.n_steps == b.n_steps && a.sub == b.sub &&
+           a.rdiv == b.rdiv && a.n_qsteps == b.n_qsteps && a.pos_level == b.pos_level && a.up_ptr == b.up_ptr &&
+           a.up_pos == b.up_pos && a.pos_flags == b.pos_flags && a.C1 == b.C1 && a.C2 == b.C2 && a.qout == b.qout &&
+           a.qtr == b.qtr && a.qmod == b.qmod && a.qtin1 == b.qtin1 && a.qtr1 == b.qtr1 &&
+           a.member_step0 == b.member_step0;
+}
+
 struct ForcingSrc {
     const double *ptr = nullptr;
     int32_t row0 = 0, n_rows = 0, on_device = 0;
@@ -155,6 +174,8 @@ struct mhm_ctx {
     double t_ms[4] = {0, 0, 0, 0};
     size_t chunk_bytes = (size_t)8 << 30;
     int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
+    bool route_graphs_on = true;
+    std::vector<RouteGraph> route_graphs; // most recently used last
     int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
     // routing case 2: per-member routing time step [s] and the link lengths
     std::vector<double> ts_rout, length_h;
@@ -628,6 +649,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         int v = std::atoi(s);
         if (v == 4 || v == 6 || v == 8) ctx->cell_occ = v;
     }
+    if (const char *s = std::getenv("MHM_ROUTE_GRAPH")) ctx->route_graphs_on = std::atoi(s) != 0;
     *out = ctx;
     return MHM_OK;
 }
@@ -653,6 +675,8 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
     for (cudaEvent_t e : ctx->ev_members_done)
         if (e) cudaEventDestroy(e);
     if (ctx->run_a) cudaEventDestroy(ctx->run_a);
+    for (auto &rg : ctx->route_graphs)
+        if (rg.exec) cudaGraphExecDestroy(rg.exec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->route_stream) cudaStreamDestroy(ctx->route_stream);
@@ -1185,14 +1209,52 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             // wavefront: tick k advances sub-chunk k - l of level l
             const int D = ctx->net.n_levels;
             const int n_sub = (n_rsteps + r.sub - 1) / r.sub;
-            for (int k = 0; k < D + n_sub - 1; ++k) {
-                const int lo = std::max(0, k - n_sub + 1), hi = std::min(k, D - 1);
-                r.tick = k;
-                r.pos_begin = ctx->net.level_ptr[lo];
-                r.pos_end = ctx->net.level_ptr[hi + 1];
-                CK(launch_route_tick(r, rs), "route launch");
-                g_launches++;
+            const int n_ticks = D + n_sub - 1;
+            auto enqueue_ticks = [&]() -> int {
+                for (int k = 0; k < n_ticks; ++k) {
+                    const int lo = std::max(0, k - n_sub + 1), hi = std::min(k, D - 1);
+                    r.tick = k;
+                    r.pos_begin = ctx->net.level_ptr[lo];
+                    r.pos_end = ctx->net.level_ptr[hi + 1];
+                    CK(launch_route_tick(r, rs), "route launch");
+                }
+                return MHM_OK;
+            };
+            if (ctx->route_graphs_on) {
+                auto &cache = ctx->route_graphs;
+                auto it = std::find_if(cache.begin(), cache.end(),
+                                       [&](const RouteGraph &g) { return same_route_shape(g.key, r); });
+                if (it == cache.end()) {
+                    RouteGraph rg;
+                    rg.key = r;
+                    rg.n_ticks = n_ticks;
+                    cudaGraph_t graph = nullptr;
+                    CK(cudaStreamBeginCapture(rs, cudaStreamCaptureModeThreadLocal), "route capture");
+                    const int rc_cap = enqueue_ticks();
+                    const cudaError_t e_end = cudaStreamEndCapture(rs, &graph);
+                    if (rc_cap) {
+                        if (graph) cudaGraphDestroy(graph);
+                        return rc_cap;
+                    }
+                    CK(e_end, "route capture end");
+                    const cudaError_t e_inst = cudaGraphInstantiate(&rg.exec, graph, 0);
+                    cudaGraphDestroy(graph);
+                    CK(e_inst, "route graph instantiate");
+                    if (cache.size() >= 8) { // keep the most recently used shapes
+                        cudaGraphExecDestroy(cache.front().exec);
+                        cache.erase(cache.begin());
+                    }
+                    cache.push_back(rg);
+                    it = cache.end() - 1;
+                } else if (it != cache.end() - 1) {
+                    std::rotate(it, it + 1, cache.end());
+                    it = cache.end() - 1;
+                }
+                CK(cudaGraphLaunch(it->exec, rs), "route graph launch");
+            } else if (int rc = enqueue_ticks()) {
+                return rc;
             }
+            g_launches += n_ticks;
             if (R > 1 || F > 1) {
                 QmodStepArgs qs{};
                 qs.n_members = ctx->M;
