@@ -54,6 +54,19 @@ def _env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_throughput(local_ms: float, units_per_rank: float, world: int, device=None) -> tuple[float, float]:
+    """(job ms, whole-job units/s) of `world` independent replicas: the
+    slowest rank's time (all-reduce MAX over the process group when
+    world > 1) against the units of all ranks."""
+    ms = float(local_ms)
+    if world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, units_per_rank * world / (ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
 
@@ -247,12 +260,7 @@ def run_gpu(args) -> dict:
     n_acc, t_acc = g.get_timing(1)
     n_rt, t_rt = g.get_timing(2)
     g.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    units = float(N) * chunk * args.steps * world
-    value = units / (ms * 1e-3)
+    ms, value = replica_throughput(ms, float(N) * chunk * args.steps, world, device)
 
     # ---- e2e: host forcing (pinned), H2D + compute + D2H of the gauge series per step ----
     host = [torch.empty((chunk, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
@@ -277,11 +285,7 @@ def run_gpu(args) -> dict:
     e2e_ms = e0.elapsed_time(e1)
     wall_ms = (time.perf_counter() - t0) * 1e3
     e2e_ms = max(e2e_ms, wall_ms)  # host copies happen inside mhm_run; count whichever is longer
-    if world > 1:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = float(N) * chunk * e2e_steps * world / (e2e_ms * 1e-3)
+    e2e_ms, e2e_value = replica_throughput(e2e_ms, float(N) * chunk * e2e_steps, world, device)
 
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
