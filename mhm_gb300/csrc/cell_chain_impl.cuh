@@ -336,12 +336,14 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
                     if (!wet && hm_gt(smh, pw))
                         stress = hm_div_r(froots * (smh - pw), hs(HS_FC, h) - pw, hm_d2b(hs(HS_RDEN, h)));
                 } else {
+                    // with SMs == PW the quotient can be NaN (0 / 0): IEEE
+                    // comparisons then leave the stress at 0 as the oracle does
                     double th = hm_div_r(smh - pw, sms - pw, hm_d2b(hs(HS_RDEN, h)));
-                    th = hm_sel(hm_lt0(th), 0.0, th);
-                    th = hm_sel(hm_gt(th, 1.0), 1.0, th);
-                    const bool wet = hm_ge(th, c.jarvis);
+                    th = hm_sel(hm_lt_ieee(th, 0.0), 0.0, th);
+                    th = hm_sel(hm_gt_ieee(th, 1.0), 1.0, th);
+                    const bool wet = hm_ge_ieee(th, c.jarvis);
                     stress = hm_sel(wet, froots, 0.0);
-                    if (!wet && hm_lt(th, c.jarvis)) stress = froots * hm_div_r(th, c.jarvis, c.r_jarvis);
+                    if (!wet && hm_lt_ieee(th, c.jarvis)) stress = froots * hm_div_r(th, c.jarvis, c.r_jarvis);
                 }
                 aet = aet * stress;
                 aet = hm_sel(hm_lt0(aet), 0.0, aet);

@@ -38,6 +38,7 @@ HM_FN int hm_lt(double a, double b) { return hm_okey(a) < hm_okey(b); }
 HM_FN int hm_le(double a, double b) { return hm_okey(a) <= hm_okey(b); }
 HM_FN int hm_gt_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(b) && hm_gt(a, b); }
 HM_FN int hm_lt_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(b) && hm_lt(a, b); }
+HM_FN int hm_ge_ieee(double a, double b) { return !hm_isnan_i(a) && !hm_isnan_i(b) && hm_ge(a, b); }
 /* x > 0, x < 0 against the constant zero */
 HM_FN int hm_gt0(double x) { return hm_okey(x) > 0; }
 HM_FN int hm_lt0(double x) { return hm_okey(x) < 0; }

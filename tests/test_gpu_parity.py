@@ -215,3 +215,36 @@ def test_device_forcing(small):
     b.set_meteo(1, dev["pre"], dev["temp"], dev["pet"], on_device=True)
     qb = b.run(1, n)
     assert bitwise(qa, qb)
+
+
+@pytest.mark.parametrize("proc_sm", [1, 3])
+def test_degenerate_parameters_bitwise(proc_sm):
+    """Parameters at the edges the branches and divisions must handle like the
+    reference: no / full sealing, zero sealed storage capacity (the huge()
+    evaporation path), zero interception capacity in some months, field
+    capacity or saturation equal to the wilting point (a zero stress
+    denominator: IEEE division by zero), karstic gain (karstLoss > 1) and a
+    zero Jarvis threshold."""
+    dom = synth.make_domain(16, 20, 3, 4, seed=31)
+    N, H = dom.n_cells, dom.n_horizons
+    p = {k: np.array(v, np.float64, copy=True) for k, v in synth.make_eff_params(dom, seed=32).items()
+         if v is not None}
+    rng = np.random.default_rng(33)
+    pick = lambda frac: rng.random(N) < frac   # noqa: E731
+    p["fSealed"][pick(0.2)] = 0.0
+    p["fSealed"][pick(0.1)] = 1.0
+    p["sealedThresh"][pick(0.3)] = 0.0
+    mi = p["maxInter"].reshape(12, N)
+    mi[:, pick(0.2)] = 0.0
+    for name in ("soilMoistFC", "soilMoistSat"):
+        a = p[name].reshape(H, N)
+        sel = pick(0.15)
+        a[1, sel] = p["wiltingPoint"].reshape(H, N)[1, sel]
+    p["karstLoss"][pick(0.2)] = 1.05
+    if "jarvis_thresh_c1" in p:
+        p["jarvis_thresh_c1"][pick(0.3)] = 0.0
+    else:
+        p["jarvis_thresh_c1"] = np.where(pick(0.3), 0.0, 0.5)
+    f = synth.make_forcing(dom, 24 * 20, seed=34, gamma_theta=4.0)
+    gpu, ora = run_pair(dom, p, f, 24 * 20, proc_sm=proc_sm)
+    _assert_all_bitwise(gpu, ora)
