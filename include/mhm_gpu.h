@@ -307,6 +307,21 @@ int mhm_get_var(mhm_ctx *ctx, int32_t member, const char *name, double *out);
 int mhm_set_timing(mhm_ctx *ctx, int32_t on);
 int mhm_get_timing(mhm_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
 
+/* L11 links from the L11 flow directions (host computation, no device
+ * needed): replaces L11_set_network_topology
+ * (src/mRM/mo_mrm_net_startup.f90:630-727).  Cell k (1-based, packed
+ * column-major over the L11 mask) at grid row cell_row[k-1], column
+ * cell_col[k-1] (1-based) drains into the cell its D8 code fdir[k-1]
+ * (1, 2, 4, ..., 128 as moveDownOneCell steps them) points at; a cell that
+ * points at itself (code 0, the outlet) gives no link.  id2d [ncols * nrows]
+ * is the 1-based cell id of every grid cell, row index fastest (Fortran's
+ * iD11(row, col)).  from_n / to_n [n_cells] receive L11_fromN / L11_toN in
+ * cell order (-9999 past the last link), *n_links their number.
+ * MHM_ERR_INVALID if a direction leaves the grid or the mask. */
+int mhm_network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
+                         const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n,
+                         int32_t *n_links);
+
 /* Routing order of an L11 network (host computation, no device needed):
  * replaces L11_routing_order (src/mRM/mo_mrm_net_startup.f90:728-886) with an
  * O(nLinks x sweeps) algorithm giving the same ranks.  Inputs fromN/toN

@@ -1814,6 +1814,21 @@ int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n,
     return MHM_OK;
 }
 
+int mhm_network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
+                         const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n,
+                         int32_t *n_links)
+{
+    if (nrows < 1 || ncols < 1 || n_cells < 1 || !id2d || !cell_row || !cell_col || !fdir || !from_n || !to_n ||
+        !n_links)
+        return MHM_ERR_INVALID;
+    std::string err;
+    if (!network_topology(nrows, ncols, id2d, n_cells, cell_row, cell_col, fdir, from_n, to_n, n_links, err)) {
+        std::fprintf(stderr, "mhm_network_topology: %s\n", err.c_str());
+        return MHM_ERR_INVALID;
+    }
+    return MHM_OK;
+}
+
 int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t n, int32_t *month,
                       int32_t *hour, int32_t *doy)
 {

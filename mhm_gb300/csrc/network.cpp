@@ -166,4 +166,45 @@ bool routing_order(int32_t L, int32_t n_outlets, const int32_t *from_n, const in
     return true;
 }
 
+bool network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
+                      const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n, int32_t *n_links,
+                      std::string &err)
+{
+    for (int32_t k = 0; k < n_cells; ++k) from_n[k] = to_n[k] = -9999; // nodata_i4
+    int32_t nl = 0;
+    for (int32_t k = 0; k < n_cells; ++k) {
+        // row / column offsets of the ESRI D8 codes, as moveDownOneCell
+        // steps them (src/mRM/mo_mrm_net_startup.f90:1768-1801); any other
+        // code leaves the cell where it is
+        int32_t di = 0, dj = 0;
+        switch (fdir[k]) {
+        case 1: dj = 1; break;
+        case 2: di = 1; dj = 1; break;
+        case 4: di = 1; break;
+        case 8: di = 1; dj = -1; break;
+        case 16: dj = -1; break;
+        case 32: di = -1; dj = -1; break;
+        case 64: di = -1; break;
+        case 128: di = -1; dj = 1; break;
+        default: break;
+        }
+        const int32_t i = cell_row[k] + di, j = cell_col[k] + dj; // 1-based
+        if (i < 1 || i > nrows || j < 1 || j > ncols) {
+            err = "network_topology: flow direction of cell " + std::to_string(k + 1) + " leaves the grid";
+            return false;
+        }
+        const int32_t to = id2d[(size_t)(j - 1) * nrows + (i - 1)];
+        if (to == k + 1) continue; // points at itself: an outlet
+        if (to < 1 || to > n_cells) {
+            err = "network_topology: flow direction of cell " + std::to_string(k + 1) + " leaves the mask";
+            return false;
+        }
+        from_n[nl] = k + 1;
+        to_n[nl] = to;
+        ++nl;
+    }
+    *n_links = nl;
+    return true;
+}
+
 } // namespace mhm

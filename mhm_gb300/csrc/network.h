@@ -35,4 +35,14 @@ bool build_level_network(int32_t n_nodes, int32_t n_outlets, const int32_t *net_
 bool routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n, const int32_t *to_n,
                    int32_t *net_perm, int32_t *r_order, std::string &err);
 
+// L11 links from the L11 flow directions (L11_set_network_topology,
+// src/mRM/mo_mrm_net_startup.f90:630-727): cell k (1-based, packed order)
+// drains into the cell its D8 code points at; cells pointing at themselves
+// (outlets) give no link.  id2d [ncols][nrows] holds the 1-based cell id of
+// every grid cell (column-major over (row, col)); from_n / to_n [n_cells]
+// receive the links in cell order, -9999 past the last.
+bool network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
+                      const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n, int32_t *n_links,
+                      std::string &err);
+
 } // namespace mhm

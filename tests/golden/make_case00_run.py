@@ -8,7 +8,8 @@ pre/tavg/pet netCDF-4, L2 = L1 = 24 km) for the simulated period 1990-01-01
 .. 1991-06-30 (181 warm-up days + the evaluation year), the L11 network mRM
 built (L11_fromN/toN/netPerm/length/slope, the floodplain impervious
 fraction per land-cover scene, cell areas, the gauge node) from
-b1_mRM_restart_001.nc, and case_00's mhm.nml meteo tables.  Outputs: the
+b1_mRM_restart_001.nc (with the L11 mask and flow directions it was built
+from), and case_00's mhm.nml meteo tables.  Outputs: the
 daily simulated discharge of b1_daily_discharge.out and the final states of
 both restart files.  Cell arrays are packed column-major over mHM's (x, y)
 L1 mask, i.e. in the row-major order of the north-first grids.
@@ -141,6 +142,7 @@ def main():
         jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
         warming_days=WARMING_DAYS, scene2_from_day=SCENE2_FROM_DAY,
         from_n=mrm.read("L11_fromN").astype(np.int32), to_n=mrm.read("L11_toN").astype(np.int32),
+        mask11=mask11.astype(np.uint8), l11_fdir=mrm.read("L11_fDir")[mask11].astype(np.int32),
         net_perm=mrm.read("L11_netPerm").astype(np.int32), r_order=mrm.read("L11_rOrder").astype(np.int32),
         length=mrm.read("L11_length")[:n_links], slope=mrm.read("L11_slope")[:n_links],
         ffp_imp=np.stack([ffp[s][mask11][:n_links] for s in range(ffp.shape[0])]),

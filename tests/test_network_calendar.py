@@ -4,6 +4,7 @@ O(n^2) sweep, src/mRM/mo_mrm_net_startup.f90:728-886), the network topology
 (:630-727) and the per-step calendar (integer Gregorian arithmetic vs the
 restated dec2date of newTime - 0.5).  All bit-exact."""
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -79,3 +80,42 @@ def test_step_calendar(jul_start, timestep, n, lib, ora_hmath):
     mo, ho, do = (np.zeros(n, np.int32) for _ in range(3))
     ora_hmath.ora_step_calendar(jul_start, timestep, n, _p(mo), _p(ho), _p(do), None, None)
     assert np.array_equal(m, mo) and np.array_equal(h, ho) and np.array_equal(d, do)
+
+
+def _topology(lib, nrows, ncols, id2d, rows, cols, fdir):
+    n = len(fdir)
+    fn = np.zeros(n, np.int32)
+    tn = np.zeros(n, np.int32)
+    nl = np.zeros(1, np.int32)
+    rc = lib.mhm_network_topology(nrows, ncols, _p(np.ascontiguousarray(id2d, np.int32)), n,
+                                  _p(np.ascontiguousarray(rows, np.int32)), _p(np.ascontiguousarray(cols, np.int32)),
+                                  _p(np.ascontiguousarray(fdir, np.int32)), _p(fn), _p(tn), _p(nl))
+    assert rc == 0
+    return fn, tn, int(nl[0])
+
+
+def test_native_network_topology_matches_oracle(lib, ora_hmath):
+    dom = synth.make_domain(60, 44, 2, 4, seed=3, dem_kind="fractal", ridges=1)
+    fn, tn, nl = _topology(lib, dom.nrows11, dom.ncols11, dom.id11_2d, dom.cell_row11, dom.cell_col11, dom.fdir11)
+    assert nl == dom.n_links
+    assert np.array_equal(fn, dom.from_n) and np.array_equal(tn, dom.to_n)
+
+
+def test_native_network_topology_reproduces_case00(lib):
+    """check/case_00's L11 flow directions give exactly the L11_fromN / L11_toN
+    its mRM restart file holds (integer parity of the network set-up)."""
+    z = np.load(Path(__file__).resolve().parent / "golden" / "case00_run.npz")
+    mask = z["mask11"].astype(bool)                 # [ncols][nrows]
+    ncols, nrows = mask.shape
+    jj, ii = np.nonzero(mask)                       # packing order (row index fastest)
+    n = int(mask.sum())
+    id2d = np.full(mask.shape, -9999, np.int32)
+    id2d[mask] = np.arange(1, n + 1)
+    fn, tn, nl = _topology(lib, nrows, ncols, id2d, ii + 1, jj + 1, z["l11_fdir"])
+    assert nl == n - 1
+    assert np.array_equal(fn, z["from_n"]) and np.array_equal(tn, z["to_n"])
+    # and the routing order built from them is the reference's netPerm / rOrder
+    perm = np.zeros(n, np.int32)
+    ro = np.zeros(n, np.int32)
+    assert lib.mhm_routing_order(n, 1, _p(fn), _p(tn), _p(perm), _p(ro)) == 0
+    assert np.array_equal(perm, z["net_perm"]) and np.array_equal(ro, z["r_order"])
