@@ -193,6 +193,12 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
 int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge);
 /* Wait for all enqueued work of the context. */
 int mhm_sync(mhm_ctx *ctx);
+/* Without waiting: *done = 1 if all work enqueued so far has completed on
+ * the device (mhm_sync then returns at once and finishes the host side:
+ * gauge series into the caller's buffers), else 0.  For a serving loop that
+ * advances several contexts independently.  No counterpart in the
+ * reference. */
+int mhm_poll(mhm_ctx *ctx, int32_t *done);
 
 /* Members at different model steps (continuous batching of independent runs
  * of one basin): member m advances its own steps member_tt0[m] ..

@@ -95,6 +95,7 @@ EXPORTS = [
     "mhm_enable_fluxes", "mhm_get_fluxes", "mhm_set_link_fpimp",
     "mhm_enable_flux_state_outputs", "mhm_read_flux_state_outputs", "mhm_enable_routed_outputs",
     "mhm_read_routed_outputs", "mhm_set_output_weights", "mhm_set_link_celerity", "mhm_network_topology",
+    "mhm_poll",
 ]
 
 _LIB = None
@@ -167,6 +168,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_read_routed_outputs.argtypes = [vp, _dp, i64p, C.c_int32, _ip]
     L.mhm_set_output_weights.argtypes = [vp, C.c_int32, C.c_int64, _dp, _dp]
     L.mhm_set_link_celerity.argtypes = [vp, C.c_int32, _dp]
+    L.mhm_poll.argtypes = [vp, _ip]
     L.mhm_network_topology.argtypes = [C.c_int32, C.c_int32, _ip, C.c_int32, _ip, _ip, _ip, _ip, _ip, _ip]
     L.mhm_snapshot_load.argtypes = [vp, C.c_int32, C.c_int32]
     _LIB = L

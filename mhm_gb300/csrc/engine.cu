@@ -168,6 +168,7 @@ struct mhm_ctx {
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_cell_done[2] = {nullptr, nullptr}, ev_acc_done[2] = {nullptr, nullptr};
     cudaEvent_t ev_route_end = nullptr, run_a = nullptr;
+    cudaEvent_t ev_poll[3] = {nullptr, nullptr, nullptr};
     bool timing = false;
     std::vector<TimedLaunch> pending;
     int64_t t_launches[4] = {0, 0, 0, 0};
@@ -668,6 +669,8 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
         if (ctx->ev_acc_done[i]) cudaEventDestroy(ctx->ev_acc_done[i]);
     }
     if (ctx->ev_route_end) cudaEventDestroy(ctx->ev_route_end);
+    for (cudaEvent_t e : ctx->ev_poll)
+        if (e) cudaEventDestroy(e);
     for (auto &st : ctx->qg_stage) {
         if (st.pinned) cudaFreeHost(st.pinned);
         if (st.ev) cudaEventDestroy(st.ev);
@@ -1357,6 +1360,26 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     ctx->call_seq += 1;
     ctx->last_steps = n_steps;
     ctx->pending_outputs = ctx->out_tro || ctx->out_qmod;
+    return MHM_OK;
+}
+
+int mhm_poll(mhm_ctx *ctx, int32_t *done)
+{
+    if (!ctx || !done) return MHM_ERR_INVALID;
+    // events recorded now cover everything enqueued so far on the streams
+    if (!ctx->ev_poll[0])
+        for (auto &e : ctx->ev_poll) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    cudaStream_t ss[3] = {ctx->stream, ctx->route_stream, ctx->copy_stream};
+    *done = 1;
+    for (int i = 0; i < 3; ++i) {
+        CK(cudaEventRecord(ctx->ev_poll[i], ss[i]), "poll record");
+        const cudaError_t e = cudaEventQuery(ctx->ev_poll[i]);
+        if (e == cudaErrorNotReady) {
+            *done = 0;
+        } else if (e != cudaSuccess) {
+            return cuda_fail(ctx, e, "poll");
+        }
+    }
     return MHM_OK;
 }
 

@@ -352,6 +352,12 @@ class MhmGpu:
     def sync(self):
         self._check(self.L.mhm_sync(self.ctx), "mhm_sync")
 
+    def poll(self) -> bool:
+        """True if all enqueued work has completed (sync() then returns at once)."""
+        d = C.c_int32()
+        self._check(self.L.mhm_poll(self.ctx, C.byref(d)), "mhm_poll")
+        return bool(d.value)
+
     def get_outputs(self):
         n = self._last_steps
         tro = np.zeros((n, self.n_members, self.dom.n_cells)) if self._out[0] else None

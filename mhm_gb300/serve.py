@@ -4,17 +4,19 @@ A request is one forecast run on a basin of the catalogue: a global
 parameter vector (regionalised on the device by MPR), a horizon in hourly
 steps and a warm start from the basin's restart state, which stays resident
 on the device as a snapshot.  The server keeps, per basin with work, one
-context whose members are request slots; every iteration it
+context whose members are request slots; the loop
 
-  1. admits waiting requests into free slots (device MPR for the slot, the
-     restart snapshot loaded into it) -- creating a basin's context only when
-     its device footprint fits the HBM budget, and retiring contexts that
-     have gone idle to make room;
-  2. enqueues one chunk of steps for every context with work, each member at
-     its own model step (mhm_run_members_async), so the contexts' kernels
-     overlap on the device;
-  3. waits, hands each active slot its chunk of outlet discharge, and frees
-     the slots whose horizon is complete.
+  1. admits waiting requests into free slots of idle contexts (device MPR
+     for the slot, the restart snapshot loaded into it) -- creating a basin's
+     context only when its device footprint fits the HBM budget, and
+     retiring contexts that have gone idle to make room;
+  2. enqueues one chunk of steps on every idle context with work, each
+     member at its own model step (mhm_run_members_async), so the contexts'
+     kernels overlap on the device;
+  3. polls the contexts without waiting (mhm_poll) and, for each whose chunk
+     has completed, hands its active slots their chunk of outlet discharge,
+     frees the slots whose horizon is complete and makes the context idle --
+     every context advances at its own pace.
 
 Requests that arrive while others run join at the next chunk boundary of
 their basin's context.  A member's arithmetic does not depend on the other
@@ -157,7 +159,7 @@ class Server:
             t = g.autotune(1, self.chunk)
             self.tuned[b.name] = {k: t[k] for k in ("cell_blocks_per_sm", "route_sub_steps")}
         self.ctx[bi] = {"g": g, "slots": [None] * members, "tt0": np.zeros(members, np.int32), "bytes": need,
-                        "q": np.zeros((members, len(b.dom.gauge_node), self.chunk))}
+                        "q": np.zeros((members, len(b.dom.gauge_node), self.chunk)), "busy": False}
         self.used += need
         return True
 
@@ -177,6 +179,9 @@ class Server:
                 still.append(r)
                 continue
             c = self.ctx.get(r.basin)
+            if c is not None and c["busy"]:
+                still.append(r)          # its chunk in flight: admit at the next completion
+                continue
             if c is None:
                 want = min(self.max_slots, max(1, sum(1 for w in self.waiting
                                                       if w.basin == r.basin and w.arrival <= now)))
@@ -202,18 +207,30 @@ class Server:
         self.waiting = still
 
     def step(self, now: float) -> bool:
-        """One iteration; returns False when there is nothing to do."""
+        """One pass of the loop; returns False when there is nothing to do.
+        Every context advances at its own pace: a chunk is enqueued on each
+        idle context with active slots, and a context whose chunk has
+        completed (mhm_poll, no waiting) is finished and can take its next
+        chunk and new requests at once -- a small basin is not held back by
+        the chunk of a large one."""
         self._admit(now)
-        active = [(bi, c) for bi, c in self.ctx.items() if any(s is not None for s in c["slots"])]
-        if not active:
-            return False
-        for bi, c in active:                       # enqueue every context's chunk ...
+        for bi, c in self.ctx.items():
+            if c["busy"] or not any(s is not None for s in c["slots"]):
+                continue
             tt0 = np.where([s is not None for s in c["slots"]], c["tt0"], 0).astype(np.int32)
             c["tt0_now"] = tt0
             c["g"].run_members_async(tt0, self.chunk, c["q"])
-        t_done = None
-        for bi, c in active:                       # ... then wait for all of them
-            c["g"].sync()
+            c["busy"] = True
+        busy = [(bi, c) for bi, c in self.ctx.items() if c["busy"]]
+        if not busy:
+            return False
+        progressed = False
+        for bi, c in busy:
+            if not c["g"].poll():
+                continue
+            c["g"].sync()                          # host side of the chunk (gauge series)
+            c["busy"] = False
+            progressed = True
             t_done = time.perf_counter()
             n = self.basins[bi].n_cells
             for m, r in enumerate(c["slots"]):
@@ -226,6 +243,8 @@ class Server:
                     r.done = t_done - self._t0
                     self.finished.append(r)
                     c["slots"][m] = None
+        if not progressed:
+            time.sleep(2e-4)
         self.iterations += 1
         return True
 
