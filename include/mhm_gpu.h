@@ -51,6 +51,7 @@ extern "C" {
 #define MHM_FORC_PET 2
 #define MHM_FORC_TMIN 3
 #define MHM_FORC_TMAX 4
+#define MHM_FORC_NETRAD 5 /* L1_netrad [W m-2], Priestley-Taylor PET (proc_pet = 2) */
 
 typedef struct mhm_ctx mhm_ctx;
 
@@ -65,7 +66,7 @@ typedef struct {
     int32_t n_outlets;           /* L11_nOutlets                               */
     int32_t timestep;            /* model time step [h] (mhm.nml timestep)     */
     int32_t proc_soilmoist;      /* processMatrix(3,1): 1..4                   */
-    int32_t proc_pet;            /* processMatrix(5,1): -1, 0 or 1             */
+    int32_t proc_pet;            /* processMatrix(5,1): -1, 0, 1 or 2          */
     int32_t proc_routing;        /* processMatrix(8,1): 0, 1 (Muskingum), 2
                                     (Muskingum with a routing time step chosen
                                     from a constant celerity) or 3 (from each
@@ -106,6 +107,8 @@ typedef struct {
     const double *maxInter;        /* [12 * n_cells] (cell, LAI month)          */
     const double *petLAIcorFactor; /* [12 * n_cells] or NULL (proc_pet = -1)    */
     const double *fRoots, *soilMoistSat, *soilMoistFC, *wiltingPoint, *soilMoistExp; /* [H * n_cells] */
+    const double *PrieTayAlpha;    /* [12 * n_cells] or NULL (proc_pet = 2, L1_PrieTayAlpha); it shares
+                                      the device planes of petLAIcorFactor, which is then not read back */
 } mhm_eff_params;
 
 /* Restart state of one member: the fields of src/mHM/mo_restart.f90:146-258

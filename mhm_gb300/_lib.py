@@ -19,7 +19,7 @@ MHM_ERR_TIMEOUT = -4
 MHM_ERR_NAN = -5
 MHM_ERR_UNSUPPORTED = -6
 
-FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX = range(5)
+FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX, FORC_NETRAD = range(6)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -45,7 +45,7 @@ EFF_PARAM_FIELDS = [
     "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco",
     "jarvis_thresh_c1", "tempThresh", "unsatThresh", "sealedThresh",
     "maxInter", "petLAIcorFactor",
-    "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp",
+    "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "PrieTayAlpha",
 ]
 
 

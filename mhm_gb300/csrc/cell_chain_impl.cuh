@@ -33,6 +33,9 @@ constexpr double kTwoPiD = 6.283185307179586476925286766559005768394;
 constexpr double kDaySecs = 86400.0, kYearDays = 365.0, kSolarConst = 1367.0, kSpecHeatET = 2.45e06;
 constexpr double kDeg2Rad = 3.141592653589793238462643383279502884197 / 180.0;
 constexpr double kHarSamConst = 17.800;
+// src/common/mo_constants.f90 (Psychro_dp) and src/mHM/mo_mhm_constants.f90 (tetens_c*, satpressureslope1)
+constexpr double kPsychro = 0.0646, kTetensC1 = 0.6108, kTetensC2 = 17.270, kTetensC3 = 237.30;
+constexpr double kSatPressureSlope1 = 4098.0;
 
 // src/mHM/mo_pet.f90:314-355 (CUDA's sin/cos/tan/acos; only the daily-forcing
 // Hargreaves variant uses it)
@@ -60,6 +63,16 @@ __device__ double pet_hargreaves(double coeff, double tavg, double tmax, double 
     double delta_temp = tmax - tmin;
     if (le_dp(delta_temp, 0.0) || le_dp(tavg, -kHarSamConst)) return 0.0;
     return coeff * rad * (tavg + kHarSamConst) * sqrt(delta_temp);
+}
+
+// src/mHM/mo_pet.f90:149-174 (pet_priestly), with slope_satpressure (:384-399)
+// and sat_vap_pressure written as the reference does: exp(2 log(T + c3)) for
+// the square, divisions in the same order
+__device__ double pet_priestly(double alpha, double rn, double tavg)
+{
+    const double svp = kTetensC1 * hm_exp(kTetensC2 * tavg / (tavg + kTetensC3));
+    const double delta = kSatPressureSlope1 * svp / hm_exp(2.0 * hm_log(tavg + kTetensC3));
+    return alpha * delta / (kPsychro + delta) * (rn * kDaySecs / kSpecHeatET);
 }
 
 // Per-thread scalars live in registers; the per-horizon parameters and soil
@@ -197,7 +210,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             r_imax = hm_recip_of(imax);
             evap = a.tab.evap[month - 1];
             r_evap = hm_recip_of(evap);
-            if (a.proc_pet == -1) petlai = par(P_PETLAI + month - 1);
+            // petLAIcorFactor (proc_pet -1) or PrieTayAlpha (proc_pet 2) of the LAI month
+            if (a.proc_pet == -1 || a.proc_pet == 2) petlai = par(P_PETLAI + month - 1);
         }
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
         // output weights: write_output runs after the calendar has advanced, so
@@ -218,6 +232,9 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             pv = c.fasp * __ldg(a.pet + f);
         } else if (a.proc_pet == -1) {
             pv = petlai * __ldg(a.pet + f);
+        } else if (a.proc_pet == 2) { // Rn = max(L1_netrad, 0), src/meteo/mo_meteo_handler.f90:1080-1085
+            const double rn = __ldg(a.netrad + f);
+            pv = pet_priestly(petlai, rn > 0.0 ? rn : 0.0, __ldg(a.temp + f));
         } else {
             if (si.doy != cur_doy) {
                 cur_doy = si.doy;

@@ -132,14 +132,14 @@ struct mhm_ctx {
     // device: per run / chunk
     DevBuf<StepInfo> steps;
     DevBuf<double> tro[2], qout, qtr, qmod, q_gauge[2];
-    DevBuf<double> stage[5][2];
+    DevBuf<double> stage[kForcKinds][2];
     int32_t tc_cap = 0, stage_rows = 0;
     size_t qg_cap[2] = {0, 0};
     int64_t chunk_seq = 0, call_seq = 0;
     bool slot_used[2] = {false, false};
     bool pending_outputs = false;
     // forcing
-    ForcingSrc forc[5];
+    ForcingSrc forc[kForcKinds];
     // gauge series of the calls in flight: device -> pinned staging (an
     // asynchronous copy; a copy into pageable memory would block the host
     // until the routing finished) -> the caller's buffer at the next
@@ -481,7 +481,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     if (d->n_members < 1) return bad("n_members < 1");
     if (d->timestep < 1 || 24 % d->timestep != 0) return bad("timestep must divide 24 hours");
     if (d->proc_soilmoist < 1 || d->proc_soilmoist > 4) return bad("proc_soilmoist must be 1..4");
-    if (d->proc_pet < -1 || d->proc_pet > 1) return bad("proc_pet must be -1, 0 or 1 (2, 3 unsupported)");
+    if (d->proc_pet < -1 || d->proc_pet > 2) return bad("proc_pet must be -1, 0, 1 or 2 (3 unsupported)");
     if (d->proc_routing < 0 || d->proc_routing > 3) return bad("proc_routing must be 0, 1, 2 or 3");
     if (d->n_tstep_forcing_day != 24 && d->n_tstep_forcing_day != 1)
         return bad("n_tstep_forcing_day must be 24 or 1");
@@ -714,10 +714,12 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
     CK(cudaMemcpyAsync(base + (size_t)P_MAXINTER * N, p->maxInter, 12 * N * sizeof(double),
                        cudaMemcpyHostToDevice, ctx->stream),
        "maxInter");
-    if (ctx->proc_pet == -1) {
-        if (!p->petLAIcorFactor) return fail(ctx, MHM_ERR_INVALID, "petLAIcorFactor missing");
-        CK(cudaMemcpyAsync(base + (size_t)P_PETLAI * N, p->petLAIcorFactor, 12 * N * sizeof(double),
-                           cudaMemcpyHostToDevice, ctx->stream),
+    if (ctx->proc_pet == -1 || ctx->proc_pet == 2) { // the same planes hold either monthly factor
+        const double *monthly = ctx->proc_pet == -1 ? p->petLAIcorFactor : p->PrieTayAlpha;
+        if (!monthly) return fail(ctx, MHM_ERR_INVALID, ctx->proc_pet == -1 ? "petLAIcorFactor missing"
+                                                                              : "PrieTayAlpha missing");
+        CK(cudaMemcpyAsync(base + (size_t)P_PETLAI * N, monthly, 12 * N * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream),
            "petLAI");
     }
     const double *hz[5] = {p->fRoots, p->soilMoistSat, p->soilMoistFC, p->wiltingPoint, p->soilMoistExp};
@@ -768,7 +770,9 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
         const double *dst;
         int plane, n_planes;
     };
-    const Part parts[] = {{p->maxInter, P_MAXINTER, 12},          {p->petLAIcorFactor, P_PETLAI, 12},
+    const Part parts[] = {{p->maxInter, P_MAXINTER, 12},
+                          {ctx->proc_pet == 2 ? nullptr : p->petLAIcorFactor, P_PETLAI, 12},
+                          {ctx->proc_pet == 2 ? p->PrieTayAlpha : nullptr, P_PETLAI, 12},
                           {p->fRoots, P_HORIZON, H},              {p->soilMoistSat, P_HORIZON + H, H},
                           {p->soilMoistFC, P_HORIZON + 2 * H, H}, {p->wiltingPoint, P_HORIZON + 3 * H, H},
                           {p->soilMoistExp, P_HORIZON + 4 * H, H}};
@@ -842,7 +846,7 @@ int mhm_init_states(mhm_ctx *ctx, int32_t m, const double *hd)
 int mhm_set_forcing(mhm_ctx *ctx, int32_t kind, int32_t row0, int32_t n_rows, const double *data, int32_t on_device)
 {
     if (!ctx) return MHM_ERR_INVALID;
-    if (kind < 0 || kind > 4) return fail(ctx, MHM_ERR_INVALID, "forcing kind");
+    if (kind < 0 || kind >= kForcKinds) return fail(ctx, MHM_ERR_INVALID, "forcing kind");
     if (row0 < 1 || n_rows < 1 || !data) return fail(ctx, MHM_ERR_INVALID, "forcing rows");
     ForcingSrc &f = ctx->forc[kind];
     f.ptr = data;
@@ -897,7 +901,8 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
     const int H = ctx->H;
     CK(cudaSetDevice(ctx->device), "set device");
-    bool need[5] = {true, true, ctx->proc_pet != 1, ctx->proc_pet == 1, ctx->proc_pet == 1};
+    const bool need[kForcKinds] = {true, true, ctx->proc_pet == 0 || ctx->proc_pet == -1, ctx->proc_pet == 1,
+                                   ctx->proc_pet == 1, ctx->proc_pet == 2};
     const int32_t stride = (int32_t)std::lround(24.0 / (double)ctx->ntfd);
     const bool members = member_tt0 != nullptr;
     if (members && (stride != 1 || ctx->ntfd != 24))
@@ -915,7 +920,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     const int32_t last_row = members ? ctx->forc[0].row0 + n_steps - 1 : (tt0 + n_steps - 1 + stride - 1) / stride;
     int on_device = -1;
     int32_t row0_all = 0;
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < kForcKinds; ++k) {
         if (!need[k]) continue;
         const ForcingSrc &f = ctx->forc[k];
         if (!f.set) return fail(ctx, MHM_ERR_INVALID, "forcing kind " + std::to_string(k) + " not set");
@@ -967,7 +972,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             CK(ctx->qmod.ensure(M * (size_t)Tc * L), "qmod chunk");
         }
         const int32_t max_rows = (Tc + stride - 1) / stride + 1;
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < kForcKinds; ++k)
             for (int s = 0; s < 2; ++s) ctx->stage[k][s].release();
         ctx->stage_rows = max_rows;
         ctx->tc_cap = Tc;
@@ -981,7 +986,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         }
     }
     if (!on_device)
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < kForcKinds; ++k)
             if (need[k])
                 for (int s = 0; s < 2; ++s) CK(ctx->stage[k][s].ensure((size_t)ctx->stage_rows * N), "forcing staging");
     if (ctx->proc_rout >= 1 && ctx->G > 0 && q_gauge) {
@@ -1013,7 +1018,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         int32_t r0, r1;
         chunk_rows(c, r0, r1);
         if (ctx->slot_used[slot]) CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_consumed[slot], 0), "wait slot");
-        for (int k = 0; k < 5; ++k) {
+        for (int k = 0; k < kForcKinds; ++k) {
             if (!need[k]) continue;
             const ForcingSrc &f = ctx->forc[k];
             CK(cudaMemcpyAsync(ctx->stage[k][slot].p, f.ptr + (size_t)(r0 - f.row0) * N,
@@ -1083,16 +1088,16 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.reset_sm = (tt0 + s0 == 1) && !ctx->read_states;
         a.c2TSTu = (double)ctx->timestep / 24.0;
         a.nTstepDay = 24.0 / (double)ctx->timestep;
-        const double *fp[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        const double *fp[kForcKinds] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
         if (on_device) {
             a.row_base = row0_all;
-            for (int k = 0; k < 5; ++k)
+            for (int k = 0; k < kForcKinds; ++k)
                 if (need[k]) fp[k] = ctx->forc[k].ptr;
         } else {
             int32_t r0, r1;
             chunk_rows(c, r0, r1);
             a.row_base = r0;
-            for (int k = 0; k < 5; ++k)
+            for (int k = 0; k < kForcKinds; ++k)
                 if (need[k]) fp[k] = ctx->stage[k][slot].p;
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[slot], 0), "wait copied");
         }
@@ -1101,6 +1106,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.pet = fp[2];
         a.tmin = fp[3];
         a.tmax = fp[4];
+        a.netrad = fp[5];
         a.steps = ctx->steps.p;
         if (members) {
             a.steps = ctx->steps_all.p;
@@ -1881,8 +1887,8 @@ int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
     if (!ctx || !l0) return MHM_ERR_INVALID;
     if (int rc = mhm_sync(ctx)) return rc;
     ctx->mpr_ready = false;
-    if (ctx->proc_pet != -1 && ctx->proc_pet != 0 && ctx->proc_pet != 1)
-        return fail(ctx, MHM_ERR_UNSUPPORTED, "MPR supports PET cases -1, 0 and 1");
+    if (ctx->proc_pet < -1 || ctx->proc_pet > 2)
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "MPR supports PET cases -1, 0, 1 and 2");
     if (l0->max_soil_hor > kMprMaxSoilHor)
         return fail(ctx, MHM_ERR_UNSUPPORTED, "more than 16 soil layers per soil type");
     MprSetup &m = ctx->mpr;

@@ -6,6 +6,7 @@
 namespace mhm {
 
 constexpr int kMaxHorizons = 8;
+constexpr int kForcKinds = 6; // pre, temp, pet, tmin, tmax, net radiation
 
 // Per-member effective-parameter planes, each [n_cells] contiguous:
 // params[(m * n_planes + plane) * n_cells + k].
@@ -100,6 +101,7 @@ struct CellArgs {
     double c2TSTu;      // timestep / 24
     double nTstepDay;   // 24 / timestep
     const double *pre, *temp, *pet, *tmin, *tmax; // [rows][n_cells] from row_base
+    const double *netrad;                         // [rows][n_cells] (proc_pet 2) or null
     const StepInfo *steps;                        // [n_steps]
     const double *params;                         // [M][planes][n_cells]
     double *states;                               // [M][planes][n_cells]

@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
     const size_t slots = (size_t)a.max_sub * N;
     const double *plai = a.petlai + (size_t)m * 3 * a.n_lai_classes * 12;
     for (int mo = 0; mo < 12; ++mo) {
-        double s_int = 0.0, s_pet = 0.0;
+        double s_int = 0.0, s_pet = 0.0, s_pt = 0.0;
         for (int j = 0; j < ns; ++j) {
             const uint32_t c = __ldg(code + (size_t)j * N);
             double lai;
@@ -333,6 +333,8 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
                 lai = __ldg(a.lai_lut + ((c >> 16) & 0xFFu) * 12 + mo);
             }
             s_int = s_int + lai * gi;
+            // priestley_taylor_alpha, src/MPR/mo_mpr_pet.f90:311-369: alpha0 = p1 + p2 LAI0
+            if (a.proc_pet == 2) s_pt = s_pt + (pp[0] + pp[1] * lai);
             if (a.proc_pet == -1) {
                 const int l = (int)((c & kMprKeyMask) % 3u);
                 double inv;
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
             }
         }
         out[(size_t)(P_MAXINTER + mo) * N + k] = s_int / dn;
-        out[(size_t)(P_PETLAI + mo) * N + k] = (a.proc_pet == -1) ? dn / s_pet : 0.0;
+        out[(size_t)(P_PETLAI + mo) * N + k] = (a.proc_pet == -1) ? dn / s_pet : (a.proc_pet == 2) ? s_pt / dn : 0.0;
     }
 }
 

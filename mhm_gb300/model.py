@@ -160,7 +160,7 @@ class MhmGpu:
         """The member's effective parameters (L1_* arrays) read back."""
         N, H = self.dom.n_cells, self.dom.n_horizons
         sizes = {"maxInter": 12 * N, "petLAIcorFactor": 12 * N, "fRoots": H * N, "soilMoistSat": H * N,
-                 "soilMoistFC": H * N, "wiltingPoint": H * N, "soilMoistExp": H * N}
+                 "soilMoistFC": H * N, "wiltingPoint": H * N, "soilMoistExp": H * N, "PrieTayAlpha": 12 * N}
         out = {n: np.zeros(sizes.get(n, N)) for n in _lib.EFF_PARAM_FIELDS}
         ep = _lib.EffParams(**{n: _d(a) for n, a in out.items()})
         self._check(self.L.mhm_get_eff_params(self.ctx, member, C.byref(ep)), "mhm_get_eff_params")
@@ -227,7 +227,8 @@ class MhmGpu:
         self._check(self.L.mhm_set_forcing(self.ctx, kind, row0, n_rows, ptr, 1 if on_device else 0),
                     "mhm_set_forcing")
 
-    def set_meteo(self, row0: int, pre, temp, pet=None, tmin=None, tmax=None, on_device: bool = False):
+    def set_meteo(self, row0: int, pre, temp, pet=None, tmin=None, tmax=None, on_device: bool = False,
+                  netrad=None):
         self.set_forcing(_lib.FORC_PRE, row0, pre, on_device)
         self.set_forcing(_lib.FORC_TEMP, row0, temp, on_device)
         if pet is not None:
@@ -236,6 +237,8 @@ class MhmGpu:
             self.set_forcing(_lib.FORC_TMIN, row0, tmin, on_device)
         if tmax is not None:
             self.set_forcing(_lib.FORC_TMAX, row0, tmax, on_device)
+        if netrad is not None:
+            self.set_forcing(_lib.FORC_NETRAD, row0, netrad, on_device)
 
     # ---- time stepping (do_time_step x n) ----
     def enable_outputs(self, total_runoff: bool = False, qmod: bool = False):

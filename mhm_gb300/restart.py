@@ -50,6 +50,7 @@ EFF_PARAMS = {
     "L1_wiltingPoint": ("wiltingPoint", ("scene", "horizon")),
     "L1_fAsp": ("fAsp", ()),
     "L1_HarSamCoeff": ("HarSamCoeff", ()),
+    "L1_PrieTayAlpha": ("PrieTayAlpha", ("lai",)),
 }
 # mHM restart variable -> state name of mhm_restart (the L1 storages)
 STATES = {"L1_Inter": "interc", "L1_snowPack": "snowpack", "L1_sealSTW": "sealSTW", "L1_soilMoist": "soilMoist",

@@ -908,6 +908,7 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
         const double *pet = f->pet ? f->pet + (size_t)row * N : NULL;
         const double *tmin = f->tmin ? f->tmin + (size_t)row * N : NULL;
         const double *tmax = f->tmax ? f->tmax + (size_t)row * N : NULL;
+        const double *netrad = f->netrad ? f->netrad + (size_t)row * N : NULL;
         const double evap_coeff = d->evap_coeff[month - 1];
         const int iLAI = month; /* timeStep_LAI_input = 0 (mo_common_datetime_type.f90:135-155) */
         /* this step's outputs (write_output after do_time_step) */
@@ -935,6 +936,10 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
             switch (d->proc_pet) {
             case -1: pv = p->petLAIcorFactor[(size_t)(iLAI - 1) * N + k] * pet[k]; break;
             case 0: pv = p->fAsp[k] * pet[k]; break;
+            case 2: /* Priestley-Taylor, not defined for netrad < 0 (mo_meteo_handler.f90:1079-1084) */
+                pv = ora_pet_priestly(p->PrieTayAlpha[(size_t)(iLAI - 1) * N + k],
+                                      netrad[k] > 0.0 ? netrad[k] : 0.0, tmp[k]);
+                break;
             default:
                 pv = p->fAsp[k] * ora_pet_hargreaves(p->HarSamCoeff[k], HARSAMCONST, tmp[k], tmax[k],
                                                      tmin[k], d->latitude[k], doy);

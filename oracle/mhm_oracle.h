@@ -112,7 +112,7 @@ double ora_link_celerity(double slope_factor, const double *path_slope, int n);
 typedef struct {
     int32_t nCells, nH, nNodes, nOutlets, timestep;
     int32_t proc_sm;      /* processMatrix(3,1): 1..4 */
-    int32_t proc_pet;     /* processMatrix(5,1): -1, 0, 1 */
+    int32_t proc_pet;     /* processMatrix(5,1): -1, 0, 1, 2 */
     int32_t proc_rout;    /* processMatrix(8,1): 0, 1, 2 or 3 */
     int32_t nTstepForcingDay; /* 24 (hourly) or 1 (daily) */
     int32_t read_states;  /* 1: states (and C1/C2) come from a restart */
@@ -143,6 +143,7 @@ typedef struct {
     const double *maxInter;        /* [12][nCells] (column-major (nCells, 12)) */
     const double *petLAIcorFactor; /* [12][nCells] or NULL */
     const double *fRoots, *SMs, *FC, *PW, *beta; /* [nH][nCells] */
+    const double *PrieTayAlpha;    /* [12][nCells] Priestley-Taylor alpha (proc_pet 2) or NULL */
 } ora_params;
 
 typedef struct {
@@ -160,6 +161,7 @@ typedef struct {
     const double *pre, *temp, *pet, *tmin, *tmax;
     int32_t forc_row0;
     int32_t n_rows;
+    const double *netrad; /* net radiation [W m-2] (proc_pet 2) or NULL */
 } ora_forcing;
 
 /* Aggregated outputs of the run (mhm_interface_run_write_output,
@@ -222,7 +224,7 @@ typedef struct {
     int32_t maxHor;    /* stride of the per-soil horizon arrays */
     int32_t nGeo;      /* geological units */
     int32_t proc_sm;   /* processMatrix(3,1): 1..4 */
-    int32_t proc_pet;  /* processMatrix(5,1): -1, 0, 1 */
+    int32_t proc_pet;  /* processMatrix(5,1): -1, 0, 1, 2 */
     int32_t n_soil_params; /* processMatrix(3,2): 17, 18, 22 or 21 */
     int32_t pad_;
     double fracSealed_cityArea;
@@ -258,6 +260,7 @@ typedef struct {
     double *jarvis_c1, *tempThresh, *unsatThresh, *sealedThresh;
     double *maxInter, *petLAIcorFactor;
     double *fRoots, *SMs, *FC, *PW, *beta;
+    double *PrieTayAlpha; /* [12][nCells1] (proc_pet 2) or NULL */
 } ora_mpr_out;
 
 int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o);

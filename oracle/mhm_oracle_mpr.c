@@ -375,6 +375,23 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->fAsp[k] = 0.0;
             o->HarSamCoeff[k] = 0.0;
         }
+    } else if (d->proc_pet == 2) {
+        /* ---- Priestley-Taylor alpha, src/MPR/mo_mpr_pet.f90:311-369: arithmetic
+         * block mean of alpha0 = p1 + p2 * LAI0 per LAI month ---- */
+        const double *p = g->pet;
+        for (int m = 0; m < 12; ++m) {
+            for (int k = 0; k < N0; ++k)
+                tmp0[k] = p[0] + p[1] * d->LAI0[(size_t)m * N0 + k];
+            for (int k = 0; k < N1; ++k)
+                o->PrieTayAlpha[(size_t)m * N1 + k] = upscale_arith(d, k, tmp0);
+        }
+        for (int k = 0; k < N1; ++k) {
+            o->fAsp[k] = 0.0; /* not regionalised for this PET process */
+            o->HarSamCoeff[k] = 0.0;
+        }
+        if (o->petLAIcorFactor)
+            for (size_t i = 0; i < (size_t)12 * N1; ++i)
+                o->petLAIcorFactor[i] = 0.0;
     } else {
         /* ---- PET correction by aspect, src/MPR/mo_mpr_pet.f90:214-272 ---- */
         const double *p = g->pet;

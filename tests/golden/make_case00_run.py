@@ -116,6 +116,11 @@ def main():
         t = f.read("time")
         assert t[off] == off and a.shape[1:] == mask1.shape
         met[key] = np.ascontiguousarray(a[off:off + SIM_DAYS][:, mask1])
+    # daily net radiation (Priestley-Taylor PET): days since 1984-01-02, row 1826 = 1989-01-01
+    f = h5lite.H5File(str(TD / "meteo" / "net_rad.nc"))
+    a, t = f.read("net_rad"), f.read("time")
+    o = int(np.nonzero(t == julday(*SIM_START) - julday(1984, 1, 2))[0][0])
+    met["netrad"] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
     # daily minimum / maximum temperature (Hargreaves-Samani PET): days since 1933-12-31
     for key in ("tmin", "tmax"):
         f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
@@ -138,7 +143,7 @@ def main():
         gold_states[name] = np.stack([a[i][mask11] for i in range(a.shape[0])])
     np.savez_compressed(
         HERE / "case00_run.npz",
-        pre=met["pre"], temp=met["temp"], pet=met["pet"], tmin=met["tmin"], tmax=met["tmax"],
+        pre=met["pre"], temp=met["temp"], pet=met["pet"], tmin=met["tmin"], tmax=met["tmax"], netrad=met["netrad"],
         jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
         warming_days=WARMING_DAYS, scene2_from_day=SCENE2_FROM_DAY,
         from_n=mrm.read("L11_fromN").astype(np.int32), to_n=mrm.read("L11_toN").astype(np.int32),
@@ -163,16 +168,16 @@ def main():
 import make_case00_mpr as mpr_fix  # noqa: E402
 
 # processCase(3), processCase(5), processCase(8)
-CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2)}
+CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2), "case_02": (2, 2, 0)}
 PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "karstLoss", "kfastFlow",
                "kSlowFlow", "kBaseFlow", "kPerco", "tempThresh", "unsatThresh", "sealedThresh", "maxInter",
                "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "petLAIcorFactor",
-               "jarvis_thresh_c1")
+               "jarvis_thresh_c1", "PrieTayAlpha")
 
 
 def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
     cdir = REF / "check" / case
-    mrm = h5lite.H5File(str(cdir / "output_save" / "b1_mRM_restart_001.nc"))
+    mrm = h5lite.H5File(str(cdir / "output_save" / "b1_mRM_restart_001.nc")) if proc_rout else None
     mhm = h5lite.H5File(str(cdir / "output_save" / "b1_mHM_restart_001.nc"))
     mask1 = mhm.read("L1_domain_mask").astype(bool)
     names = mhm.group()
@@ -190,12 +195,13 @@ def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
         gold["s_" + name] = mhm.read(name)[mask1]
     sm = mhm.read("L1_soilMoist")
     gold["s_L1_soilMoist"] = np.stack([sm[h][mask1] for h in range(sm.shape[0])])
-    for name in ("L11_qOUT", "L11_Qmod", "L11_C1", "L11_C2"):
+    for name in ("L11_qOUT", "L11_Qmod", "L11_C1", "L11_C2") if mrm else ():
         gold["s_" + name] = mrm.read(name)[mask1]
-    q = np.loadtxt(cdir / "output_save" / "b1_daily_discharge.out", skiprows=1)
+    q = np.loadtxt(cdir / "output_save" / "b1_daily_discharge.out", skiprows=1) if mrm else np.zeros((0, 6))
     blocks = ["interception1", "snow1", f"soilmoisture{proc_sm}", "directRunoff1",
-              {-1: "PETminus1", 0: "PET0", 1: "PET1"}[proc_pet], "interflow1", "percolation1",
-              f"routing{proc_rout}", "geoparameter"]
+              {-1: "PETminus1", 0: "PET0", 1: "PET1", 2: "PET2"}[proc_pet], "interflow1", "percolation1"]
+    blocks += [f"routing{proc_rout}"] if proc_rout else []
+    blocks += ["geoparameter"]
     gamma = mpr_fix.namelist_values(cdir / "mhm_parameter.nml", blocks)
     extra = {}
     if proc_rout == 2:
