@@ -64,6 +64,7 @@ class MhmGpu:
         d.proc_soilmoist = proc_soilmoist
         d.proc_pet = proc_pet
         d.proc_routing = proc_routing
+        self.proc_soilmoist, self.proc_pet = proc_soilmoist, proc_pet
         d.n_tstep_forcing_day = 24 if hourly else 1
         d.jul_start = dom.jul_start
         d.map_flag = 1
@@ -409,7 +410,8 @@ class MhmGpu:
         from . import restart
         st = self.get_state(member)
         m1 = np.ones((1, self.dom.n_cells), bool) if mask is None else np.asarray(mask, bool)
-        restart.write_mhm_restart(mhm_path, m1, st, params_by_scene, self.dom.horizon_depth)
+        restart.write_mhm_restart(mhm_path, m1, st, params_by_scene, self.dom.horizon_depth,
+                                  proc_sm=self.proc_soilmoist, proc_pet=self.proc_pet)
         if mrm_path is not None:
             m11 = np.ones((1, self.dom.n_nodes), bool) if mask11 is None else np.asarray(mask11, bool)
             restart.write_mrm_restart(mrm_path, m11, {k: st[k] for k in restart.MRM_STATES.values()},

@@ -173,12 +173,41 @@ def read_mrm_restart(path) -> MrmRestart:
     return MrmRestart(mask, states, net, ts)
 
 
+def process_params(proc_sm: int, proc_pet: int) -> set[str]:
+    """The process-dependent restart variables the reference writes for
+    processCase(3) = proc_sm and processCase(5) = proc_pet
+    (src/MPR/mo_mpr_restart.f90:257-312): the Jarvis threshold for soil
+    moisture cases 2 and 3; per PET case the LAI correction factor (-1),
+    the aspect factor (-1, 0, 1), the Hargreaves-Samani coefficient (1) or
+    the Priestley-Taylor alpha (2)."""
+    out = set()
+    if proc_sm in (2, 3):
+        out.add("L1_jarvis_thresh_c1")
+    if proc_pet == -1:
+        out.add("L1_petLAIcorFactor")
+    if proc_pet in (-1, 0, 1):
+        out.add("L1_fAsp")
+    if proc_pet == 1:
+        out.add("L1_HarSamCoeff")
+    if proc_pet == 2:
+        out.add("L1_PrieTayAlpha")
+    return out
+
+
+PROCESS_DEPENDENT = {"L1_jarvis_thresh_c1", "L1_petLAIcorFactor", "L1_fAsp", "L1_HarSamCoeff", "L1_PrieTayAlpha"}
+
+
 def write_mhm_restart(path, mask: np.ndarray, states: dict[str, np.ndarray], params_by_scene: list[dict],
-                      horizon_depth, lai_bounds=None) -> None:
+                      horizon_depth, lai_bounds=None, proc_sm: int | None = None,
+                      proc_pet: int | None = None) -> None:
     """The states and the effective parameters of every scene in the layout
     of write_restart_files / write_eff_params (64-bit-offset netCDF).
     `states` as mhm_get_state returns them, `params_by_scene` one
-    mhm_eff_params dict per land-cover scene (flattened arrays)."""
+    mhm_eff_params dict per land-cover scene (flattened arrays).  With the
+    process cases given, the process-dependent parameters are the ones the
+    reference writes for them (process_params); otherwise every parameter
+    present in all scenes is written."""
+    keep = None if proc_sm is None or proc_pet is None else process_params(proc_sm, proc_pet)
     from scipy.io import netcdf_file
     mask = np.asarray(mask, bool)
     n = int(mask.sum())
@@ -211,6 +240,8 @@ def write_mhm_restart(path, mask: np.ndarray, states: dict[str, np.ndarray], par
         dim_of = {"scene": "L1_LandCoverPeriods", "horizon": "L1_SoilHorizons", "lai": "L1_LAITimesteps"}
         for var, (name, dims) in EFF_PARAMS.items():
             if any(name not in p or p[name] is None for p in params_by_scene):
+                continue
+            if keep is not None and var in PROCESS_DEPENDENT and var not in keep:
                 continue
             if dims and dims[0] == "scene":
                 cells = np.stack([np.asarray(p[name], np.float64) for p in params_by_scene])

@@ -156,6 +156,7 @@ def main():
         l11_l1_id=mrm.read("L11_L1_Id")[mask11].astype(np.int32),
         l1_area_km2=mrm.read("L1_domain_cellarea")[mask1], l11_area_km2=mrm.read("L11_domain_cellarea")[mask11],
         latitude=mrm.read("L1_domain_lat")[mask1],
+        gold_restart_vars=np.array(sorted(mhm.group())),
         evap_coeff=np.array(EVAP_COEFF), fnight_pet=np.array(FNIGHT_PET), fnight_prec=np.array(FNIGHT_PREC),
         fnight_temp=np.array(FNIGHT_TEMP), gold_q_daily=q[:, 5], gold_q_dmy=q[:, 1:4].astype(np.int32),
         gold_q_obs=q[:, 4], gold_gauge_id=int(qtext.split()[4][5:]),
@@ -211,6 +212,7 @@ def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
         extra = dict(length=mrm.read("L11_length")[:n_links], ts_rout=float(mrm.read("L11_TSrout")[0]))
     np.savez_compressed(HERE / f"{case.replace('_', '')}_gold.npz", gamma=np.array(gamma), proc_sm=proc_sm,
                         proc_pet=proc_pet, proc_rout=proc_rout, q_daily=q[:, 5], **gold, **extra,
+                        restart_vars=np.array(sorted(names)),
                         **output_golds(cdir, mask1))
     print("wrote", HERE / f"{case.replace('_', '')}_gold.npz", len(gamma), sorted(gold))
 

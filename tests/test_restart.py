@@ -139,3 +139,28 @@ def test_gpu_run_from_case00_restart(tmp_path):
     assert np.array_equal(st["Qmod"], o.state["Qmod"])
     # the restart's soil moisture was used: step 1 did not reset it to 0.5 FC
     assert not np.array_equal(mhm.states["soilMoist"], 0.5 * mhm.eff_params(1)["soilMoistFC"])
+
+
+@pytest.mark.parametrize("case", list(run_case.CASES))
+def test_restart_parameter_set_of_the_check_cases(case, tmp_path):
+    """With the process cases given, the writer emits the effective
+    parameters the reference's restart of that check case holds: no more,
+    no fewer (the process-dependent ones: Jarvis threshold, LAI/aspect
+    factors, Hargreaves-Samani coefficient, Priestley-Taylor alpha)."""
+    gamma, (proc_sm, proc_pet, proc_rout), _ = run_case.case_setup(case)
+    z = np.load(run_case.FIX if case == "case_00" else run_case.GOLD_DIR / f"{case.replace('_', '')}_gold.npz")
+    ref_vars = {str(v) for v in z["gold_restart_vars" if case == "case_00" else "restart_vars"]}
+    p, _ = run_case.regionalised("hmath", gamma, proc_sm, proc_pet, proc_rout)
+    n, H = p[0]["fSealed"].size, run_case.H
+    names = {"jarvis_c1": "jarvis_thresh_c1", "SMs": "soilMoistSat", "FC": "soilMoistFC", "PW": "wiltingPoint",
+             "beta": "soilMoistExp"}
+    scenes = [{names.get(k, k): v for k, v in q.items()} for q in p]
+    states = {k: np.zeros(n) for k in ("interc", "snowpack", "sealSTW", "unsatSTW", "satSTW")}
+    states["soilMoist"] = np.zeros(H * n)
+    path = tmp_path / "r.nc"
+    restart.write_mhm_restart(path, np.ones((n, 1), bool), states, scenes, np.array([200.0, 1000.0]),
+                              proc_sm=proc_sm, proc_pet=proc_pet)
+    from scipy.io import netcdf_file
+    with netcdf_file(str(path), "r", mmap=False) as f:
+        ours = set(f.variables)
+    assert ours & set(restart.EFF_PARAMS) == ref_vars & set(restart.EFF_PARAMS), case
