@@ -147,6 +147,17 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
  * mhm_mpr computes C1/C2 with it. */
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp);
 
+/* read_meteo_weights = .true.: daily forcing is spread over the day with
+ * hourly weights instead of the day/night ratios (temporal_disagg_meteo_weights,
+ * src/meteo/mo_meteo_temporal_tools.f90:32-50, called from
+ * src/meteo/mo_meteo_handler.f90:1102-1107, 1183-1189, 1265-1270):
+ * x = (x_day + c) * w(cell, month, hour) - c with c = 273.15 K for the
+ * temperature and 0 otherwise.  Each array is L1_{pre,pet,temp}_weights
+ * (cell, month, hour) in the reference's column-major order, i.e.
+ * [24][12][n_cells]; the three together, or all NULL to return to the
+ * day/night ratios.  Hourly forcing ignores them, as the reference does. */
+int mhm_set_meteo_weights(mhm_ctx *ctx, const double *pre_w, const double *pet_w, const double *temp_w);
+
 /* Muskingum coefficients C1/C2 of `member` from the five routing parameters
  * (reg_rout, src/mRM/mo_mrm_mpr.f90:61-119; evaluated on the device).  With
  * routing case 2 rout_param5[0] is the streamflow celerity [m s-1]

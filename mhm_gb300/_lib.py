@@ -95,7 +95,7 @@ EXPORTS = [
     "mhm_enable_fluxes", "mhm_get_fluxes", "mhm_set_link_fpimp",
     "mhm_enable_flux_state_outputs", "mhm_read_flux_state_outputs", "mhm_enable_routed_outputs",
     "mhm_read_routed_outputs", "mhm_set_output_weights", "mhm_set_link_celerity", "mhm_network_topology",
-    "mhm_poll",
+    "mhm_poll", "mhm_set_meteo_weights",
 ]
 
 _LIB = None
@@ -159,6 +159,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_autotune.argtypes = [vp, C.c_int32, C.c_int32, _ip, _ip, _dp]
     L.mhm_enable_fluxes.argtypes = [vp, C.c_int32]
     L.mhm_set_link_fpimp.argtypes = [vp, _dp]
+    L.mhm_set_meteo_weights.argtypes = [vp, _dp, _dp, _dp]
     L.mhm_get_fluxes.argtypes = [vp, _dp, _dp]
     L.mhm_snapshot_save.argtypes = [vp, C.c_int32, C.c_int32]
     i64p = C.POINTER(C.c_int64)

@@ -21,6 +21,7 @@ __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32
     si.month = (int8_t)sd.month;
     si.dflags = (int8_t)step_dflags(jul_start, timestep, tt);
     si.doy = (int16_t)sd.doy;
+    si.hour = (int8_t)sd.hour;
     steps[i] = si;
 }
 

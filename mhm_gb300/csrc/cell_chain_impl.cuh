@@ -36,6 +36,7 @@ constexpr double kHarSamConst = 17.800;
 // src/common/mo_constants.f90 (Psychro_dp) and src/mHM/mo_mhm_constants.f90 (tetens_c*, satpressureslope1)
 constexpr double kPsychro = 0.0646, kTetensC1 = 0.6108, kTetensC2 = 17.270, kTetensC3 = 237.30;
 constexpr double kSatPressureSlope1 = 4098.0;
+constexpr double kT0 = 273.15; // FORCES mo_constants T0_dp (Celsius <-> Kelvin)
 
 // src/mHM/mo_pet.f90:314-355 (CUDA's sin/cos/tan/acos; only the daily-forcing
 // Hargreaves variant uses it)
@@ -247,6 +248,14 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             pet = pv;
             temp = __ldg(a.temp + f);
             prec = __ldg(a.pre + f);
+        } else if (a.w_pet) {
+            // temporal_disagg_meteo_weights (mo_meteo_temporal_tools.f90:32-50) with
+            // L1_*_weights(k, month, hour + 1), mo_meteo_handler.f90:1102-1107, 1183-1189,
+            // 1265-1270; temperature corrected by T0 = 273.15 K
+            const size_t wi = ((size_t)si.hour * 12 + (size_t)(month - 1)) * N + k;
+            pet = (pv + 0.0) * __ldg(a.w_pet + wi) - 0.0;
+            temp = (__ldg(a.temp + f) + kT0) * __ldg(a.w_temp + wi) - kT0;
+            prec = (__ldg(a.pre + f) + 0.0) * __ldg(a.w_pre + wi) - 0.0;
         } else { // temporal_disagg_*_daynight, mo_meteo_temporal_tools.f90:66-161
             const int mi = month - 1;
             const double nd = a.nTstepDay;

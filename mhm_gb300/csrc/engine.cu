@@ -195,6 +195,9 @@ struct mhm_ctx {
     int32_t n_snap = 0;
     // multiscale parameter regionalisation (after mhm_mpr_setup)
     bool mpr_ready = false;
+    // read_meteo_weights: [3][24][12][N] (pre, pet, temp)
+    DevBuf<double> meteo_w;
+    bool meteo_w_on = false;
     MprSetup mpr;
     DevBuf<int32_t> mpr_nhor, mpr_ntill, mpr_nsub;
     DevBuf<uint32_t> mpr_code;
@@ -742,6 +745,27 @@ int mhm_set_link_celerity(mhm_ctx *ctx, int32_t m, const double *celerity)
     return set_adaptive_member(ctx, m, 0.0, celerity);
 }
 
+int mhm_set_meteo_weights(mhm_ctx *ctx, const double *pre_w, const double *pet_w, const double *temp_w)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the old weights
+    if (!pre_w && !pet_w && !temp_w) {
+        ctx->meteo_w_on = false;
+        return MHM_OK;
+    }
+    if (!pre_w || !pet_w || !temp_w)
+        return fail(ctx, MHM_ERR_INVALID, "meteo weights come as pre, pet and temp together");
+    const size_t n = (size_t)24 * 12 * ctx->N;
+    CK(ctx->meteo_w.ensure(3 * n), "meteo weights");
+    const double *src[3] = {pre_w, pet_w, temp_w};
+    for (int i = 0; i < 3; ++i)
+        CK(cudaMemcpyAsync(ctx->meteo_w.p + i * n, src[i], n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+           "meteo weights");
+    CK(cudaStreamSynchronize(ctx->stream), "meteo weights sync");
+    ctx->meteo_w_on = true;
+    return MHM_OK;
+}
+
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 {
     if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
@@ -1107,6 +1131,12 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.tmin = fp[3];
         a.tmax = fp[4];
         a.netrad = fp[5];
+        if (ctx->meteo_w_on) {
+            const size_t wn = (size_t)24 * 12 * N;
+            a.w_pre = ctx->meteo_w.p;
+            a.w_pet = ctx->meteo_w.p + wn;
+            a.w_temp = ctx->meteo_w.p + 2 * wn;
+        }
         a.steps = ctx->steps.p;
         if (members) {
             a.steps = ctx->steps_all.p;

@@ -45,6 +45,7 @@ struct StepInfo {
     int8_t month;
     int8_t dflags;  // SF_ISDAY: 6 < hour <= 18; SF_*_END: the next step starts a new day / month / year
     int16_t doy;
+    int8_t hour;    // 0..23, the hour index of the meteo weights
 };
 
 // Aggregated flux/state outputs (outputFlxState of mhm_outputs.nml), indexes
@@ -102,6 +103,9 @@ struct CellArgs {
     double nTstepDay;   // 24 / timestep
     const double *pre, *temp, *pet, *tmin, *tmax; // [rows][n_cells] from row_base
     const double *netrad;                         // [rows][n_cells] (proc_pet 2) or null
+    // read_meteo_weights: L1_{pre,pet,temp}_weights(cell, month, hour) as
+    // [24][12][n_cells] (the reference's column-major order); null: day/night ratios
+    const double *w_pre, *w_pet, *w_temp;
     const StepInfo *steps;                        // [n_steps]
     const double *params;                         // [M][planes][n_cells]
     double *states;                               // [M][planes][n_cells]

@@ -136,6 +136,16 @@ class MhmGpu:
         a = np.ascontiguousarray(celerity, np.float64)
         self._check(self.L.mhm_set_link_celerity(self.ctx, member, _d(a)), "mhm_set_link_celerity")
 
+    def set_meteo_weights(self, pre=None, pet=None, temp=None):
+        """read_meteo_weights: hourly weights [24][12][n_cells] (the reference's
+        L1_*_weights(cell, month, hour)) for pre, pet and temp; all None returns
+        to the day/night ratios."""
+        if pre is None and pet is None and temp is None:
+            self._check(self.L.mhm_set_meteo_weights(self.ctx, None, None, None), "mhm_set_meteo_weights")
+            return
+        w = [np.ascontiguousarray(a, np.float64) for a in (pre, pet, temp)]
+        self._check(self.L.mhm_set_meteo_weights(self.ctx, *[_d(a) for a in w]), "mhm_set_meteo_weights")
+
     def set_link_fpimp(self, ffp):
         """Floodplain impervious fraction of the links for a new land-cover scene."""
         a = np.ascontiguousarray(ffp, np.float64)

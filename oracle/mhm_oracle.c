@@ -42,6 +42,7 @@ static const double DEG2RAD_DP = 3.141592653589793238462643383279502884197 / 180
 static const double PSYCHRO_DP = 0.0646;
 static const double RHO0_DP = 1.225;
 static const double CP0_DP = 1005.0;
+static const double T0_DP = 273.15; /* FORCES mo_constants T0_dp: Celsius <-> Kelvin */
 /* src/mHM/mo_mhm_constants.f90 */
 static const double DUFFIE_DR = 0.0330;
 static const double DUFFIE_DELTA1 = 0.4090;
@@ -950,6 +951,14 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
                 pet_k = pv;
                 temp_k = tmp[k];
                 prec_k = pre[k];
+            } else if (d->pet_w) {
+                /* temporal_disagg_meteo_weights with L1_*_weights(k, month, hour + 1),
+                 * src/meteo/mo_meteo_handler.f90:1102-1107, 1183-1189, 1265-1270;
+                 * temperature corrected by T0 = 273.15 K */
+                const size_t wi = ((size_t)hour * 12 + (size_t)(month - 1)) * N + k;
+                pet_k = ora_disagg_meteo_weights(pv, d->pet_w[wi], 0.0);
+                temp_k = ora_disagg_meteo_weights(tmp[k], d->temp_w[wi], T0_DP);
+                prec_k = ora_disagg_meteo_weights(pre[k], d->pre_w[wi], 0.0);
             } else {
                 pet_k = ora_disagg_flux_daynight(isday, nTstepDay_dp, pv, d->fday_pet[month - 1],
                                                  d->fnight_pet[month - 1]);

@@ -134,6 +134,9 @@ typedef struct {
     const int32_t *gauge_node;                /* [nGauges] */
     const double *latitude;                   /* [nCells] degrees */
     const double *link_celerity;              /* [nLinks] L11_celerity (routing case 3) */
+    /* read_meteo_weights: hourly weights L1_{pre,pet,temp}_weights(cell, month, hour),
+     * [24][12][nCells]; NULL: day/night ratios */
+    const double *pre_w, *pet_w, *temp_w;
 } ora_domain;
 
 typedef struct {

@@ -36,6 +36,7 @@ class OraDomain(C.Structure):
         ("l1_area_km2", _dp), ("l1_l11_id", _ip), ("l11_area_km2", _dp), ("l11_l1_id", _ip),
         ("net_perm", _ip), ("from_n", _ip), ("to_n", _ip), ("length", _dp), ("slope", _dp),
         ("ffp_imp", _dp), ("rout_param", _dp), ("gauge_node", _ip), ("latitude", _dp), ("link_celerity", _dp),
+        ("pre_w", _dp), ("pet_w", _dp), ("temp_w", _dp),
     ]
 
 
@@ -194,7 +195,7 @@ class OracleRun:
     """The mhm_eval time loop of one basin on the CPU (oracle)."""
 
     def __init__(self, dom, params: dict, rout_param=None, proc_sm=1, proc_pet=0, proc_rout=1,
-                 hourly=True, read_states=False, kind="hmath", link_celerity=None):
+                 hourly=True, read_states=False, kind="hmath", link_celerity=None, meteo_weights=None):
         self.L = load(kind)
         self.dom = dom
         self.keep = []
@@ -221,6 +222,9 @@ class OracleRun:
         d.rout_param = _d(rp)
         if link_celerity is not None:
             d.link_celerity = _d(k(link_celerity))
+        if meteo_weights is not None:   # {"pre", "pet", "temp"}: [24][12][n_cells] each
+            for n in ("pre", "pet", "temp"):
+                setattr(d, n + "_w", _d(k(meteo_weights[n])))
         self.d = d
         p = OraParams()
         for name, arr in params.items():
