@@ -910,6 +910,8 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
         const double *tmin = f->tmin ? f->tmin + (size_t)row * N : NULL;
         const double *tmax = f->tmax ? f->tmax + (size_t)row * N : NULL;
         const double *netrad = f->netrad ? f->netrad + (size_t)row * N : NULL;
+        const double *eabs = f->eabs ? f->eabs + (size_t)row * N : NULL;
+        const double *wind = f->windspeed ? f->windspeed + (size_t)row * N : NULL;
         const double evap_coeff = d->evap_coeff[month - 1];
         const int iLAI = month; /* timeStep_LAI_input = 0 (mo_common_datetime_type.f90:135-155) */
         /* this step's outputs (write_output after do_time_step) */
@@ -940,6 +942,11 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
             case 2: /* Priestley-Taylor, not defined for netrad < 0 (mo_meteo_handler.f90:1079-1084) */
                 pv = ora_pet_priestly(p->PrieTayAlpha[(size_t)(iLAI - 1) * N + k],
                                       netrad[k] > 0.0 ? netrad[k] : 0.0, tmp[k]);
+                break;
+            case 3: /* Penman-Monteith, mo_meteo_handler.f90:1087-1095 */
+                pv = ora_pet_penman(netrad[k] > 0.0 ? netrad[k] : 0.0, tmp[k], eabs[k] / 1000.0,
+                                    p->aeroResist[(size_t)(iLAI - 1) * N + k] / wind[k],
+                                    p->surfResist[(size_t)(iLAI - 1) * N + k], 1.0, 1.0);
                 break;
             default:
                 pv = p->fAsp[k] * ora_pet_hargreaves(p->HarSamCoeff[k], HARSAMCONST, tmp[k], tmax[k],

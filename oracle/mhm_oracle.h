@@ -147,6 +147,7 @@ typedef struct {
     const double *petLAIcorFactor; /* [12][nCells] or NULL */
     const double *fRoots, *SMs, *FC, *PW, *beta; /* [nH][nCells] */
     const double *PrieTayAlpha;    /* [12][nCells] Priestley-Taylor alpha (proc_pet 2) or NULL */
+    const double *aeroResist, *surfResist; /* [12][nCells] Penman-Monteith resistances (proc_pet 3) or NULL */
 } ora_params;
 
 typedef struct {
@@ -164,7 +165,8 @@ typedef struct {
     const double *pre, *temp, *pet, *tmin, *tmax;
     int32_t forc_row0;
     int32_t n_rows;
-    const double *netrad; /* net radiation [W m-2] (proc_pet 2) or NULL */
+    const double *netrad; /* net radiation [W m-2] (proc_pet 2, 3) or NULL */
+    const double *eabs, *windspeed; /* absolute vapour pressure [Pa], wind speed [m s-1] (proc_pet 3) */
 } ora_forcing;
 
 /* Aggregated outputs of the run (mhm_interface_run_write_output,
@@ -264,6 +266,7 @@ typedef struct {
     double *maxInter, *petLAIcorFactor;
     double *fRoots, *SMs, *FC, *PW, *beta;
     double *PrieTayAlpha; /* [12][nCells1] (proc_pet 2) or NULL */
+    double *aeroResist, *surfResist; /* [12][nCells1] (proc_pet 3) or NULL */
 } ora_mpr_out;
 
 int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o);

@@ -375,6 +375,61 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->fAsp[k] = 0.0;
             o->HarSamCoeff[k] = 0.0;
         }
+    } else if (d->proc_pet == 3) {
+        /* ---- Penman-Monteith resistances per LAI month: aerodynamical_resistance
+         * (src/MPR/mo_multi_param_reg.f90:1165-1262, parameters 1-6) and
+         * bulksurface_resistance (src/MPR/mo_mpr_pet.f90:407-475, parameter 7),
+         * each the arithmetic block mean of its L0 field ---- */
+        const double *p = g->pet;
+        const double zm_meas = 10.0, karman = 0.41; /* WindMeasHeight, karman (mo_mpr_constants.f90:65-67) */
+        const double nodata = -9999.0;
+        double *hc0 = (double *)malloc((size_t)N0 * sizeof(double));
+        double *maxlai = (double *)malloc((size_t)N0 * sizeof(double));
+        if (!hc0 || !maxlai) {
+            free(hc0);
+            free(maxlai);
+            rc = -2;
+            goto done;
+        }
+        for (int k = 0; k < N0; ++k) {
+            const int lc = d->LCover0[k];
+            hc0[k] = lc == 1 ? p[0] : (lc == 2 ? p[1] : nodata); /* forest, impervious */
+            double mx = d->LAI0[k];                                  /* MAXVAL(LAI0, dim=2) */
+            for (int m = 1; m < 12; ++m)
+                if (d->LAI0[(size_t)m * N0 + k] > mx) mx = d->LAI0[(size_t)m * N0 + k];
+            maxlai[k] = mx;
+        }
+        for (int m = 0; m < 12; ++m) {
+            for (int k = 0; k < N0; ++k) {
+                const double lai = d->LAI0[(size_t)m * N0 + k];
+                if (d->LCover0[k] == 3) hc0[k] = p[2] * lai / maxlai[k]; /* pervious: the month's LAI */
+                double zm = zm_meas;
+                if (fabs(zm - nodata) > DBL_EPSILON && zm < hc0[k]) zm = hc0[k] + zm;
+                const double displace = p[3] * hc0[k];
+                const double zm_zero = p[4] * hc0[k];
+                const double zh_zero = p[5] * zm_zero;
+                tmp0[k] = ORA_LOG((zm - displace) / zm_zero) * ORA_LOG((zm - displace) / zh_zero) /
+                          (karman * karman);
+            }
+            for (int k = 0; k < N1; ++k)
+                o->aeroResist[(size_t)m * N1 + k] = upscale_arith(d, k, tmp0);
+            for (int k = 0; k < N0; ++k) {
+                const double lai = d->LAI0[(size_t)m * N0 + k];
+                double r = p[6] / (lai / (0.3 * lai + 1.2)); /* LAI_factor/offset_surfResi */
+                tmp0[k] = r > 250.0 ? 250.0 : r;             /* max_surfResist */
+            }
+            for (int k = 0; k < N1; ++k)
+                o->surfResist[(size_t)m * N1 + k] = upscale_arith(d, k, tmp0);
+        }
+        free(hc0);
+        free(maxlai);
+        for (int k = 0; k < N1; ++k) {
+            o->fAsp[k] = 0.0;
+            o->HarSamCoeff[k] = 0.0;
+        }
+        if (o->petLAIcorFactor)
+            for (size_t i = 0; i < (size_t)12 * N1; ++i)
+                o->petLAIcorFactor[i] = 0.0;
     } else if (d->proc_pet == 2) {
         /* ---- Priestley-Taylor alpha, src/MPR/mo_mpr_pet.f90:311-369: arithmetic
          * block mean of alpha0 = p1 + p2 * LAI0 per LAI month ---- */

@@ -43,7 +43,7 @@ class OraDomain(C.Structure):
 PARAM_FIELDS = ["fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "HarSamCoeff",
                 "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco", "jarvis_c1", "tempThresh",
                 "unsatThresh", "sealedThresh", "maxInter", "petLAIcorFactor", "fRoots", "SMs", "FC", "PW",
-                "beta", "PrieTayAlpha"]
+                "beta", "PrieTayAlpha", "aeroResist", "surfResist"]
 # mhm_eff_params name -> oracle name
 PARAM_ALIAS = {"jarvis_thresh_c1": "jarvis_c1", "soilMoistSat": "SMs", "soilMoistFC": "FC",
                "wiltingPoint": "PW", "soilMoistExp": "beta"}
@@ -63,7 +63,8 @@ class OraState(C.Structure):
 
 class OraForcing(C.Structure):
     _fields_ = [("pre", _dp), ("temp", _dp), ("pet", _dp), ("tmin", _dp), ("tmax", _dp),
-                ("forc_row0", C.c_int32), ("n_rows", C.c_int32), ("netrad", _dp)]
+                ("forc_row0", C.c_int32), ("n_rows", C.c_int32), ("netrad", _dp), ("eabs", _dp),
+                ("windspeed", _dp)]
 
 
 class OraOutput(C.Structure):
@@ -98,7 +99,7 @@ class OraGamma(C.Structure):
 MPR_OUT_FIELDS = ["fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "HarSamCoeff",
                   "karstLoss", "kFastFlow", "kSlowFlow", "kBaseFlow", "kPerco", "jarvis_c1", "tempThresh",
                   "unsatThresh", "sealedThresh", "maxInter", "petLAIcorFactor", "fRoots", "SMs", "FC", "PW",
-                  "beta", "PrieTayAlpha"]
+                  "beta", "PrieTayAlpha", "aeroResist", "surfResist"]
 
 
 class OraMprOut(C.Structure):
@@ -286,7 +287,7 @@ class OracleRun:
             want_tro: bool = False, want_qmod: bool = False):
         f = OraForcing()
         keep = []
-        for n in ("pre", "temp", "pet", "tmin", "tmax", "netrad"):
+        for n in ("pre", "temp", "pet", "tmin", "tmax", "netrad", "eabs", "windspeed"):
             a = forcing.get(n)
             if a is not None:
                 a = np.ascontiguousarray(a, np.float64)
@@ -365,7 +366,8 @@ def oracle_mpr(n1: int, H: int, l0, gamma: np.ndarray, offsets, proc_sm: int = 1
         setattr(gm, n, C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[i])), _dp))
     gm.geo = C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[8])), _dp)
     sizes = {"maxInter": 12 * n1, "petLAIcorFactor": 12 * n1, "fRoots": H * n1, "SMs": H * n1, "FC": H * n1,
-             "PW": H * n1, "beta": H * n1, "PrieTayAlpha": 12 * n1}
+             "PW": H * n1, "beta": H * n1, "PrieTayAlpha": 12 * n1, "aeroResist": 12 * n1,
+             "surfResist": 12 * n1}
     out = {n: np.zeros(sizes.get(n, n1)) for n in MPR_OUT_FIELDS}
     o = OraMprOut(**{n: _d(out[n]) for n in MPR_OUT_FIELDS})
     rc = L.ora_mpr(C.byref(d), C.byref(gm), C.byref(o))

@@ -121,6 +121,12 @@ def main():
     a, t = f.read("net_rad"), f.read("time")
     o = int(np.nonzero(t == julday(*SIM_START) - julday(1984, 1, 2))[0][0])
     met["netrad"] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
+    # daily absolute vapour pressure and wind speed (Penman-Monteith PET), each on its own time axis
+    for key, base in (("eabs", (1983, 12, 31)), ("windspeed", (1984, 1, 1))):
+        f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
+        a, t = f.read(key), f.read("time")
+        o = int(np.nonzero(t == julday(*SIM_START) - julday(*base))[0][0])
+        met[key] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
     # daily minimum / maximum temperature (Hargreaves-Samani PET): days since 1933-12-31
     for key in ("tmin", "tmax"):
         f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
@@ -144,6 +150,7 @@ def main():
     np.savez_compressed(
         HERE / "case00_run.npz",
         pre=met["pre"], temp=met["temp"], pet=met["pet"], tmin=met["tmin"], tmax=met["tmax"], netrad=met["netrad"],
+        eabs=met["eabs"], windspeed=met["windspeed"],
         jul_start=julday(*SIM_START), sim_days=SIM_DAYS,
         warming_days=WARMING_DAYS, scene2_from_day=SCENE2_FROM_DAY,
         from_n=mrm.read("L11_fromN").astype(np.int32), to_n=mrm.read("L11_toN").astype(np.int32),
@@ -169,7 +176,8 @@ def main():
 import make_case00_mpr as mpr_fix  # noqa: E402
 
 # processCase(3), processCase(5), processCase(8)
-CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2), "case_02": (2, 2, 0)}
+CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2), "case_02": (2, 2, 0),
+         "case_03": (1, 3, 1)}
 PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "karstLoss", "kfastFlow",
                "kSlowFlow", "kBaseFlow", "kPerco", "tempThresh", "unsatThresh", "sealedThresh", "maxInter",
                "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "petLAIcorFactor",
@@ -179,9 +187,11 @@ PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAs
 def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
     cdir = REF / "check" / case
     mrm = h5lite.H5File(str(cdir / "output_save" / "b1_mRM_restart_001.nc")) if proc_rout else None
-    mhm = h5lite.H5File(str(cdir / "output_save" / "b1_mHM_restart_001.nc"))
-    mask1 = mhm.read("L1_domain_mask").astype(bool)
-    names = mhm.group()
+    # an optimisation run (case_03) writes no mHM restart
+    mfile = cdir / "output_save" / "b1_mHM_restart_001.nc"
+    mhm = h5lite.H5File(str(mfile)) if mfile.exists() else None
+    mask1 = (mhm or mrm).read("L1_domain_mask").astype(bool)
+    names = list(mhm.group()) if mhm else []
     gold = {}
     for name in PARAM_NAMES:
         if "L1_" + name not in names:
@@ -192,18 +202,28 @@ def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
         else:   # leading dims: [scene][(horizon|month)] then the grid
             lead = a.shape[:-2]
             gold["p_" + name] = a.reshape(-1, *a.shape[-2:])[:, mask1].reshape(*lead, -1)
-    for name in ("L1_Inter", "L1_snowPack", "L1_sealSTW", "L1_unsatSTW", "L1_satSTW"):
+    for name in ("L1_Inter", "L1_snowPack", "L1_sealSTW", "L1_unsatSTW", "L1_satSTW") if mhm else ():
         gold["s_" + name] = mhm.read(name)[mask1]
-    sm = mhm.read("L1_soilMoist")
-    gold["s_L1_soilMoist"] = np.stack([sm[h][mask1] for h in range(sm.shape[0])])
+    if mhm:
+        sm = mhm.read("L1_soilMoist")
+        gold["s_L1_soilMoist"] = np.stack([sm[h][mask1] for h in range(sm.shape[0])])
     for name in ("L11_qOUT", "L11_Qmod", "L11_C1", "L11_C2") if mrm else ():
         gold["s_" + name] = mrm.read(name)[mask1]
     q = np.loadtxt(cdir / "output_save" / "b1_daily_discharge.out", skiprows=1) if mrm else np.zeros((0, 6))
     blocks = ["interception1", "snow1", f"soilmoisture{proc_sm}", "directRunoff1",
-              {-1: "PETminus1", 0: "PET0", 1: "PET1", 2: "PET2"}[proc_pet], "interflow1", "percolation1"]
+              {-1: "PETminus1", 0: "PET0", 1: "PET1", 2: "PET2", 3: "PET3"}[proc_pet], "interflow1",
+              "percolation1"]
     blocks += [f"routing{proc_rout}"] if proc_rout else []
     blocks += ["geoparameter"]
     gamma = mpr_fix.namelist_values(cdir / "mhm_parameter.nml", blocks)
+    dds = cdir / "output_save" / "dds_results.out"
+    if dds.exists():
+        # an optimisation: the outputs are those of the last evaluation, which is the
+        # best one when the last DDS line improved (its 17 digits give the doubles exactly)
+        rows = [ln.split() for ln in dds.read_text().splitlines() if ln.strip() and not ln.lstrip().startswith("#")]
+        rows = [r for r in rows if len(r) == len(gamma) + 2]
+        assert float(rows[-1][1]) < float(rows[-2][1]), "the last evaluation is not the best"
+        gamma = [float(x) for x in rows[-1][2:]]
     extra = {}
     if proc_rout == 2:
         # link lengths as mRM sets them up for adaptive routing (cut at their 40th

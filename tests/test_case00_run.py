@@ -48,7 +48,7 @@ def load_run():
             ffp_imp=np.ascontiguousarray(z["ffp_imp"][scene]), gauge_node=z["gauge_node"], latitude=z["latitude"],
             horizon_depth=np.array([200.0, 1000.0])))
     forcing = {"pre": z["pre"], "temp": z["temp"], "pet": z["pet"], "tmin": z["tmin"], "tmax": z["tmax"],
-               "netrad": z["netrad"]}
+               "netrad": z["netrad"], "eabs": z["eabs"], "windspeed": z["windspeed"]}
     return z, doms, forcing
 
 
@@ -76,7 +76,10 @@ SCENE_INDEPENDENT = ("unsatThresh", "karstLoss", "sealedThresh", "jarvis_thresh_
 GOLD_DIR = Path(__file__).resolve().parent / "golden"
 # check case -> (processCase(3), processCase(5), processCase(8)); all on the test_domain inputs
 CASES = {"case_00": (1, 0, 1), "case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2),
-         "case_02": (2, 2, 0)}
+         "case_02": (2, 2, 0), "case_03": (1, 3, 1)}
+# case_03 is an optimisation (DDS): it writes the discharge and the mRM restart of its
+# last (here also best) evaluation, but no flux/state file and no mHM restart
+OUTPUT_CASES = [c for c in CASES if c != "case_03"]
 
 
 def case_setup(case):
@@ -116,8 +119,10 @@ def regionalised(kind, gamma, proc_sm=1, proc_pet=0, proc_rout=1):
 def check_states(g, st, rtol=0.0):
     gold = {"qOUT": g["s_L11_qOUT"], "Qmod": g["s_L11_Qmod"],
             "C1": g["s_L11_C1"][:-1], "C2": g["s_L11_C2"][:-1]} if "s_L11_qOUT" in g else {}
-    gold.update(interc=g["s_L1_Inter"], snowpack=g["s_L1_snowPack"], sealSTW=g["s_L1_sealSTW"],
-                unsatSTW=g["s_L1_unsatSTW"], satSTW=g["s_L1_satSTW"], soilMoist=g["s_L1_soilMoist"].reshape(-1))
+    if "s_L1_Inter" in g:   # an optimisation run (case_03) writes no mHM restart
+        gold.update(interc=g["s_L1_Inter"], snowpack=g["s_L1_snowPack"], sealSTW=g["s_L1_sealSTW"],
+                    unsatSTW=g["s_L1_unsatSTW"], satSTW=g["s_L1_satSTW"],
+                    soilMoist=g["s_L1_soilMoist"].reshape(-1))
     bad = {}
     for k, want in gold.items():
         got = np.asarray(st[k]).reshape(-1)[: want.size]
@@ -197,7 +202,7 @@ def output_golds(case):
 
 
 @pytest.mark.parametrize("kind", ["libm", "hmath"])
-@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("case", OUTPUT_CASES)
 def test_oracle_reproduces_case_outputs(case, kind):
     """b1_mHM_Fluxes_States.nc (SWC, Q, PET, aET, recharge over the evaluation
     year) and b1_mRM_Fluxes_States.nc (Qrouted, daily means or the year's
@@ -240,7 +245,7 @@ def test_oracle_reproduces_case_outputs(case, kind):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("case", [c for c in CASES if c != "case_03"])
 def test_gpu_reproduces_case_discharge_and_states(case):
     from mhm_gb300.model import MhmGpu
     z, doms, forcing = load_run()
@@ -294,7 +299,7 @@ def test_gpu_reproduces_case_discharge_and_states(case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("case", OUTPUT_CASES)
 def test_gpu_reproduces_case_outputs(case):
     """The device's aggregated outputs against b1_mHM_Fluxes_States.nc and
     b1_mRM_Fluxes_States.nc."""

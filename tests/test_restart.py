@@ -141,7 +141,7 @@ def test_gpu_run_from_case00_restart(tmp_path):
     assert not np.array_equal(mhm.states["soilMoist"], 0.5 * mhm.eff_params(1)["soilMoistFC"])
 
 
-@pytest.mark.parametrize("case", list(run_case.CASES))
+@pytest.mark.parametrize("case", run_case.OUTPUT_CASES)
 def test_restart_parameter_set_of_the_check_cases(case, tmp_path):
     """With the process cases given, the writer emits the effective
     parameters the reference's restart of that check case holds: no more,
