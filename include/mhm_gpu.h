@@ -51,7 +51,9 @@ extern "C" {
 #define MHM_FORC_PET 2
 #define MHM_FORC_TMIN 3
 #define MHM_FORC_TMAX 4
-#define MHM_FORC_NETRAD 5 /* L1_netrad [W m-2], Priestley-Taylor PET (proc_pet = 2) */
+#define MHM_FORC_NETRAD 5    /* L1_netrad [W m-2] (proc_pet = 2, 3)                   */
+#define MHM_FORC_EABS 6      /* L1_absvappress [Pa], Penman-Monteith PET (proc_pet = 3) */
+#define MHM_FORC_WINDSPEED 7 /* L1_windspeed [m s-1] (proc_pet = 3)                   */
 
 typedef struct mhm_ctx mhm_ctx;
 
@@ -66,7 +68,7 @@ typedef struct {
     int32_t n_outlets;           /* L11_nOutlets                               */
     int32_t timestep;            /* model time step [h] (mhm.nml timestep)     */
     int32_t proc_soilmoist;      /* processMatrix(3,1): 1..4                   */
-    int32_t proc_pet;            /* processMatrix(5,1): -1, 0, 1 or 2          */
+    int32_t proc_pet;            /* processMatrix(5,1): -1, 0, 1, 2 or 3       */
     int32_t proc_routing;        /* processMatrix(8,1): 0, 1 (Muskingum), 2
                                     (Muskingum with a routing time step chosen
                                     from a constant celerity) or 3 (from each
@@ -109,6 +111,8 @@ typedef struct {
     const double *fRoots, *soilMoistSat, *soilMoistFC, *wiltingPoint, *soilMoistExp; /* [H * n_cells] */
     const double *PrieTayAlpha;    /* [12 * n_cells] or NULL (proc_pet = 2, L1_PrieTayAlpha); it shares
                                       the device planes of petLAIcorFactor, which is then not read back */
+    const double *aeroResist, *surfResist; /* [12 * n_cells] or NULL (proc_pet = 3, L1_aeroResist of
+                                              the scene and L1_surfResist); aeroResist shares those planes too */
 } mhm_eff_params;
 
 /* Restart state of one member: the fields of src/mHM/mo_restart.f90:146-258

@@ -19,7 +19,7 @@ MHM_ERR_TIMEOUT = -4
 MHM_ERR_NAN = -5
 MHM_ERR_UNSUPPORTED = -6
 
-FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX, FORC_NETRAD = range(6)
+FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX, FORC_NETRAD, FORC_EABS, FORC_WINDSPEED = range(8)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -46,6 +46,7 @@ EFF_PARAM_FIELDS = [
     "jarvis_thresh_c1", "tempThresh", "unsatThresh", "sealedThresh",
     "maxInter", "petLAIcorFactor",
     "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "PrieTayAlpha",
+    "aeroResist", "surfResist",
 ]
 
 

@@ -37,6 +37,7 @@ constexpr double kHarSamConst = 17.800;
 constexpr double kPsychro = 0.0646, kTetensC1 = 0.6108, kTetensC2 = 17.270, kTetensC3 = 237.30;
 constexpr double kSatPressureSlope1 = 4098.0;
 constexpr double kT0 = 273.15; // FORCES mo_constants T0_dp (Celsius <-> Kelvin)
+constexpr double kRho0 = 1.225, kCp0 = 1005.0; // air density, heat capacity (FORCES mo_constants)
 
 // src/mHM/mo_pet.f90:314-355 (CUDA's sin/cos/tan/acos; only the daily-forcing
 // Hargreaves variant uses it)
@@ -74,6 +75,16 @@ __device__ double pet_priestly(double alpha, double rn, double tavg)
     const double svp = kTetensC1 * hm_exp(kTetensC2 * tavg / (tavg + kTetensC3));
     const double delta = kSatPressureSlope1 * svp / hm_exp(2.0 * hm_log(tavg + kTetensC3));
     return alpha * delta / (kPsychro + delta) * (rn * kDaySecs / kSpecHeatET);
+}
+
+// src/mHM/mo_pet.f90:235-272 (pet_penman) with a_s = a_sh = 1, as the meteo
+// handler calls it (mo_meteo_handler.f90:1087-1095); the same operation order
+__device__ double pet_penman(double net_rad, double tavg, double act_vap, double ra, double rs)
+{
+    const double svp = kTetensC1 * hm_exp(kTetensC2 * tavg / (tavg + kTetensC3));
+    const double slope = kSatPressureSlope1 * svp / hm_exp(2.0 * hm_log(tavg + kTetensC3));
+    return kDaySecs / kSpecHeatET * (slope * net_rad + kRho0 * kCp0 * (svp - act_vap) * 1.0 / ra) /
+           (slope + kPsychro * 1.0 / 1.0 * (1.0 + rs / ra));
 }
 
 // Per-thread scalars live in registers; the per-horizon parameters and soil
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
     const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
     int cur_month = -1;
-    double imax = 0.0, petlai = 0.0, evap = 0.0;
+    double imax = 0.0, petlai = 0.0, petsurf = 0.0, evap = 0.0;
     uint64_t r_imax = 0, r_evap = 0;
     int cur_doy = -1;
     double rad = 0.0;
@@ -212,7 +223,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             evap = a.tab.evap[month - 1];
             r_evap = hm_recip_of(evap);
             // petLAIcorFactor (proc_pet -1) or PrieTayAlpha (proc_pet 2) of the LAI month
-            if (a.proc_pet == -1 || a.proc_pet == 2) petlai = par(P_PETLAI + month - 1);
+            if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = par(P_PETLAI + month - 1);
+            if (a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
         }
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
         // output weights: write_output runs after the calendar has advanced, so
@@ -236,6 +248,10 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         } else if (a.proc_pet == 2) { // Rn = max(L1_netrad, 0), src/meteo/mo_meteo_handler.f90:1080-1085
             const double rn = __ldg(a.netrad + f);
             pv = pet_priestly(petlai, rn > 0.0 ? rn : 0.0, __ldg(a.temp + f));
+        } else if (a.proc_pet == 3) { // aeroResist / wind speed, eabs in kPa, :1087-1095
+            const double rn = __ldg(a.netrad + f);
+            pv = pet_penman(rn > 0.0 ? rn : 0.0, __ldg(a.temp + f), __ldg(a.eabs + f) / 1000.0,
+                            petlai / __ldg(a.wind + f), petsurf);
         } else {
             if (si.doy != cur_doy) {
                 cur_doy = si.doy;

@@ -484,7 +484,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     if (d->n_members < 1) return bad("n_members < 1");
     if (d->timestep < 1 || 24 % d->timestep != 0) return bad("timestep must divide 24 hours");
     if (d->proc_soilmoist < 1 || d->proc_soilmoist > 4) return bad("proc_soilmoist must be 1..4");
-    if (d->proc_pet < -1 || d->proc_pet > 2) return bad("proc_pet must be -1, 0, 1 or 2 (3 unsupported)");
+    if (d->proc_pet < -1 || d->proc_pet > 3) return bad("proc_pet must be -1, 0, 1, 2 or 3");
     if (d->proc_routing < 0 || d->proc_routing > 3) return bad("proc_routing must be 0, 1, 2 or 3");
     if (d->n_tstep_forcing_day != 24 && d->n_tstep_forcing_day != 1)
         return bad("n_tstep_forcing_day must be 24 or 1");
@@ -717,13 +717,21 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
     CK(cudaMemcpyAsync(base + (size_t)P_MAXINTER * N, p->maxInter, 12 * N * sizeof(double),
                        cudaMemcpyHostToDevice, ctx->stream),
        "maxInter");
-    if (ctx->proc_pet == -1 || ctx->proc_pet == 2) { // the same planes hold either monthly factor
-        const double *monthly = ctx->proc_pet == -1 ? p->petLAIcorFactor : p->PrieTayAlpha;
-        if (!monthly) return fail(ctx, MHM_ERR_INVALID, ctx->proc_pet == -1 ? "petLAIcorFactor missing"
-                                                                              : "PrieTayAlpha missing");
+    if (ctx->proc_pet == -1 || ctx->proc_pet >= 2) { // the same planes hold the PET case's monthly field
+        const double *monthly = ctx->proc_pet == -1 ? p->petLAIcorFactor
+                                : ctx->proc_pet == 2 ? p->PrieTayAlpha
+                                                     : p->aeroResist;
+        if (!monthly) return fail(ctx, MHM_ERR_INVALID, "monthly PET parameter (petLAIcorFactor / PrieTayAlpha / "
+                                                        "aeroResist) missing");
         CK(cudaMemcpyAsync(base + (size_t)P_PETLAI * N, monthly, 12 * N * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream),
            "petLAI");
+    }
+    if (ctx->proc_pet == 3) {
+        if (!p->surfResist) return fail(ctx, MHM_ERR_INVALID, "surfResist missing");
+        CK(cudaMemcpyAsync(base + (size_t)P_PET2 * N, p->surfResist, 12 * N * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "surfResist");
     }
     const double *hz[5] = {p->fRoots, p->soilMoistSat, p->soilMoistFC, p->wiltingPoint, p->soilMoistExp};
     for (int g = 0; g < 5; ++g) {
@@ -795,8 +803,10 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
         int plane, n_planes;
     };
     const Part parts[] = {{p->maxInter, P_MAXINTER, 12},
-                          {ctx->proc_pet == 2 ? nullptr : p->petLAIcorFactor, P_PETLAI, 12},
+                          {ctx->proc_pet >= 2 ? nullptr : p->petLAIcorFactor, P_PETLAI, 12},
                           {ctx->proc_pet == 2 ? p->PrieTayAlpha : nullptr, P_PETLAI, 12},
+                          {ctx->proc_pet == 3 ? p->aeroResist : nullptr, P_PETLAI, 12},
+                          {ctx->proc_pet == 3 ? p->surfResist : nullptr, P_PET2, 12},
                           {p->fRoots, P_HORIZON, H},              {p->soilMoistSat, P_HORIZON + H, H},
                           {p->soilMoistFC, P_HORIZON + 2 * H, H}, {p->wiltingPoint, P_HORIZON + 3 * H, H},
                           {p->soilMoistExp, P_HORIZON + 4 * H, H}};
@@ -925,8 +935,14 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
     const int H = ctx->H;
     CK(cudaSetDevice(ctx->device), "set device");
-    const bool need[kForcKinds] = {true, true, ctx->proc_pet == 0 || ctx->proc_pet == -1, ctx->proc_pet == 1,
-                                   ctx->proc_pet == 1, ctx->proc_pet == 2};
+    const bool need[kForcKinds] = {true,
+                                   true,
+                                   ctx->proc_pet == 0 || ctx->proc_pet == -1,
+                                   ctx->proc_pet == 1,
+                                   ctx->proc_pet == 1,
+                                   ctx->proc_pet == 2 || ctx->proc_pet == 3,
+                                   ctx->proc_pet == 3,
+                                   ctx->proc_pet == 3};
     const int32_t stride = (int32_t)std::lround(24.0 / (double)ctx->ntfd);
     const bool members = member_tt0 != nullptr;
     if (members && (stride != 1 || ctx->ntfd != 24))
@@ -1112,7 +1128,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.reset_sm = (tt0 + s0 == 1) && !ctx->read_states;
         a.c2TSTu = (double)ctx->timestep / 24.0;
         a.nTstepDay = 24.0 / (double)ctx->timestep;
-        const double *fp[kForcKinds] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        const double *fp[kForcKinds] = {};
         if (on_device) {
             a.row_base = row0_all;
             for (int k = 0; k < kForcKinds; ++k)
@@ -1131,6 +1147,8 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.tmin = fp[3];
         a.tmax = fp[4];
         a.netrad = fp[5];
+        a.eabs = fp[6];
+        a.wind = fp[7];
         if (ctx->meteo_w_on) {
             const size_t wn = (size_t)24 * 12 * N;
             a.w_pre = ctx->meteo_w.p;
@@ -1917,8 +1935,8 @@ int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
     if (!ctx || !l0) return MHM_ERR_INVALID;
     if (int rc = mhm_sync(ctx)) return rc;
     ctx->mpr_ready = false;
-    if (ctx->proc_pet < -1 || ctx->proc_pet > 2)
-        return fail(ctx, MHM_ERR_UNSUPPORTED, "MPR supports PET cases -1, 0, 1 and 2");
+    if (ctx->proc_pet < -1 || ctx->proc_pet > 3)
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "MPR supports PET cases -1 to 3");
     if (l0->max_soil_hor > kMprMaxSoilHor)
         return fail(ctx, MHM_ERR_UNSUPPORTED, "more than 16 soil layers per soil type");
     MprSetup &m = ctx->mpr;

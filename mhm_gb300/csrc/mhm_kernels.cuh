@@ -6,7 +6,7 @@
 namespace mhm {
 
 constexpr int kMaxHorizons = 8;
-constexpr int kForcKinds = 6; // pre, temp, pet, tmin, tmax, net radiation
+constexpr int kForcKinds = 8; // pre, temp, pet, tmin, tmax, net radiation, abs. vapour pressure, wind speed
 
 // Per-member effective-parameter planes, each [n_cells] contiguous:
 // params[(m * n_planes + plane) * n_cells + k].
@@ -28,8 +28,9 @@ enum ParamPlane : int {
     P_UTHRESH,
     P_STHRESH,
     P_MAXINTER,             // 12 planes (LAI month)
-    P_PETLAI = P_MAXINTER + 12, // 12 planes
-    P_HORIZON = P_PETLAI + 12,  // then 5 groups of H planes: fRoots, SMs, FC, PW, beta
+    P_PETLAI = P_MAXINTER + 12, // 12 planes: petLAIcorFactor, PrieTayAlpha or aeroResist (by PET case)
+    P_PET2 = P_PETLAI + 12,     // 12 planes: surfResist (Penman-Monteith)
+    P_HORIZON = P_PET2 + 12,    // then 5 groups of H planes: fRoots, SMs, FC, PW, beta
 };
 __host__ __device__ constexpr int n_param_planes(int H) { return P_HORIZON + 5 * H; }
 
@@ -102,7 +103,8 @@ struct CellArgs {
     double c2TSTu;      // timestep / 24
     double nTstepDay;   // 24 / timestep
     const double *pre, *temp, *pet, *tmin, *tmax; // [rows][n_cells] from row_base
-    const double *netrad;                         // [rows][n_cells] (proc_pet 2) or null
+    const double *netrad;                         // [rows][n_cells] (proc_pet 2, 3) or null
+    const double *eabs, *wind;                    // [rows][n_cells] (proc_pet 3) or null
     // read_meteo_weights: L1_{pre,pet,temp}_weights(cell, month, hour) as
     // [24][12][n_cells] (the reference's column-major order); null: day/night ratios
     const double *w_pre, *w_pet, *w_temp;

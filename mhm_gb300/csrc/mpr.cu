@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
     const size_t slots = (size_t)a.max_sub * N;
     const double *plai = a.petlai + (size_t)m * 3 * a.n_lai_classes * 12;
     for (int mo = 0; mo < 12; ++mo) {
-        double s_int = 0.0, s_pet = 0.0, s_pt = 0.0;
+        double s_int = 0.0, s_pet = 0.0, s_pt = 0.0, s_ra = 0.0, s_rs = 0.0;
         for (int j = 0; j < ns; ++j) {
             const uint32_t c = __ldg(code + (size_t)j * N);
             double lai;
@@ -335,6 +335,29 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
             s_int = s_int + lai * gi;
             // priestley_taylor_alpha, src/MPR/mo_mpr_pet.f90:311-369: alpha0 = p1 + p2 LAI0
             if (a.proc_pet == 2) s_pt = s_pt + (pp[0] + pp[1] * lai);
+            if (a.proc_pet == 3) {
+                // aerodynamical_resistance, src/MPR/mo_multi_param_reg.f90:1165-1262: canopy
+                // height by land cover (pervious: p3 LAI / max over the months), measurement
+                // height 10 m raised above the canopy, log profile with karman = 0.41
+                const int l = (int)((c & kMprKeyMask) % 3u); // 0 forest, 1 impervious, 2 pervious
+                double hc = (l == 0) ? pp[0] : pp[1];
+                if (l == 2) {
+                    double mx = -1.0e300;
+                    for (int t = 0; t < 12; ++t) {
+                        const double x = a.lai ? __ldg(a.lai + t * slots + (size_t)j * N + k)
+                                               : __ldg(a.lai_lut + ((c >> 16) & 0xFFu) * 12 + t);
+                        mx = (t == 0 || x > mx) ? x : mx;
+                    }
+                    hc = pp[2] * lai / mx;
+                }
+                double zm = 10.0;
+                if (zm < hc) zm = hc + zm;
+                const double disp = pp[3] * hc, z0m = pp[4] * hc, z0h = pp[5] * z0m;
+                s_ra = s_ra + hm_log((zm - disp) / z0m) * hm_log((zm - disp) / z0h) / (0.41 * 0.41);
+                // bulksurface_resistance, src/MPR/mo_mpr_pet.f90:407-475, capped at 250 s m-1
+                const double rs = pp[6] / (lai / (0.3 * lai + 1.2));
+                s_rs = s_rs + (rs > 250.0 ? 250.0 : rs);
+            }
             if (a.proc_pet == -1) {
                 const int l = (int)((c & kMprKeyMask) % 3u);
                 double inv;
@@ -348,7 +371,10 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
             }
         }
         out[(size_t)(P_MAXINTER + mo) * N + k] = s_int / dn;
-        out[(size_t)(P_PETLAI + mo) * N + k] = (a.proc_pet == -1) ? dn / s_pet : (a.proc_pet == 2) ? s_pt / dn : 0.0;
+        out[(size_t)(P_PETLAI + mo) * N + k] = (a.proc_pet == -1) ? dn / s_pet
+                                               : (a.proc_pet == 2) ? s_pt / dn
+                                               : (a.proc_pet == 3) ? s_ra / dn : 0.0;
+        out[(size_t)(P_PET2 + mo) * N + k] = (a.proc_pet == 3) ? s_rs / dn : 0.0;
     }
 }
 

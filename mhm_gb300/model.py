@@ -171,7 +171,8 @@ class MhmGpu:
         """The member's effective parameters (L1_* arrays) read back."""
         N, H = self.dom.n_cells, self.dom.n_horizons
         sizes = {"maxInter": 12 * N, "petLAIcorFactor": 12 * N, "fRoots": H * N, "soilMoistSat": H * N,
-                 "soilMoistFC": H * N, "wiltingPoint": H * N, "soilMoistExp": H * N, "PrieTayAlpha": 12 * N}
+                 "soilMoistFC": H * N, "wiltingPoint": H * N, "soilMoistExp": H * N, "PrieTayAlpha": 12 * N,
+                 "aeroResist": 12 * N, "surfResist": 12 * N}
         out = {n: np.zeros(sizes.get(n, N)) for n in _lib.EFF_PARAM_FIELDS}
         ep = _lib.EffParams(**{n: _d(a) for n, a in out.items()})
         self._check(self.L.mhm_get_eff_params(self.ctx, member, C.byref(ep)), "mhm_get_eff_params")
@@ -239,7 +240,7 @@ class MhmGpu:
                     "mhm_set_forcing")
 
     def set_meteo(self, row0: int, pre, temp, pet=None, tmin=None, tmax=None, on_device: bool = False,
-                  netrad=None):
+                  netrad=None, eabs=None, windspeed=None):
         self.set_forcing(_lib.FORC_PRE, row0, pre, on_device)
         self.set_forcing(_lib.FORC_TEMP, row0, temp, on_device)
         if pet is not None:
@@ -250,6 +251,10 @@ class MhmGpu:
             self.set_forcing(_lib.FORC_TMAX, row0, tmax, on_device)
         if netrad is not None:
             self.set_forcing(_lib.FORC_NETRAD, row0, netrad, on_device)
+        if eabs is not None:
+            self.set_forcing(_lib.FORC_EABS, row0, eabs, on_device)
+        if windspeed is not None:
+            self.set_forcing(_lib.FORC_WINDSPEED, row0, windspeed, on_device)
 
     # ---- time stepping (do_time_step x n) ----
     def enable_outputs(self, total_runoff: bool = False, qmod: bool = False):

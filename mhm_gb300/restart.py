@@ -51,6 +51,8 @@ EFF_PARAMS = {
     "L1_fAsp": ("fAsp", ()),
     "L1_HarSamCoeff": ("HarSamCoeff", ()),
     "L1_PrieTayAlpha": ("PrieTayAlpha", ("lai",)),
+    "L1_aeroResist": ("aeroResist", ("scene", "lai")),
+    "L1_surfResist": ("surfResist", ("lai",)),
 }
 # mHM restart variable -> state name of mhm_restart (the L1 storages)
 STATES = {"L1_Inter": "interc", "L1_snowPack": "snowpack", "L1_sealSTW": "sealSTW", "L1_soilMoist": "soilMoist",
@@ -178,8 +180,9 @@ def process_params(proc_sm: int, proc_pet: int) -> set[str]:
     processCase(3) = proc_sm and processCase(5) = proc_pet
     (src/MPR/mo_mpr_restart.f90:257-312): the Jarvis threshold for soil
     moisture cases 2 and 3; per PET case the LAI correction factor (-1),
-    the aspect factor (-1, 0, 1), the Hargreaves-Samani coefficient (1) or
-    the Priestley-Taylor alpha (2)."""
+    the aspect factor (-1, 0, 1), the Hargreaves-Samani coefficient (1),
+    the Priestley-Taylor alpha (2) or the aerodynamic and bulk surface
+    resistances (3)."""
     out = set()
     if proc_sm in (2, 3):
         out.add("L1_jarvis_thresh_c1")
@@ -191,10 +194,13 @@ def process_params(proc_sm: int, proc_pet: int) -> set[str]:
         out.add("L1_HarSamCoeff")
     if proc_pet == 2:
         out.add("L1_PrieTayAlpha")
+    if proc_pet == 3:
+        out |= {"L1_aeroResist", "L1_surfResist"}
     return out
 
 
-PROCESS_DEPENDENT = {"L1_jarvis_thresh_c1", "L1_petLAIcorFactor", "L1_fAsp", "L1_HarSamCoeff", "L1_PrieTayAlpha"}
+PROCESS_DEPENDENT = {"L1_jarvis_thresh_c1", "L1_petLAIcorFactor", "L1_fAsp", "L1_HarSamCoeff", "L1_PrieTayAlpha",
+                     "L1_aeroResist", "L1_surfResist"}
 
 
 def write_mhm_restart(path, mask: np.ndarray, states: dict[str, np.ndarray], params_by_scene: list[dict],

@@ -245,7 +245,7 @@ def test_oracle_reproduces_case_outputs(case, kind):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", [c for c in CASES if c != "case_03"])
+@pytest.mark.parametrize("case", list(CASES))
 def test_gpu_reproduces_case_discharge_and_states(case):
     from mhm_gb300.model import MhmGpu
     z, doms, forcing = load_run()
@@ -270,7 +270,7 @@ def test_gpu_reproduces_case_discharge_and_states(case):
         g.set_eff_params(p0)
         g.init_states(0)
         g.set_meteo(1, forcing["pre"], forcing["temp"], forcing["pet"], forcing["tmin"], forcing["tmax"],
-                    netrad=forcing["netrad"])
+                    netrad=forcing["netrad"], eabs=forcing["eabs"], windspeed=forcing["windspeed"])
         q1 = g.run(1, s2)[0, 0]
         g.mpr_setup(l0_for(1))            # land-cover scene 1991: new parameters, states kept
         g.set_link_fpimp(doms[1].ffp_imp)
