@@ -52,6 +52,7 @@ EVAP_COEFF = [1.3, 1.2, 0.72, 0.75, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1.5]
 FILE_START = (1989, 1, 1)     # meteo time axis: days since 1989-01-01
 SIM_START = (1990, 1, 1)      # eval_Per start 1990-07-01 minus warming_days 181
 SIM_DAYS = 546                # .. 1991-06-30
+FORCING_DAYS = 730            # forcing rows kept: 1990-01-01 .. 1991-12-31 (case_07 runs both years)
 WARMING_DAYS = 181
 SCENE2_FROM_DAY = 365         # land-cover scene 1991 from 1991-01-01 on
 
@@ -115,24 +116,24 @@ def main():
         a = f.read({"temp": "tavg"}.get(key, key))
         t = f.read("time")
         assert t[off] == off and a.shape[1:] == mask1.shape
-        met[key] = np.ascontiguousarray(a[off:off + SIM_DAYS][:, mask1])
+        met[key] = np.ascontiguousarray(a[off:off + FORCING_DAYS][:, mask1])
     # daily net radiation (Priestley-Taylor PET): days since 1984-01-02, row 1826 = 1989-01-01
     f = h5lite.H5File(str(TD / "meteo" / "net_rad.nc"))
     a, t = f.read("net_rad"), f.read("time")
     o = int(np.nonzero(t == julday(*SIM_START) - julday(1984, 1, 2))[0][0])
-    met["netrad"] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
+    met["netrad"] = np.ascontiguousarray(a[o:o + FORCING_DAYS][:, mask1])
     # daily absolute vapour pressure and wind speed (Penman-Monteith PET), each on its own time axis
     for key, base in (("eabs", (1983, 12, 31)), ("windspeed", (1984, 1, 1))):
         f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
         a, t = f.read(key), f.read("time")
         o = int(np.nonzero(t == julday(*SIM_START) - julday(*base))[0][0])
-        met[key] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
+        met[key] = np.ascontiguousarray(a[o:o + FORCING_DAYS][:, mask1])
     # daily minimum / maximum temperature (Hargreaves-Samani PET): days since 1933-12-31
     for key in ("tmin", "tmax"):
         f = h5lite.H5File(str(TD / "meteo" / f"{key}.nc"))
         a, t = f.read(key), f.read("time")
         o = int(np.nonzero(t == julday(*SIM_START) - julday(1933, 12, 31))[0][0])
-        met[key] = np.ascontiguousarray(a[o:o + SIM_DAYS][:, mask1])
+        met[key] = np.ascontiguousarray(a[o:o + FORCING_DAYS][:, mask1])
     n_links = int(mrm.read("L11_fromN").size) - 1
     ffp = mrm.read("L11_nLinkFracFPimp")                      # [scene][y][x], link i at packed position i
     q = np.loadtxt(CASE / "output_save" / "b1_daily_discharge.out", skiprows=1)
@@ -177,7 +178,9 @@ import make_case00_mpr as mpr_fix  # noqa: E402
 
 # processCase(3), processCase(5), processCase(8)
 CASES = {"case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2), "case_02": (2, 2, 0),
-         "case_03": (1, 3, 1)}
+         "case_03": (1, 3, 1), "case_07": (1, 0, 1)}
+# cases whose run period differs from case_00's: (simulated days from 1990-01-01, warming days)
+PERIODS = {"case_07": (730, 0)}
 PARAM_NAMES = ("fSealed", "alpha", "degDayInc", "degDayMax", "degDayNoPre", "fAsp", "karstLoss", "kfastFlow",
                "kSlowFlow", "kBaseFlow", "kPerco", "tempThresh", "unsatThresh", "sealedThresh", "maxInter",
                "fRoots", "soilMoistSat", "soilMoistFC", "wiltingPoint", "soilMoistExp", "petLAIcorFactor",
@@ -233,6 +236,7 @@ def case_golds(case: str, proc_sm: int, proc_pet: int, proc_rout: int):
     np.savez_compressed(HERE / f"{case.replace('_', '')}_gold.npz", gamma=np.array(gamma), proc_sm=proc_sm,
                         proc_pet=proc_pet, proc_rout=proc_rout, q_daily=q[:, 5], **gold, **extra,
                         restart_vars=np.array(sorted(names)),
+                        **({"sim_days": PERIODS[case][0], "warming_days": PERIODS[case][1]} if case in PERIODS else {}),
                         **output_golds(cdir, mask1))
     print("wrote", HERE / f"{case.replace('_', '')}_gold.npz", len(gamma), sorted(gold))
 

@@ -76,10 +76,20 @@ SCENE_INDEPENDENT = ("unsatThresh", "karstLoss", "sealedThresh", "jarvis_thresh_
 GOLD_DIR = Path(__file__).resolve().parent / "golden"
 # check case -> (processCase(3), processCase(5), processCase(8)); all on the test_domain inputs
 CASES = {"case_00": (1, 0, 1), "case_10": (3, -1, 1), "case_12": (4, -1, 1), "case_09": (1, 1, 2),
-         "case_02": (2, 2, 0), "case_03": (1, 3, 1)}
-# case_03 is an optimisation (DDS): it writes the discharge and the mRM restart of its
-# last (here also best) evaluation, but no flux/state file and no mHM restart
-OUTPUT_CASES = [c for c in CASES if c != "case_03"]
+         "case_02": (2, 2, 0), "case_03": (1, 3, 1), "case_07": (1, 0, 1)}
+# case_03 and case_07 are optimisations (DDS): they write the discharge and the mRM restart
+# of their last (here also best) evaluation, but no flux/state file and no mHM restart
+OUTPUT_CASES = [c for c in CASES if c not in ("case_03", "case_07")]
+
+
+def period(case, z):
+    """(model steps, warming days) of a case's run from 1990-01-01: case_07 runs
+    1990-1991 without warming, the others case_00's 181 warming days and a year."""
+    if case != "case_00":
+        g = np.load(GOLD_DIR / f"{case.replace('_', '')}_gold.npz")
+        if "sim_days" in g.files:
+            return int(g["sim_days"]) * 24, int(g["warming_days"])
+    return int(z["sim_days"]) * 24, int(z["warming_days"])
 
 
 def case_setup(case):
@@ -168,7 +178,7 @@ def test_oracle_reproduces_case_discharge_and_states(case, kind):
     gamma, (proc_sm, proc_pet, proc_rout), gold = case_setup(case)
     doms = case_domains(case, doms, gold)
     p, rp = regionalised(kind, gamma, proc_sm, proc_pet, proc_rout)
-    n_steps = int(z["sim_days"]) * 24
+    n_steps, warm_days = period(case, z)
     s2 = int(z["scene2_from_day"]) * 24
     kw = dict(rout_param=rp, proc_sm=proc_sm, proc_pet=proc_pet, proc_rout=proc_rout, hourly=False, kind=kind)
     r1 = oracle.OracleRun(doms[0], p[0], **kw)
@@ -179,7 +189,7 @@ def test_oracle_reproduces_case_discharge_and_states(case, kind):
             np.copyto(r2.state[k], v)
     q2, _, _ = r2.run(forcing, 1, s2 + 1, n_steps - s2)
     q = np.concatenate([q1[:, 0], q2[:, 0]])
-    qd = daily_means(q, int(z["warming_days"]))
+    qd = daily_means(q, warm_days)
     if proc_rout:
         assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), (case, kind, np.abs(qd - gold["q"]).max())
     if case == "case_00":
@@ -252,7 +262,7 @@ def test_gpu_reproduces_case_discharge_and_states(case):
     l0_for, _, _, n1 = mpr_case.load_case()
     gamma, (proc_sm, proc_pet, proc_rout), gold = case_setup(case)
     doms = case_domains(case, doms, gold)
-    n_steps = int(z["sim_days"]) * 24
+    n_steps, warm_days = period(case, z)
     s2 = int(z["scene2_from_day"]) * 24
     g = MhmGpu(doms[0], proc_soilmoist=proc_sm, proc_pet=proc_pet, proc_routing=proc_rout, hourly=False,
                n_members=1)
@@ -280,7 +290,7 @@ def test_gpu_reproduces_case_discharge_and_states(case):
     finally:
         g.close()
     q = np.concatenate([q1, q2])
-    qd = daily_means(q, int(z["warming_days"]))
+    qd = daily_means(q, warm_days)
     if proc_rout:
         assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), np.abs(qd - gold["q"]).max()
     if case == "case_00":
