@@ -113,7 +113,11 @@ struct CellRegs {
 enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, HS_RSMS, HS_RDEN, HS_PLANES };
 
 
-template <int H, int MINB, bool FLUX>
+// LEAN: compiled for PET input (cases -1, 0) and the Feddes stress (soil-moisture
+// cases 1, 4) only -- the configurations of the throughput workloads -- so that
+// the Hargreaves / Priestley-Taylor / Penman-Monteith and Jarvis code is not in
+// the instruction stream and the register allocation.
+template <int H, int MINB, bool FLUX, bool LEAN>
 __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
 {
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     extern __shared__ double hsm[];
     const int tb = threadIdx.x, B = blockDim.x;
     auto hs = [&](int plane, int h) -> double & { return hsm[(plane * H + h) * B + tb]; };
-    const bool feddes = (a.proc_sm == 1 || a.proc_sm == 4);
+    const bool feddes = LEAN || (a.proc_sm == 1 || a.proc_sm == 4);
     CellRegs c;
     const double c2 = a.c2TSTu;
     c.fsealed = par(P_FSEALED);
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             r_evap = hm_recip_of(evap);
             // petLAIcorFactor (proc_pet -1) or PrieTayAlpha (proc_pet 2) of the LAI month
             if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = par(P_PETLAI + month - 1);
-            if (a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
+            if (!LEAN && a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
         }
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
         // output weights: write_output runs after the calendar has advanced, so
@@ -240,11 +244,12 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             ofns = 1.0 - ofs; // run_cfg%L1_fNotSealed = 1 - L1_fSealed (:239)
         }
         // ---- meteo for the step (mo_meteo_handler.f90:915-1285) ----
-        double pv;
+        double pv = 0.0;
         if (a.proc_pet == 0) {
             pv = c.fasp * __ldg(a.pet + f);
         } else if (a.proc_pet == -1) {
             pv = petlai * __ldg(a.pet + f);
+        } else if constexpr (LEAN) {
         } else if (a.proc_pet == 2) { // Rn = max(L1_netrad, 0), src/meteo/mo_meteo_handler.f90:1080-1085
             const double rn = __ldg(a.netrad + f);
             pv = pet_priestly(petlai, rn > 0.0 ? rn : 0.0, __ldg(a.temp + f));
@@ -500,8 +505,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
 
 // Launch with H as a template parameter (shared-memory size, loop bounds);
 // MINB = resident blocks per SM the register allocation is sized for.
-template <int MINB, bool FLUX = false>
-cudaError_t launch_cell_chain_variant(const CellArgs &a, int H, cudaStream_t s)
+template <int MINB, bool FLUX, bool LEAN>
+cudaError_t launch_cell_chain_h(const CellArgs &a, int H, cudaStream_t s)
 {
     const int64_t n = (int64_t)a.n_cells * a.n_members;
     const int block = 128;
@@ -511,9 +516,9 @@ cudaError_t launch_cell_chain_variant(const CellArgs &a, int H, cudaStream_t s)
 #define MHM_CASE(HH)                                                                                               \
     case HH:                                                                                                       \
         if (smem > 48 * 1024)                                                                                      \
-            cudaFuncSetAttribute(cell_chain_kernel<HH, MINB, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                                 (int)smem);                                                                       \
-        cell_chain_kernel<HH, MINB, FLUX><<<grid, block, smem, s>>>(a);                                            \
+            cudaFuncSetAttribute(cell_chain_kernel<HH, MINB, FLUX, LEAN>,                                          \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                          \
+        cell_chain_kernel<HH, MINB, FLUX, LEAN><<<grid, block, smem, s>>>(a);                                      \
         break;
         MHM_CASE(1) MHM_CASE(2) MHM_CASE(3) MHM_CASE(4) MHM_CASE(5) MHM_CASE(6) MHM_CASE(7) MHM_CASE(8)
 #undef MHM_CASE
@@ -521,6 +526,16 @@ cudaError_t launch_cell_chain_variant(const CellArgs &a, int H, cudaStream_t s)
         return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+template <int MINB, bool FLUX = false>
+cudaError_t launch_cell_chain_variant(const CellArgs &a, int H, cudaStream_t s)
+{
+    if constexpr (!FLUX) {
+        const bool lean = (a.proc_pet == 0 || a.proc_pet == -1) && (a.proc_sm == 1 || a.proc_sm == 4);
+        if (lean) return launch_cell_chain_h<MINB, false, true>(a, H, s);
+    }
+    return launch_cell_chain_h<MINB, FLUX, false>(a, H, s);
 }
 
 } // namespace
