@@ -5,7 +5,7 @@
  * The reference has no C interface: its hot path is a set of Fortran module
  * procedures.  Each entry point below replaces one of them, with the same
  * argument meaning, and is what an iso_c_binding interface module on the
- * Fortran side binds (the binding is shown in INTEGRATION.md).
+ * Fortran side binds.
  *
  * Conventions
  *   - Every function returns an int status: MHM_OK (0) or a negative MHM_ERR_*

@@ -225,6 +225,32 @@ int cuda_fail(mhm_ctx *c, cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what);                                                    \
     } while (0)
 
+// Makes a device current for the lifetime of the guard and puts the calling
+// thread's previous device back on exit, so that a context's allocations and
+// launches land on its own GPU whatever device the caller has current, and
+// the caller's own CUDA calls afterwards still see the device it chose.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+
+// First statement of every context entry point that touches the GPU.
+#define ON_CTX_DEVICE(ctx)                                                                                         \
+    DeviceGuard dev_guard_((ctx)->device);                                                                         \
+    if (dev_guard_.err != cudaSuccess) return cuda_fail(ctx, dev_guard_.err, "set device")
+
 // Host replica of the device interval bookkeeping over steps tt_a .. tt_a+n-1
 // (same calendar and writeout rule as the kernels); with `commit` the set's
 // counters and closing steps advance, else only the written count is returned.
@@ -560,11 +586,14 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         std::fprintf(stderr, "mhm_ctx_create: no CUDA device (%s)\n", cudaGetErrorString(e));
         return MHM_ERR_CUDA;
     }
-    if (device >= 0) {
-        if (device >= ndev) return bad("device index out of range");
-        cudaSetDevice(device);
-    }
-    cudaGetDevice(&ctx->device);
+    if (device >= ndev) return bad("device index out of range");
+    int cur_dev = 0;
+    if (device < 0 && cudaGetDevice(&cur_dev) != cudaSuccess) cur_dev = 0;
+    ctx->device = device >= 0 ? device : cur_dev;
+    // the context's buffers and streams live on ctx->device; the caller's
+    // current device is put back on return
+    DeviceGuard dg(ctx->device);
+    if (dg.err != cudaSuccess) return bad(std::string("cannot use device: ") + cudaGetErrorString(dg.err));
     auto ck = [&](cudaError_t ee, const char *w) {
         if (ee != cudaSuccess) {
             std::fprintf(stderr, "mhm_ctx_create: %s: %s\n", w, cudaGetErrorString(ee));
@@ -661,6 +690,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
 int mhm_ctx_destroy(mhm_ctx *ctx)
 {
     if (!ctx) return MHM_OK;
+    DeviceGuard dg(ctx->device); // release everything on the context's own device
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     if (ctx->route_stream) cudaStreamSynchronize(ctx->route_stream);
@@ -693,6 +723,7 @@ int mhm_ctx_destroy(mhm_ctx *ctx)
 int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 {
     if (!ctx || !p) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     const size_t N = ctx->N;
@@ -747,6 +778,7 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 int mhm_set_link_celerity(mhm_ctx *ctx, int32_t m, const double *celerity)
 {
     if (!ctx || !celerity) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (ctx->proc_rout != 3) return fail(ctx, MHM_ERR_INVALID, "per-link celerity is routing case 3");
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
@@ -756,6 +788,7 @@ int mhm_set_link_celerity(mhm_ctx *ctx, int32_t m, const double *celerity)
 int mhm_set_meteo_weights(mhm_ctx *ctx, const double *pre_w, const double *pet_w, const double *temp_w)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the old weights
     if (!pre_w && !pet_w && !temp_w) {
         ctx->meteo_w_on = false;
@@ -777,6 +810,7 @@ int mhm_set_meteo_weights(mhm_ctx *ctx, const double *pre_w, const double *pet_w
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 {
     if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still use the old fractions
     if (ctx->n_links == 0) return MHM_OK;
     CK(cudaMemcpyAsync(ctx->ffp.p, ffp_imp, (size_t)ctx->n_links * sizeof(double), cudaMemcpyHostToDevice,
@@ -789,6 +823,7 @@ int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 {
     if (!ctx || !p) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     const size_t N = ctx->N;
@@ -827,6 +862,7 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t m, const mhm_eff_params *p)
 int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
 {
     if (!ctx || !p5) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (ctx->proc_rout == 2) return set_adaptive_member(ctx, m, p5[0], nullptr); // p5[0]: celerity [m s-1]
@@ -850,6 +886,7 @@ int mhm_set_routing_params(mhm_ctx *ctx, int32_t m, const double *p5)
 int mhm_init_states(mhm_ctx *ctx, int32_t m, const double *hd)
 {
     if (!ctx || !hd) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read what changes
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     const size_t N = ctx->N;
@@ -934,7 +971,6 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
     const int H = ctx->H;
-    CK(cudaSetDevice(ctx->device), "set device");
     const bool need[kForcKinds] = {true,
                                    true,
                                    ctx->proc_pet == 0 || ctx->proc_pet == -1,
@@ -1420,6 +1456,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
 int mhm_poll(mhm_ctx *ctx, int32_t *done)
 {
     if (!ctx || !done) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     // events recorded now cover everything enqueued so far on the streams
     if (!ctx->ev_poll[0])
         for (auto &e : ctx->ev_poll) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
@@ -1440,6 +1477,7 @@ int mhm_poll(mhm_ctx *ctx, int32_t *done)
 int mhm_sync(mhm_ctx *ctx)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (ctx->timing && ctx->run_a) {
         cudaEvent_t b;
         cudaEventCreate(&b);
@@ -1471,6 +1509,7 @@ int mhm_sync(mhm_ctx *ctx)
 int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (ctx->out_tro || ctx->out_qmod || ctx->out_flux)
         return fail(ctx, MHM_ERR_INVALID, "per-step outputs need the synchronous mhm_run");
     return run_enqueue(ctx, tt0, n_steps, q_gauge);
@@ -1479,6 +1518,7 @@ int mhm_run_async(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 int mhm_run_members_async(mhm_ctx *ctx, const int32_t *member_tt0, int32_t n_steps, double *q_gauge)
 {
     if (!ctx || !member_tt0) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (ctx->out_tro || ctx->out_qmod || ctx->out_flux)
         return fail(ctx, MHM_ERR_INVALID, "per-step outputs need the synchronous mhm_run");
     return run_enqueue(ctx, 1, n_steps, q_gauge, member_tt0);
@@ -1487,6 +1527,7 @@ int mhm_run_members_async(mhm_ctx *ctx, const int32_t *member_tt0, int32_t n_ste
 int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots)
 {
     if (!ctx || n_slots < 0) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t per = (size_t)n_state_planes(ctx->H) * ctx->N + 4 * (size_t)ctx->L;
     ctx->snap.release();
@@ -1501,9 +1542,9 @@ int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots)
 static int snapshot_copy(mhm_ctx *ctx, int32_t member, int32_t slot, bool save)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (member < 0 || member >= ctx->M || slot < 0 || slot >= ctx->n_snap)
         return fail(ctx, MHM_ERR_INVALID, "member or snapshot slot out of range");
-    CK(cudaSetDevice(ctx->device), "set device");
     const size_t N = ctx->N, L = ctx->L, ns = n_state_planes(ctx->H);
     const size_t per = ns * N + 4 * L;
     double *sp = ctx->snap.p + (size_t)slot * per;
@@ -1538,6 +1579,7 @@ int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member) { return snaps
 int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out)
 {
     if (!ctx || n_steps < 1) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t N = ctx->N, M = ctx->M, L = ctx->L, ns = n_state_planes(ctx->H);
     // every trial starts from the same states: keep a device copy
@@ -1614,6 +1656,7 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
 int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     int rc = run_enqueue(ctx, tt0, n_steps, q_gauge);
     int rs = mhm_sync(ctx);
     return rc ? rc : rs;
@@ -1622,6 +1665,7 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
 int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     ctx->out_flux = on ? 1 : 0;
     if (!on) {
@@ -1635,6 +1679,7 @@ int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on)
 int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     if (!ctx->out_flux) return fail(ctx, MHM_ERR_INVALID, "flux outputs are not enabled");
     if (aet) std::memcpy(aet, ctx->host_aet.data(), ctx->host_aet.size() * sizeof(double));
@@ -1645,6 +1690,7 @@ int mhm_get_fluxes(mhm_ctx *ctx, double *aet, double *loss)
 int mhm_enable_flux_state_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     OutSet &o = ctx->fso;
     o.on = false;
@@ -1673,7 +1719,6 @@ int mhm_enable_flux_state_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
     }
     if (n == 0) return MHM_OK;
     const size_t MN = (size_t)ctx->M * ctx->N;
-    CK(cudaSetDevice(ctx->device), "set device");
     CK(o.acc.ensure((size_t)n * MN), "output sums");
     CK(o.out.ensure((size_t)cfg->max_slots * n * MN), "output intervals");
     CK(cudaMemsetAsync(o.acc.p, 0, (size_t)n * MN * sizeof(double), ctx->stream), "output sums");
@@ -1697,6 +1742,7 @@ int mhm_enable_flux_state_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
 int mhm_enable_routed_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     OutSet &o = ctx->qro;
     o.on = false;
@@ -1709,7 +1755,6 @@ int mhm_enable_routed_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
     if (cfg->flags[1]) return fail(ctx, MHM_ERR_UNSUPPORTED, "river temperature (process 11) is not part of this build");
     if (cfg->max_slots < 1) return fail(ctx, MHM_ERR_INVALID, "max_slots >= 1 required");
     const size_t ML = (size_t)ctx->M * ctx->L;
-    CK(cudaSetDevice(ctx->device), "set device");
     CK(o.acc.ensure(ML), "Qrouted sums");
     CK(o.out.ensure((size_t)cfg->max_slots * ML), "Qrouted intervals");
     CK(cudaMemsetAsync(o.acc.p, 0, ML * sizeof(double), ctx->stream), "Qrouted sums");
@@ -1726,6 +1771,7 @@ int mhm_enable_routed_outputs(mhm_ctx *ctx, const mhm_output_config *cfg)
 int mhm_set_output_weights(mhm_ctx *ctx, int32_t m, int64_t tt, const double *fsealed, const double *soil_moist_sat)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (!ctx->fso.on) return fail(ctx, MHM_ERR_INVALID, "flux/state outputs are not enabled");
     if (tt >= 1 && (!fsealed || !soil_moist_sat)) return fail(ctx, MHM_ERR_INVALID, "weights missing");
@@ -1746,6 +1792,7 @@ int mhm_read_flux_state_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int
                                 int32_t *n_planes)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (n_planes) *n_planes = ctx->fso.on ? ctx->fso.n_planes : 0;
     return read_outset(ctx, ctx->fso, out, slot_tt, max_slots, n_slots, false);
 }
@@ -1753,12 +1800,14 @@ int mhm_read_flux_state_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int
 int mhm_read_routed_outputs(mhm_ctx *ctx, double *out, int64_t *slot_tt, int32_t max_slots, int32_t *n_slots)
 {
     if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     return read_outset(ctx, ctx->qro, out, slot_tt, max_slots, n_slots, true);
 }
 
 int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
 {
     if (!ctx || !st) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (int rc = mhm_sync(ctx)) return rc; // states of all enqueued steps
     const size_t N = ctx->N, L = ctx->L;
@@ -1805,6 +1854,7 @@ int mhm_get_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
 int mhm_set_state(mhm_ctx *ctx, int32_t m, const mhm_restart *st)
 {
     if (!ctx || !st) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (m < 0 || m >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t N = ctx->N, L = ctx->L;
@@ -1933,6 +1983,7 @@ int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_rout
 int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
 {
     if (!ctx || !l0) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     ctx->mpr_ready = false;
     if (ctx->proc_pet < -1 || ctx->proc_pet > 3)
@@ -1979,6 +2030,7 @@ int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
 int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma)
 {
     if (!ctx || !gammas) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the parameters
     if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
     if (n < 1 || member0 < 0 || member0 + n > ctx->M) return fail(ctx, MHM_ERR_INVALID, "members out of range");
@@ -2081,6 +2133,7 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
 int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n_gamma)
 {
     if (!ctx || !gamma) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
     if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
     if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
     if (ctx->proc_rout >= 2) return fail(ctx, MHM_ERR_UNSUPPORTED, "adaptive routing: use mhm_mpr");
@@ -2090,7 +2143,9 @@ int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n
         return fail(ctx, MHM_ERR_INVALID, "no parameter layout for these processes");
     if (n_gamma != off.total) return fail(ctx, MHM_ERR_INVALID, "parameter vector length does not match the layout");
     const int ts = mpr_table_stride(ctx->H);
-    const size_t n_table = (size_t)m.n_keys * ts, n_petlai = (size_t)3 * m.n_lai_classes * 12;
+    // the LAI-correction table is used only by PET case -1 with class LAI
+    const size_t n_table = (size_t)m.n_keys * ts;
+    const size_t n_petlai = (ctx->proc_pet == -1 && m.n_lai_classes > 0) ? (size_t)3 * m.n_lai_classes * 12 : 0;
     const size_t need = align32((size_t)n_gamma) + align32(n_table) + n_petlai;
     if (need > kMprScratchDoubles)
         return fail(ctx, MHM_ERR_INVALID,
@@ -2098,7 +2153,6 @@ int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n
                         std::to_string(kMprScratchDoubles) + " (512 KiB): use mhm_mpr");
     if (ctx->device < 0 || ctx->device >= kMaxScratchDevices)
         return fail(ctx, MHM_ERR_UNSUPPORTED, "device ordinal beyond the scratch address table");
-    CK(cudaSetDevice(ctx->device), "set device");
     double *scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_scratch_mu);

@@ -4,7 +4,7 @@ the reference's regression case check/case_00 (the test_domain basin) and the
 L1 effective parameters the reference itself wrote for it
 (check/case_00/output_save/b1_mHM_restart_001.nc).
 
-Run in a checkout where the reference tree is at REF (default below); the
+Run as `python make_case00_mpr.py <mHM source tree>` (the tree is REF); the
 fixture is committed, so tests never read the reference.  What is restated
 here (input handling, not the hot path):
   * ESRI ASCII grids -> mHM's (x, y) grids packed column-major over the L0
@@ -35,7 +35,9 @@ sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parents[1]))
 from mhm_gb300 import h5read as h5lite  # noqa: E402
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+if len(sys.argv) < 2:
+    sys.exit(f"usage: python {Path(__file__).name} <path of the mHM source tree>")
+REF = Path(sys.argv[1])
 TD = REF / "test_domain" / "input"
 CASE = REF / "check" / "case_00"
 

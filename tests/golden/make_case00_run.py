@@ -40,7 +40,9 @@ sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parents[1]))
 from mhm_gb300 import h5read as h5lite  # noqa: E402
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+if len(sys.argv) < 2:
+    sys.exit(f"usage: python {Path(__file__).name} <path of the mHM source tree>")
+REF = Path(sys.argv[1])
 TD = REF / "test_domain" / "input"
 CASE = REF / "check" / "case_00"
 

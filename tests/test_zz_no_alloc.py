@@ -2,6 +2,11 @@
 per-call data in the library's static device scratch, called through the C
 ABI and compared with mhm_mpr on the same inputs, two calls in a row.
 
+Both entry points launch the same kernels on the same inputs, so every
+effective parameter (including the LAI-based PET correction of PET case -1,
+which uses the third region of the scratch) and the Muskingum coefficients
+must be BIT-IDENTICAL.
+
 The file name sorts last so that the test also runs after every other test
 in one session (the scratch is a process-wide device array)."""
 import ctypes as C
@@ -13,20 +18,21 @@ from mhm_gb300 import params, synth
 
 _dp = C.POINTER(C.c_double)
 
-RTOL = 1e-12   # the two paths run the same kernels: expected bit-equal
 
-
-def _close(a, b):
-    return np.allclose(a, b, rtol=RTOL, atol=0.0)
+def _bitwise(a, b):
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
 
 
 @pytest.mark.gpu
-def test_mpr_noalloc_matches_mpr_two_calls_in_a_row():
+@pytest.mark.parametrize("proc_pet", [0, -1])
+def test_mpr_noalloc_matches_mpr_two_calls_in_a_row(proc_pet):
     from mhm_gb300.model import MhmGpu
     dom = synth.make_domain(12, 10, 3, l11_factor=2, seed=1)
-    l0 = synth.make_l0(dom, 4, seed=4, holes=0.1)
-    gam = params.random_gammas(2, 1, 0, 1, l0.n_geo, seed=21)
-    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, n_members=2)
+    l0 = synth.make_l0(dom, 4, seed=4, holes=0.1)     # class LAI (12 classes): petLAIcorFactor from the table
+    gam = params.random_gammas(2, 1, proc_pet, 1, l0.n_geo, seed=21)
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=proc_pet, n_members=2)
     try:
         g.mpr_setup(l0)
         for call in range(2):
@@ -35,10 +41,12 @@ def test_mpr_noalloc_matches_mpr_two_calls_in_a_row():
             rc = g.L.mhm_mpr_noalloc(g.ctx, 1, gm.ctypes.data_as(_dp), gm.size)
             assert rc == 0, g.L.mhm_last_error(g.ctx)
             want, got = g.get_eff_params(0), g.get_eff_params(1)
+            if proc_pet == -1:
+                assert "petLAIcorFactor" in want and np.all(want["petLAIcorFactor"] > 0)
             for name in want:
-                assert _close(got[name], want[name]), (call, name)
+                assert _bitwise(got[name], want[name]), (call, name)
             st0, st1 = g.get_state(0), g.get_state(1)
-            assert _close(st1["C1"], st0["C1"]) and _close(st1["C2"], st0["C2"]), call
+            assert _bitwise(st1["C1"], st0["C1"]) and _bitwise(st1["C2"], st0["C2"]), call
     finally:
         g.close()
 
