@@ -11,7 +11,10 @@ forcing for the chunk (precipitation from a Gaussian random field with a
 chain, the L1->L11 accumulation and the Muskingum routing all run.  Steps
 continue the same simulation (states carry over); the forcing window repeats
 every step.  Inputs (3 x 1.92 GB of forcing per step) exceed the 129 MB L2,
-so no extra L2 flush is needed.
+so no extra L2 flush is needed.  The effective parameters are mpr() of the
+parameter namelist's default values over level-0 maps of 2000 x 2000 cells.
+The forcing window is generated once on the host from fixed seeds: the GPU
+arm, its CPU baseline and the reference arm all run the same arrays.
 
 `value` is device-timed throughput with inputs in HBM; `e2e` is the same run
 through the C ABI with the forcing in pinned host memory, copied to the
@@ -20,7 +23,8 @@ the gauge discharge copied back every step.
 
 --impl reference times the CPU restatement of the reference (the oracle,
 libm build = the C library's exp/log/pow as gfortran calls them, OpenMP over
-cells as the reference's own loop, serial routing) on the host cores.
+cells as the reference's own loop, serial routing) on the host cores, whole
+240-step chunks of the same workload, each step timed.
 """
 from __future__ import annotations
 
@@ -42,12 +46,18 @@ sys.path.insert(0, str(ROOT))
 METRIC = "cell-timesteps/s (mHM+mRM, FP64)"
 UNIT = "cell-timesteps/s"
 CONFIGS = {
-    # name: (nrows, ncols, H, l11_factor, chunk_steps, dem kwargs)
-    "large": (1000, 1000, 6, 4, 240, dict(dem_kind="fractal", fractal_beta=3.0, tilt=0.0005, ridges=6)),
-    "medium": (500, 500, 6, 4, 240, dict(dem_kind="fractal", fractal_beta=3.0, tilt=0.0005, ridges=3)),
-    "small": (96, 96, 3, 4, 240, dict(dem_kind="plane")),
+    # name: L1 grid, soil horizons, L11 = l11 x l11 L1 cells, L0 = L1 / l0, steps per bench step, DEM
+    "large": dict(nrows=1000, ncols=1000, H=6, l11=4, l0=2, chunk=240,
+                  dem=dict(dem_kind="fractal", fractal_beta=3.0, tilt=0.0005, ridges=6)),
+    "medium": dict(nrows=500, ncols=500, H=6, l11=4, l0=2, chunk=240,
+                   dem=dict(dem_kind="fractal", fractal_beta=3.0, tilt=0.0005, ridges=3)),
+    "small": dict(nrows=96, ncols=96, H=3, l11=4, l0=4, chunk=240, dem=dict(dem_kind="plane")),
 }
 ALG_BYTES_PER_CELL_STEP = 32  # 24 B forcing read + 8 B total runoff write
+# generator seeds of every synthetic input (numpy.random.default_rng)
+SEEDS = {"domain_dem": 1, "forcing": 2, "ensemble_parameter_sets": 3, "l0_maps": 4}
+LAND_COVER_MAPPING = ("5 synthetic L0 land-cover classes -> mHM land-cover codes "
+                      "{1: 1 forest, 2: 1 forest, 3: 3 pervious, 4: 3 pervious, 5: 2 impervious}")
 
 
 def _env_rank():
@@ -145,53 +155,58 @@ def traffic_from_profiles(name: str):
     return None
 
 
-def build_workload(cfg_name: str, seed: int = 1):
+def build_workload(cfg_name: str, order=None):
+    """(domain, L0 maps, parameter vector, steps per bench step): the basin
+    of the configuration, its level-0 maps under L1 = L0 x l0 and the
+    parameter namelist's default values (mhm_parameter.nml `value` column),
+    which mpr() turns into the effective parameters.  `order` computes the
+    routing order (the CPU arms pass the oracle's)."""
+    from mhm_gb300 import params, synth
+    c = CONFIGS[cfg_name]
+    dom = synth.make_domain(c["nrows"], c["ncols"], c["H"], c["l11"], seed=SEEDS["domain_dem"], order=order,
+                            **c["dem"])
+    l0 = synth.make_l0(dom, c["l0"], seed=SEEDS["l0_maps"])
+    gamma = params.default_gamma(1, 0, 1, l0.n_geo)
+    return dom, l0, gamma, c["chunk"]
+
+
+def workload_config(cfg_name: str, dom, chunk: int) -> dict:
+    """The `config` object of both arms (the same dict for the same workload)."""
+    c = CONFIGS[cfg_name]
+    levels = dom.depth_stats()[0]
+    return {"workload": f"single large domain: L1 {dom.nrows}x{dom.ncols} ({dom.n_cells} cells), "
+                        f"{dom.n_horizons} soil horizons, hourly, L11 {dom.n_nodes} nodes ({levels} routing "
+                        f"levels); step = {chunk} time steps" if cfg_name == "large" else
+                        f"{cfg_name}: L1 {dom.nrows}x{dom.ncols}, {dom.n_horizons} horizons; step = {chunk} steps",
+            "cells": dom.n_cells, "horizons": dom.n_horizons, "l11_nodes": dom.n_nodes, "routing_levels": levels,
+            "l0_cells": dom.n_cells * c["l0"] ** 2, "steps_per_bench_step": chunk,
+            "parameters": "mpr() of the parameter namelist's default values (processes 1,1,1,1,0,1,1,1,1,0)",
+            "forcing": f"one {chunk}-step hourly window, repeated every step (states carry over): precipitation "
+                       "occurrence from a Gaussian random field (20-cell length scale, 70 % dry hours), "
+                       "Gamma(0.6, 2 mm/h) amounts; temperature 8 + 10 sin + N(0, 3) degC; Hargreaves PET",
+            "seeds": SEEDS, "land_cover_mapping": LAND_COVER_MAPPING,
+            "parallelism": "single GPU",
+            "l2": ("inputs larger than L2 (forcing 3 x %.2f GB per step)" if 3 * chunk * dom.n_cells * 8 > 129e6
+                   else "inputs smaller than L2 (forcing 3 x %.2f GB per step)") % (chunk * dom.n_cells * 8 / 1e9)}
+
+
+def host_forcing(dom, chunk: int, pinned: bool):
+    """The forcing window every arm uses (same seed -> same arrays): numpy
+    views, in pinned host memory when `pinned`."""
     from mhm_gb300 import synth
-    nr, nc, H, f11, chunk, demkw = CONFIGS[cfg_name]
-    dom = synth.make_domain(nr, nc, H, f11, seed=seed, **demkw)
-    params = synth.make_eff_params(dom, seed=3)
-    return dom, params, chunk
-
-
-def device_forcing(dom, n_steps: int, seed: int, device):
-    """Forcing window [n_steps, N] generated on the GPU (torch as plumbing):
-    GRF-correlated precipitation occurrence (20-cell length scale, 70 % dry),
-    Gamma(0.6, 2) amounts, seasonal temperature + noise, Hargreaves PET."""
-    import torch
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    nr, nc = dom.nrows, dom.ncols
-    ky = torch.fft.fftfreq(nr, device=device)[:, None]
-    kx = torch.fft.rfftfreq(nc, device=device)[None, :]
-    filt = torch.exp(-2.0 * (torch.pi * 20.0) ** 2 * (kx * kx + ky * ky))
-    pre = torch.empty((n_steps, dom.n_cells), dtype=torch.float64, device=device)
-    gam = torch.distributions.Gamma(torch.tensor(0.6, dtype=torch.float64, device=device),
-                                    torch.tensor(0.5, dtype=torch.float64, device=device))
-    torch.manual_seed(seed)
-    for t in range(n_steps):
-        w = torch.randn((nr, nc), generator=g, device=device, dtype=torch.float64)
-        field = torch.fft.irfft2(torch.fft.rfft2(w) * filt, s=(nr, nc))
-        thr = torch.quantile(field.flatten()[:: max(1, nr * nc // 100000)], 0.7)
-        amt = gam.sample((nr, nc))
-        p2d = torch.where(field > thr, amt, torch.zeros_like(amt))
-        pre[t] = p2d.T.reshape(-1)  # column-major pack
-    hours = torch.arange(n_steps, device=device, dtype=torch.float64)
-    doy = (hours // 24) % 365 + 1
-    seas = 8.0 + 10.0 * torch.sin(2 * torch.pi * (doy - 81) / 365.0)
-    temp = seas[:, None] + 3.0 * torch.randn((n_steps, dom.n_cells), generator=g, device=device, dtype=torch.float64)
-    lat = torch.deg2rad(torch.from_numpy(dom.latitude).to(device))
-    dr = 1 + 0.033 * torch.cos(2 * torch.pi * doy / 365.0)
-    dec = 0.409 * torch.sin(2 * torch.pi * doy / 365.0 - 1.39)
-    ws = torch.arccos(torch.clamp(-torch.tan(lat)[None, :] * torch.tan(dec)[:, None], -1, 1))
-    ra = 24 * 60 / torch.pi * 0.082 * dr[:, None] * (ws * torch.sin(lat)[None, :] * torch.sin(dec)[:, None] +
-                                                      torch.cos(lat)[None, :] * torch.cos(dec)[:, None] * torch.sin(ws))
-    pet = torch.clamp(0.0023 * ra * 0.408 * (seas[:, None] + 17.8) * (10.0 ** 0.5), min=0.0) / 24.0
-    return pre.contiguous(), temp.contiguous(), pet.contiguous()
+    if pinned:
+        import torch
+        bufs = {k: torch.empty((chunk, dom.n_cells), dtype=torch.float64, pin_memory=True)
+                for k in ("pre", "temp", "pet")}
+        out = {k: v.numpy() for k, v in bufs.items()}
+    else:
+        bufs, out = None, None
+    f = synth.make_forcing_grf(dom, chunk, seed=SEEDS["forcing"], out=out)
+    return f, bufs
 
 
 def run_gpu(args) -> dict:
     import torch
-    from mhm_gb300 import synth
     from mhm_gb300._lib import load
     from mhm_gb300.model import MhmGpu
 
@@ -203,11 +218,15 @@ def run_gpu(args) -> dict:
     device = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(device)
     lib = load()
-    dom, params, chunk = build_workload(args.config)
+    dom, l0, gamma, chunk = build_workload(args.config)
     N = dom.n_cells
     g = MhmGpu(dom, proc_soilmoist=1, proc_pet=0, device=device.index)
-    g.prepare(params, synth.ROUTING_PARAMS_DEFAULT)
-    pre, temp, pet = device_forcing(dom, chunk, seed=2 + rank, device=device)
+    g.mpr_setup(l0)
+    g.mpr(gamma)                      # effective parameters and Muskingum coefficients
+    g.init_states(0)
+    hf, pinned = host_forcing(dom, chunk, pinned=True)
+    pre, temp, pet = (pinned[k].to(device) for k in ("pre", "temp", "pet"))
+    torch.cuda.synchronize()
     stream = torch.cuda.ExternalStream(g.stream, device=device)
     g.set_meteo(1, pre, temp, pet, on_device=True)
     tune = None if args.no_autotune else g.autotune(1, chunk)   # register variant x routing sub-chunk
@@ -215,7 +234,7 @@ def run_gpu(args) -> dict:
     G = len(dom.gauge_node)
     qbufs = [np.zeros((1, G, chunk)) for _ in range(2)]
 
-    def step(s: int, on_device=True, host=None):
+    def step(s: int, on_device=True):
         """Enqueue one benchmark step (the library pipelines consecutive steps:
         routing of step s overlaps the cell chain of step s+1); the gauge
         series lands in a host buffer when g.sync() returns."""
@@ -223,7 +242,7 @@ def run_gpu(args) -> dict:
         if on_device:
             g.set_meteo(tt0, pre, temp, pet, on_device=True)
         else:
-            g.set_meteo(tt0, *host)
+            g.set_meteo(tt0, hf["pre"], hf["temp"], hf["pet"])
         g.run_async(tt0, chunk, qbufs[s & 1])
 
     def barrier():
@@ -263,12 +282,8 @@ def run_gpu(args) -> dict:
     ms, value = replica_throughput(ms, float(N) * chunk * args.steps, world, device)
 
     # ---- e2e: host forcing (pinned), H2D + compute + D2H of the gauge series per step ----
-    host = [torch.empty((chunk, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
-    for h, d in zip(host, (pre, temp, pet)):
-        h.copy_(d)
-    hnp = [h.numpy() for h in host]
     e2e_steps = max(1, min(args.steps, 8))
-    step(args.warmup + args.steps, on_device=False, host=hnp)  # warm the staging buffers
+    step(args.warmup + args.steps, on_device=False)  # warm the staging buffers
     g.sync()
     barrier()
     torch.cuda.synchronize()
@@ -277,7 +292,7 @@ def run_gpu(args) -> dict:
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for s in range(e2e_steps):
-        step(args.warmup + args.steps + 1 + s, on_device=False, host=hnp)
+        step(args.warmup + args.steps + 1 + s, on_device=False)
     g.sync()  # all H2D copies, compute and gauge D2H copies complete
     e1.record(stream)
     torch.cuda.synchronize()
@@ -298,26 +313,27 @@ def run_gpu(args) -> dict:
     ops = traffic_from_profiles_ops()
     if fp64_peak and ops:
         flops = ops * N * chunk / per_launch_s
-        fp64_line.update({"achieved": flops / 1e12, "frac": flops / fp64_peak, "flop_per_cell_step": ops})
+        fp64_line.update({"achieved": flops / 1e12, "frac": flops / fp64_peak, "flop_per_cell_step": ops,
+                          "kernel": "cell_chain_kernel<6>"})
+    cfg = workload_config(args.config, dom, chunk)
+    if world > 1:
+        cfg["parallelism"] = f"replicas x{world}"
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"single large domain: L1 {dom.nrows}x{dom.ncols} ({N} cells), "
-                               f"{dom.n_horizons} soil horizons, hourly, L11 {dom.n_nodes} nodes "
-                               f"({dom.depth_stats()[0]} routing levels); step = {chunk} time steps",
-                   "cells": N, "horizons": dom.n_horizons, "l11_nodes": dom.n_nodes,
-                   "routing_levels": dom.depth_stats()[0], "steps_per_bench_step": chunk,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (forcing 3 x %.2f GB per step)" % (chunk * N * 8 / 1e9)},
+        "config": cfg,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * chunk * N * 8,
                 "d2h_bytes_per_step": chunk * len(dom.gauge_node) * 8, "steps": e2e_steps},
         "gpu_launches": int(launches),
+        # the contract's HBM view of the dominant kernel; the roof that binds it
+        # is the FP64 / integer issue rate (roofline_fp64)
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": (tb * N * chunk) if tb else None,
                      "kernel": "cell_chain_kernel<6>", "alg_bytes_per_launch": alg_bytes,
                      "launch_ms": per_launch_s * 1e3, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
-                     if peaks else "of fallback"},
+                     if peaks else "of fallback",
+                     "binding_roof": "fp64+integer issue (roofline_fp64); HBM is not the limit"},
         "roofline_fp64": fp64_line,
         "kernel_time_ms": {"cell_chain": t_cell, "runoff_acc": t_acc, "routing": t_rt,
                            "timed_region": ms},
@@ -325,10 +341,12 @@ def run_gpu(args) -> dict:
         "autotune": tune,
     }
     g.close()
+    del pre, temp, pet
+    torch.cuda.empty_cache()
     if rank == 0 and not args.no_ensemble:
         out["batched"] = run_ensemble(args, device)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(dom, params, args)
+        out["cpu_baseline"] = cpu_baseline(dom, l0, gamma, hf, chunk, args)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
@@ -357,7 +375,8 @@ def run_ensemble(args, device, plain_members: int = 8) -> dict:
     l0 = synth.make_l0(dom, E["l0_factor"], seed=4)
     M, chunk, N = (args.ensemble_members or E["members"]), E["chunk"], dom.n_cells
     gam = gparams.random_gammas(M, 1, 0, 1, l0.n_geo, seed=3)
-    pre, temp, pet = device_forcing(dom, chunk, seed=2, device=device)
+    fh = synth.make_forcing(dom, chunk, seed=SEEDS["forcing"])   # i.i.d. hourly forcing of the plain basin
+    pre, temp, pet = (torch.from_numpy(fh[k]).to(device) for k in ("pre", "temp", "pet"))
     G = len(dom.gauge_node)
     K = max(1, min(args.steps, 3))
 
@@ -497,45 +516,93 @@ def traffic_from_profiles_ops():
     return None
 
 
-def cpu_baseline(dom, params, args, target_s: float = 15.0) -> dict:
-    """The oracle (libm build, OpenMP over cells, serial routing) on a bounded
-    sample of the same workload: the same basin, consecutive 24-step blocks
-    (one 24-step forcing block, repeated as the GPU run repeats its window)
-    until ~target_s seconds have been spent."""
-    from mhm_gb300 import synth
-    from oracle.oracle import OracleRun
+class OracleArm:
+    """The CPU restatement of the reference's path on this host: the oracle
+    (libm build: the C library's exp/log/pow as gfortran calls them) runs
+    mpr() of the same parameter vector and then the time loop -- OpenMP over
+    cells as the reference's own `!$OMP do schedule(static)` over L1 cells,
+    serial routing -- on the same forcing window as the GPU arm."""
+
+    def __init__(self, dom, l0, gamma, forcing):
+        from mhm_gb300 import params
+        from oracle import oracle
+        off = params.offsets(1, 0, 1, l0.n_geo)
+        t0 = time.perf_counter()
+        eff = oracle.oracle_mpr(dom.n_cells, dom.n_horizons, l0, gamma, off, 1, 0, "libm")
+        self.mpr_s = time.perf_counter() - t0
+        eff = {k: v for k, v in eff.items() if k not in ("Wd", "slope_emp", "horizon_depth")}
+        self.run = oracle.OracleRun(dom, eff, rout_param=gamma[off[7]:off[7] + 5], kind="libm")
+        self.f = forcing
+        self.dom = dom
+        self.tt = 1
+
+    def chunk(self, n_steps: int, threads: int) -> float:
+        """Advance n_steps (the forcing window's first n_steps rows, as the GPU
+        arm repeats its window); returns the wall seconds."""
+        f = {k: v[:n_steps] for k, v in self.f.items()}
+        t0 = time.perf_counter()
+        self.run.run(f, self.tt, self.tt, n_steps, nthreads=threads)
+        dt = time.perf_counter() - t0
+        self.tt += n_steps
+        return dt
+
+
+def cpu_baseline(dom, l0, gamma, forcing, chunk: int, args, target_s: float = 12.0) -> dict:
+    """The oracle on a bounded sample of the bench workload (same basin,
+    parameters and forcing window): one untimed chunk (SM initialisation),
+    then whole chunks on all host threads until ~target_s, and a 24-step
+    sample on one thread."""
     threads = os.cpu_count() or 1
-    r = OracleRun(dom, params, synth.ROUTING_PARAMS_DEFAULT, kind="libm")
-    blk = 24
-    f = synth.make_forcing(dom, blk, seed=5)
-    r.run(f, 1, 1, blk, nthreads=threads)  # first block: SM initialisation and warm-up, untimed
-    done = 0
-    t0 = time.perf_counter()
-    tt = blk + 1
-    while time.perf_counter() - t0 < target_s:
-        r.run(f, tt, tt, blk, nthreads=threads)
-        tt += blk
-        done += blk
-    dt = time.perf_counter() - t0
-    return {"value": dom.n_cells * done / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{dom.n_cells} cells x {done} hourly steps in {dt:.1f} s (oracle libm build, "
-                      f"OpenMP {threads} threads over cells, serial routing)"}
+    arm = OracleArm(dom, l0, gamma, forcing)
+    arm.chunk(chunk, threads)
+    done, spent = 0, 0.0
+    while spent < target_s or done == 0:
+        spent += arm.chunk(chunk, threads)
+        done += chunk
+    one = arm.chunk(24, 1)
+    return {"value": dom.n_cells * done / spent, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{dom.n_cells} cells x {done} hourly steps ({done // chunk} whole {chunk}-step chunks of "
+                      f"the bench workload, same forcing window and parameters) in {spent:.1f} s; oracle libm "
+                      f"build, OpenMP {threads} threads over cells, serial routing",
+            "one_thread": {"value": dom.n_cells * 24 / one, "unit": UNIT, "cores": 1,
+                           "sample": f"{dom.n_cells} cells x 24 hourly steps in {one:.1f} s"},
+            "mpr_s": arm.mpr_s}
 
 
 def run_reference(args) -> dict | None:
+    """--impl reference: the reference's CPU path (the oracle port: no
+    Fortran compiler exists here or on the GPU host, so the reference
+    itself cannot be built) on this host's cores, on the GPU arm's workload:
+    the same basin (routing order from the oracle's restatement of
+    L11_routing_order), mpr() of the same default parameters, the same
+    forcing window.  Every step advances the whole basin by one chunk on all
+    host threads, exactly as one GPU step does; W untimed steps, then K timed
+    ones, each timed on its own."""
     rank, world, _ = _env_rank()
     if rank != 0:
         return None
     from oracle import oracle
     oracle.build()
-    dom, params, chunk = build_workload(args.config)
-    base = cpu_baseline(dom, params, args, target_s=max(5.0, 60.0 / max(1, args.steps + args.warmup)))
-    v = base["value"]
+    dom, l0, gamma, chunk = build_workload(args.config, order=lambda f, t, n, o: oracle.routing_order(f, t, n, o))
+    forcing, _ = host_forcing(dom, chunk, pinned=False)
+    threads = os.cpu_count() or 1
+    arm = OracleArm(dom, l0, gamma, forcing)
+    for _ in range(args.warmup):
+        arm.chunk(chunk, threads)
+    per = [arm.chunk(chunk, threads) for _ in range(args.steps)]
+    one = arm.chunk(24, 1)
+    total = sum(per)
+    v = dom.n_cells * chunk * args.steps / total
+    base = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{args.steps} whole {chunk}-step chunks of {dom.n_cells} cells, each timed "
+                      f"(min {min(per):.2f} s, max {max(per):.2f} s); oracle libm build, OpenMP {threads} threads "
+                      f"over cells, serial routing",
+            "one_thread": {"value": dom.n_cells * 24 / one, "unit": UNIT, "cores": 1,
+                           "sample": f"{dom.n_cells} cells x 24 hourly steps in {one:.1f} s"}}
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dom.n_cells * chunk / v * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"single large domain: L1 {dom.nrows}x{dom.ncols}, {dom.n_horizons} horizons, "
-                                   f"hourly, {dom.n_nodes} L11 nodes; step = {chunk} time steps"},
+            "config": workload_config(args.config, dom, chunk),
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -109,6 +109,20 @@ def layout(proc_sm: int, proc_pet: int, proc_rout: int, n_geo: int) -> np.ndarra
     return out
 
 
+def offsets(proc_sm: int, proc_pet: int, proc_rout: int, n_geo: int) -> np.ndarray:
+    """The same start offsets as `layout`, counted from the namelist blocks
+    above without the library (for hosts that only run the CPU oracle)."""
+    blocks = [INTERCEPTION1, SNOW1, SOILMOISTURE[proc_sm], DIRECTRUNOFF1, PET[proc_pet], INTERFLOW1,
+              PERCOLATION1, ROUTING[proc_rout], geo_rows(n_geo)]
+    out = np.zeros(11, np.int32)
+    acc = 0
+    for i, b in enumerate(blocks):
+        out[i] = acc
+        acc += len(b)
+    out[9] = out[10] = acc   # process 10 (neutrons) has no parameters
+    return out
+
+
 def default_gamma(proc_sm: int = 1, proc_pet: int = 0, proc_rout: int = 1, n_geo: int = 4) -> np.ndarray:
     """The namelist's `value` column."""
     return np.array([r[3] for r in rows(proc_sm, proc_pet, proc_rout, n_geo)], np.float64)

@@ -682,6 +682,90 @@ void ora_L11_routing_order(int nNodes, int nOutlets, const int32_t *fromN, const
         netPerm[rOrder[ii] - 1] = ii + 1;
 }
 
+/* The same ranks as ora_L11_routing_order (the same sweeps over the links in
+ * index order, a link ranked once every link draining into its from-node is
+ * ranked, including links ranked earlier in the same sweep), with each link's
+ * upstream links listed once up front instead of found by a scan of all
+ * links: O(sweeps * links) instead of O(sweeps * links^2), usable at 62,500
+ * nodes.  Returns 0, or -1 if a sweep ranks nothing (a cycle). */
+int ora_L11_routing_order_listed(int nNodes, int nOutlets, const int32_t *fromN, const int32_t *toN,
+                                 int32_t *netPerm, int32_t *rOrder)
+{
+    int nLinks = nNodes - nOutlets;
+    for (int i = 0; i < nNodes; ++i) {
+        netPerm[i] = -9999;
+        rOrder[i] = -9999;
+    }
+    if (nNodes <= 1 || nLinks <= 0)
+        return 0;
+    /* links by the node they drain into (1-based node ids) */
+    int32_t *cnt = (int32_t *)calloc((size_t)nNodes + 2, sizeof(int32_t));
+    int32_t *lst = (int32_t *)malloc((size_t)nLinks * sizeof(int32_t));
+    if (!cnt || !lst) {
+        free(cnt);
+        free(lst);
+        return -1;
+    }
+    for (int jj = 0; jj < nLinks; ++jj)
+        if (toN[jj] >= 1 && toN[jj] <= nNodes)
+            cnt[toN[jj] + 1]++;
+    for (int v = 1; v <= nNodes + 1; ++v)
+        cnt[v] += cnt[v - 1];
+    {
+        int32_t *fill = (int32_t *)malloc(((size_t)nNodes + 1) * sizeof(int32_t));
+        if (!fill) {
+            free(cnt);
+            free(lst);
+            return -1;
+        }
+        memcpy(fill, cnt, ((size_t)nNodes + 1) * sizeof(int32_t));
+        for (int jj = 0; jj < nLinks; ++jj)
+            if (toN[jj] >= 1 && toN[jj] <= nNodes)
+                lst[fill[toN[jj]]++] = jj;
+        free(fill);
+    }
+    int kk = 0;
+    for (int ii = 0; ii < nLinks; ++ii) {
+        int up = 0;
+        int v = fromN[ii];
+        for (int q = cnt[v]; q < cnt[v + 1]; ++q)
+            if (lst[q] != ii)
+                up = 1;
+        rOrder[ii] = up ? -9 : 1;
+    }
+    for (int ii = 0; ii < nLinks; ++ii)
+        if (rOrder[ii] == 1)
+            rOrder[ii] = ++kk;
+    int rc = 0;
+    while (kk < nLinks) {
+        int before = kk;
+        for (int ii = 0; ii < nLinks; ++ii) {
+            if (rOrder[ii] != -9)
+                continue;
+            int flag = 1, v = fromN[ii];
+            for (int q = cnt[v]; q < cnt[v + 1]; ++q) {
+                int jj = lst[q];
+                if (jj != ii && !(rOrder[jj] > 0)) {
+                    flag = 0;
+                    break;
+                }
+            }
+            if (flag)
+                rOrder[ii] = ++kk;
+        }
+        if (kk == before) {
+            rc = -1;
+            break;
+        }
+    }
+    if (rc == 0)
+        for (int ii = 0; ii < nLinks; ++ii)
+            netPerm[rOrder[ii] - 1] = ii + 1;
+    free(cnt);
+    free(lst);
+    return rc;
+}
+
 /* ---- whole-domain run ---- */
 
 /* fluxes_states_default_init (src/mHM/mo_init_states.f90:258-345) and

@@ -99,6 +99,8 @@ int ora_L11_set_network_topology(int nrows, int ncols, const int32_t *id2d /*[nc
  * netPerm (1-based link ids in routing order), rOrder (rank of each link). */
 void ora_L11_routing_order(int nNodes, int nOutlets, const int32_t *fromN, const int32_t *toN,
                            int32_t *netPerm, int32_t *rOrder);
+int ora_L11_routing_order_listed(int nNodes, int nOutlets, const int32_t *fromN, const int32_t *toN,
+                                 int32_t *netPerm, int32_t *rOrder);
 
 /* Routing case 2 (mrm_update_param, src/mRM/mo_mrm_mpr.f90:241-329): K = length /
  * celerity per link, the routing time step TSrout [s] = given_TS(locate(given_TS,

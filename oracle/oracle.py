@@ -158,6 +158,8 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_L11_set_network_topology.argtypes = [C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _ip, _ip]
     L.ora_L11_set_network_topology.restype = C.c_int
     L.ora_L11_routing_order.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.ora_L11_routing_order_listed.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.ora_L11_routing_order_listed.restype = C.c_int
     L.ora_update_param_case2.argtypes = [d, _dp, C.c_int, _dp, _dp]
     L.ora_update_param_case2.restype = d
     L.ora_update_param_links.argtypes = [_dp, d, _dp, C.c_int, _dp, _dp]
@@ -182,6 +184,20 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_slope_emp.restype = C.c_int
     _LIBS[kind] = L
     return L
+
+
+def routing_order(from_n, to_n, n_nodes: int, n_outlets: int, kind: str = "libm"):
+    """(netPerm, rOrder) of L11_routing_order by the oracle's listed sweep
+    (the reference's ranks; no use of the GPU library)."""
+    L = load(kind)
+    perm = np.zeros(n_nodes, np.int32)
+    rord = np.zeros(n_nodes, np.int32)
+    fn = np.ascontiguousarray(from_n, np.int32)
+    tn = np.ascontiguousarray(to_n, np.int32)
+    rc = L.ora_L11_routing_order_listed(n_nodes, n_outlets, _i(fn), _i(tn), _i(perm), _i(rord))
+    if rc != 0:
+        raise RuntimeError("routing order: the network has a cycle")
+    return perm, rord
 
 
 def _d(a):

@@ -59,6 +59,31 @@ def test_routing_order_synthetic_basins(kw, ora_hmath):
     assert np.array_equal(dom.net_perm, perm_o) and np.array_equal(dom.r_order, ro_o)
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_listed_sweep_equals_literal_sweep(seed, ora_hmath):
+    """The oracle's listed sweep (used where the literal O(n^2) scan is too
+    slow) gives the literal sweep's ranks."""
+    from oracle import oracle
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(2, 600))
+    n_out = int(rng.integers(1, max(2, n // 20)))
+    from_n, to_n = random_forest(rng, n, n_out)
+    perm_o, ro_o = oracle_order(ora_hmath, from_n, to_n, n, n_out)
+    perm, ro = oracle.routing_order(from_n, to_n, n, n_out, kind="hmath")
+    assert np.array_equal(perm, perm_o) and np.array_equal(ro, ro_o)
+
+
+def test_oracle_listed_sweep_on_the_large_network():
+    """62,500 L11 nodes, 1478 levels: the oracle's listed sweep and the
+    library's ranks agree (the literal scan does not finish at this size)."""
+    from oracle import oracle
+    dom = synth.make_domain(1000, 1000, 6, 4, seed=1, dem_kind="fractal", fractal_beta=3.0, tilt=0.0005,
+                            ridges=6, order=lambda f, t, n, o: oracle.routing_order(f, t, n, o))
+    perm, ro = synth.routing_order(dom.from_n, dom.to_n, dom.n_nodes, dom.n_outlets)
+    assert np.array_equal(perm, dom.net_perm) and np.array_equal(ro, dom.r_order)
+    assert dom.depth_stats()[0] == 1478
+
+
 def test_network_topology(ora_hmath):
     dom = synth.make_domain(60, 44, 2, 4, seed=3, dem_kind="fractal", ridges=1)
     L = dom.n_nodes
