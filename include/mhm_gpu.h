@@ -181,6 +181,22 @@ int mhm_set_routing_params(mhm_ctx *ctx, int32_t member, const double *rout_para
  * coefficients to this call.) */
 int mhm_set_link_celerity(mhm_ctx *ctx, int32_t member, const double *celerity);
 
+/* Inflow gauges (InflowGauge of mRM's configuration; add_inflow,
+ * src/mRM/mo_mrm_pre_routing.f90:179-214, called from mRM_routing at
+ * src/mRM/mo_mrm_routing.f90:234-241, and the headwater cut inside
+ * L11_routing, :447-452).  n gauges at the L11 nodes node[n] (1-based):
+ * headwater[g] != 0 adds the gauge's discharge to the node's own runoff
+ * (InflowGaugeHeadwater = .true.); otherwise the discharge replaces that
+ * runoff and every link draining into the node passes no water on.  Gauges
+ * act in list order.  n = 0 removes them.  At most 64 gauges. */
+int mhm_set_inflow_gauges(mhm_ctx *ctx, int32_t n, const int32_t *node, const int32_t *headwater);
+/* Daily discharge [m3 s-1] of the inflow gauges, q[(d - day0) * n + g] for
+ * days d = day0 .. day0 + n_days - 1, where model step tt belongs to day
+ * ceiling(tt / (24 / timestep)) (iDischargeTS, InflowGauge%Q(iDischargeTS, :),
+ * src/mHM/mo_mhm_interface_run.f90:463-511).  Copied to the device; a run
+ * must lie inside the days given. */
+int mhm_set_inflow_discharge(mhm_ctx *ctx, int32_t day0, int32_t n_days, const double *q);
+
 /* Default initial states (fluxes_states_default_init,
  * src/mHM/mo_init_states.f90:258-345, and fluxes_states_default_init_routing,
  * src/mRM/mo_mrm_init.f90:453-499).  horizon_depth[n_horizons] in mm. */
@@ -242,6 +258,18 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
  * one member's cell and routing states); save/load copy on the device,
  * ordered after the context's enqueued work (warm starts without a host
  * round trip). */
+/* Failure status of each member since the last call: status[m] = MHM_OK, or
+ * MHM_ERR_NAN when a state or the total runoff of member m became NaN or
+ * infinite in any step (checked by the cell chain on the integer pipe at no
+ * measurable cost).  Waits for the enqueued work, then clears the flags.
+ * Returns MHM_ERR_NAN if any member failed (message names them), else
+ * MHM_OK.  The reference has no such check -- a non-finite value silently
+ * propagates there (its only error path is error_message -> stop,
+ * src/MPR/mo_multi_param_reg.f90:314,422); here one bad member of a batch
+ * or one bad request of a serving loop can be failed on its own while the
+ * others continue. */
+int mhm_member_status(mhm_ctx *ctx, int32_t *status);
+
 int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots);
 int mhm_snapshot_save(mhm_ctx *ctx, int32_t member, int32_t slot);
 int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member);

@@ -96,7 +96,8 @@ EXPORTS = [
     "mhm_enable_fluxes", "mhm_get_fluxes", "mhm_set_link_fpimp",
     "mhm_enable_flux_state_outputs", "mhm_read_flux_state_outputs", "mhm_enable_routed_outputs",
     "mhm_read_routed_outputs", "mhm_set_output_weights", "mhm_set_link_celerity", "mhm_network_topology",
-    "mhm_poll", "mhm_set_meteo_weights",
+    "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
+    "mhm_member_status",
 ]
 
 _LIB = None
@@ -173,5 +174,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_poll.argtypes = [vp, _ip]
     L.mhm_network_topology.argtypes = [C.c_int32, C.c_int32, _ip, C.c_int32, _ip, _ip, _ip, _ip, _ip, _ip]
     L.mhm_snapshot_load.argtypes = [vp, C.c_int32, C.c_int32]
+    L.mhm_set_inflow_gauges.argtypes = [vp, C.c_int32, _ip, _ip]
+    L.mhm_set_inflow_discharge.argtypes = [vp, C.c_int32, C.c_int32, _dp]
+    L.mhm_member_status.argtypes = [vp, _ip]
     _LIB = L
     return L

@@ -212,6 +212,11 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
             if (o.tt_w) ott_w = o.tt_w[m];
         }
     }
+    // non-finite detection, integer operations only: a double is NaN or Inf
+    // iff its sign-cleared bits are >= 0x7ff0...0, i.e. iff adding 2^52 to
+    // them carries into bit 63; the OR over the steps keeps any such carry
+    constexpr uint64_t kExpOne = 0x0010000000000000ull;
+    uint64_t nonfin = 0;
     auto oadd = [&](int plane, double x) {
         double *q = oacc + (size_t)plane * out_stride;
         *q = *q + x; // OutputVariable%data = data + value, src/common/mo_nc_output.f90:140-149
@@ -444,6 +449,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         // ---- L1_total_runoff, mo_runoff.f90:248-274 ----
         const double q_total = ((base + slow + fast) * c.fnotsealed) + (runoff_sealed * c.fsealed);
         tro[(size_t)t * out_stride] = q_total;
+        nonfin |= hm_abs_bits(hm_d2b(q_total)) + kExpOne;
         if constexpr (FLUX) {
             // mHM_updateDataset, src/mHM/mo_write_fluxes_states.f90:283-438
             if (oon) {
@@ -499,8 +505,19 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
     S[(size_t)S_SEAL * N] = c.seal;
     S[(size_t)S_UNSAT * N] = c.unsat;
     S[(size_t)S_SAT * N] = c.sat;
+    auto chk = [&](double x) { nonfin |= hm_abs_bits(hm_d2b(x)) + kExpOne; };
+    chk(c.interc);
+    chk(c.snow);
+    chk(c.seal);
+    chk(c.unsat);
+    chk(c.sat);
 #pragma unroll 1
-    for (int h = 0; h < H; ++h) S[(size_t)(S_SM + h) * N] = hs(HS_SM, h);
+    for (int h = 0; h < H; ++h) {
+        const double smh = hs(HS_SM, h);
+        S[(size_t)(S_SM + h) * N] = smh;
+        chk(smh);
+    }
+    if (a.nonfinite && (nonfin >> 63)) atomicOr(a.nonfinite + m, 1);
 }
 
 // Launch with H as a template parameter (shared-memory size, loop bounds);

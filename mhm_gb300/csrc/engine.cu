@@ -36,6 +36,7 @@ cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double
 cudaError_t launch_hmath_eval(int op, int64_t n, const double *x, const double *y, double *out, cudaStream_t s);
 cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *sink, cudaStream_t s);
 cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s);
+cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s);
 } // namespace mhm
 
 using namespace mhm;
@@ -124,6 +125,15 @@ struct mhm_ctx {
     double ss_max = 0.0;
     LevelNetwork net;
     std::vector<int32_t> gauge_pos;
+    std::vector<int32_t> link_to;    // [n_links] 0-based node each link drains into
+    DevBuf<int32_t> nonfinite;       // [M] per-member non-finite flags of the cell chain
+    // inflow gauges: position and headwater flag of each, daily discharge
+    int32_t n_inflow = 0, inflow_day0 = 1, inflow_ndays = 0;
+    std::vector<int32_t> inflow_pos;
+    std::vector<int8_t> inflow_hw;
+    DevBuf<int32_t> inflow_pos_d;
+    DevBuf<int8_t> inflow_hw_d;
+    DevBuf<double> inflow_q;
     // device: static
     DevBuf<double> params, states, latitude, l1_area, pos_area, length, slope, ffp, rout_p5;
     DevBuf<double> C1, C2, qtin1, qtr1, qout_last, qmod_last;
@@ -564,6 +574,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
             ctx->net.pos_flags = {2}; // Qmod = qOUT for a single node
         }
         ctx->n_links = ctx->net.n_links;
+        for (int i = 0; i < ctx->n_links; ++i) ctx->link_to.push_back(d->to_n[i] - 1);
         if (ctx->n_links > 0 && (!d->length || !d->slope || !d->ffp_imp)) return bad("link length/slope/fFPimp missing");
         ctx->G = d->n_gauges;
         if (ctx->G < 0 || (ctx->G > 0 && !d->gauge_node)) return bad("gauges");
@@ -618,6 +629,8 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
     bool ok = true;
     ok = ok && ck(ctx->params.ensure(M * n_param_planes((int)H) * N), "params");
     ok = ok && ck(ctx->states.ensure(M * n_state_planes((int)H) * N), "states");
+    ok = ok && ck(ctx->nonfinite.ensure(M), "member flags");
+    if (ok) cudaMemsetAsync(ctx->nonfinite.p, 0, M * sizeof(int32_t), ctx->stream);
     if (ok) {
         cudaMemsetAsync(ctx->params.p, 0, ctx->params.n * sizeof(double), ctx->stream);
         cudaMemsetAsync(ctx->states.p, 0, ctx->states.n * sizeof(double), ctx->stream);
@@ -807,6 +820,52 @@ int mhm_set_meteo_weights(mhm_ctx *ctx, const double *pre_w, const double *pet_w
     return MHM_OK;
 }
 
+int mhm_set_inflow_gauges(mhm_ctx *ctx, int32_t n, const int32_t *node, const int32_t *headwater)
+{
+    if (!ctx || n < 0 || (n > 0 && (!node || !headwater))) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the old flags
+    if (ctx->proc_rout < 1) return fail(ctx, MHM_ERR_INVALID, "routing is off");
+    if (n > kMaxInflow) return fail(ctx, MHM_ERR_UNSUPPORTED, "more than 64 inflow gauges");
+    std::vector<int32_t> pos(n);
+    std::vector<int8_t> hw(n);
+    std::vector<char> cut_node(ctx->L, 0);
+    for (int g = 0; g < n; ++g) {
+        if (node[g] < 1 || node[g] > ctx->L) return fail(ctx, MHM_ERR_INVALID, "inflow gauge node out of range");
+        pos[g] = ctx->net.pos_of_node[node[g] - 1];
+        hw[g] = headwater[g] ? 1 : 0;
+        if (!hw[g]) cut_node[node[g] - 1] = 1;
+    }
+    // links draining into a non-headwater gauge's node lose their routed outflow
+    std::vector<int8_t> flags = ctx->net.pos_flags;
+    for (int i = 0; i < ctx->n_links; ++i)
+        if (cut_node[ctx->link_to[i]]) flags[ctx->net.link_pos[i]] |= 4;
+    CK(upload(ctx->pos_flags, flags.data(), flags.size(), ctx->stream), "flags");
+    if (n > 0) {
+        CK(upload(ctx->inflow_pos_d, pos.data(), pos.size(), ctx->stream), "inflow gauges");
+        CK(upload(ctx->inflow_hw_d, hw.data(), hw.size(), ctx->stream), "inflow gauges");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "inflow sync");
+    ctx->n_inflow = n;
+    ctx->inflow_pos = pos;
+    ctx->inflow_hw = hw;
+    return MHM_OK;
+}
+
+int mhm_set_inflow_discharge(mhm_ctx *ctx, int32_t day0, int32_t n_days, const double *q)
+{
+    if (!ctx || n_days < 0 || (n_days > 0 && !q)) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc;
+    if (ctx->n_inflow < 1) return fail(ctx, MHM_ERR_INVALID, "no inflow gauges: mhm_set_inflow_gauges first");
+    if (day0 < 1) return fail(ctx, MHM_ERR_INVALID, "day0 >= 1 required");
+    CK(upload(ctx->inflow_q, q, (size_t)n_days * ctx->n_inflow, ctx->stream), "inflow discharge");
+    CK(cudaStreamSynchronize(ctx->stream), "inflow sync");
+    ctx->inflow_day0 = day0;
+    ctx->inflow_ndays = n_days;
+    return MHM_OK;
+}
+
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 {
     if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
@@ -990,6 +1049,23 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         const int32_t w = out_advance(*o, ctx->jul_start, ctx->timestep, tt0, n_steps, false);
         if (o->slots + w > o->max_slots)
             return fail(ctx, MHM_ERR_INVALID, "output intervals would exceed the device slots: read the outputs first");
+    }
+    if (ctx->n_inflow > 0 && ctx->proc_rout >= 1) {
+        // the run's days (iDischargeTS) must lie in the inflow discharge series
+        const int32_t sd = 24 / ctx->timestep;
+        int64_t lo = tt0, hi = (int64_t)tt0 + n_steps - 1;
+        if (members) {
+            lo = INT64_MAX;
+            hi = 0;
+            for (size_t m = 0; m < M; ++m)
+                if (member_tt0[m] > 0) {
+                    lo = std::min<int64_t>(lo, member_tt0[m]);
+                    hi = std::max<int64_t>(hi, (int64_t)member_tt0[m] + n_steps - 1);
+                }
+        }
+        if (lo <= hi && ((lo + sd - 1) / sd < ctx->inflow_day0 ||
+                         (hi + sd - 1) / sd > (int64_t)ctx->inflow_day0 + ctx->inflow_ndays - 1))
+            return fail(ctx, MHM_ERR_INVALID, "inflow discharge does not cover the days of the run");
     }
     // member mode reads the first n_steps rows of the device forcing window
     const int32_t first_row = members ? ctx->forc[0].row0 : (tt0 + stride - 1) / stride;
@@ -1204,6 +1280,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.tro = ctx->tro[slot].p;
         a.latitude = ctx->latitude.p;
         a.tab = ctx->tab;
+        a.nonfinite = ctx->nonfinite.p;
         if (ctx->out_flux) {
             a.flux_aet = ctx->flux_d[0].p;
             a.flux_loss = ctx->flux_d[1].p;
@@ -1274,6 +1351,31 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
                 br.done();
                 g_launches++;
             }
+        }
+        if (ctx->proc_rout >= 1 && ctx->n_inflow > 0) {
+            InflowArgs ia{};
+            ia.n_members = ctx->M;
+            ia.n_qsteps = nT / F;
+            ia.n_nodes = ctx->L;
+            ia.n_inflow = ctx->n_inflow;
+            ia.win = F;
+            ia.steps_day = 24 / ctx->timestep;
+            ia.day0 = ctx->inflow_day0;
+            // adaptive routing with a routing step not shorter than the model step:
+            // the routing step's mean (mo_mhm_interface_run.f90:497-510)
+            const double tsf = (ctx->proc_rout >= 2 && ctx->L > 1)
+                                   ? ctx->ts_rout[0] / ((double)ctx->timestep * 3600.0) : 1.0;
+            ia.mean = (ctx->proc_rout >= 2 && ctx->L > 1 && !(tsf < 1.0)) ? 1 : 0;
+            ia.tsf = tsf;
+            ia.tt_base = (int64_t)tt0 + s0;
+            ia.member_step0 = members ? ctx->member_s0_cur : nullptr;
+            ia.step_shift = s0;
+            ia.pos = ctx->inflow_pos_d.p;
+            ia.headwater = ctx->inflow_hw_d.p;
+            ia.q = ctx->inflow_q.p;
+            ia.qout = ctx->qout.p;
+            CK(launch_inflow(ia, rs), "inflow launch");
+            g_launches++;
         }
         CK(cudaEventRecord(ctx->ev_acc_done[slot], rs), "record acc done");
         if (ctx->proc_rout < 1) continue;
@@ -1660,6 +1762,24 @@ int mhm_run(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge)
     int rc = run_enqueue(ctx, tt0, n_steps, q_gauge);
     int rs = mhm_sync(ctx);
     return rc ? rc : rs;
+}
+
+int mhm_member_status(mhm_ctx *ctx, int32_t *status)
+{
+    if (!ctx || !status) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc; // flags of all enqueued steps
+    const size_t M = ctx->M;
+    std::vector<int32_t> f(M, 0);
+    CK(cudaMemcpy(f.data(), ctx->nonfinite.p, M * sizeof(int32_t), cudaMemcpyDeviceToHost), "member flags");
+    CK(cudaMemset(ctx->nonfinite.p, 0, M * sizeof(int32_t)), "member flags");
+    std::string bad;
+    for (size_t m = 0; m < M; ++m) {
+        status[m] = f[m] ? MHM_ERR_NAN : MHM_OK;
+        if (f[m]) bad += (bad.empty() ? "" : ", ") + std::to_string(m);
+    }
+    if (!bad.empty()) return fail(ctx, MHM_ERR_NAN, "non-finite state or runoff in member(s) " + bad);
+    return MHM_OK;
 }
 
 int mhm_enable_fluxes(mhm_ctx *ctx, int32_t on)

@@ -127,6 +127,9 @@ struct CellArgs {
     // lost to (or, karstLoss > 1, gained from) outside the cell
     double *flux_aet, *flux_loss;
     OutArgs out;        // aggregated flux/state outputs (flux variant only)
+    // per-member failure flag: bit 0 set when the member's total runoff of a
+    // step or a state at the chunk's end is not finite (nullptr = not checked)
+    int32_t *nonfinite;
 };
 
 struct AccArgs {
@@ -154,7 +157,8 @@ struct RouteArgs {
     const int32_t *pos_level;   // [n_nodes] topological level of each position
     const int32_t *up_ptr;      // [n_nodes+1]
     const int32_t *up_pos;      // upstream positions in rank order
-    const int8_t *pos_flags;    // bit0: is link (has C1/C2), bit1: add qOUT
+    const int8_t *pos_flags;    // bit0: is link (has C1/C2), bit1: add qOUT, bit2: the link's routed
+                                // outflow is cut (it drains into a non-headwater inflow gauge's node)
     const double *C1, *C2;      // [M][n_nodes] by position
     // routing step s reads qOUT row s / rdiv of [M][n_qsteps][n_nodes]: with an
     // adaptive routing step shorter than the model step the model step's qOUT
@@ -165,6 +169,28 @@ struct RouteArgs {
     double *qmod;               // [M][n_steps][n_nodes] (if write_qmod)
     double *qtin1, *qtr1;       // [M][n_nodes] state (previous step)
     const int32_t *member_step0; // member mode: < 0 marks an idle member (skipped)
+};
+
+// add_inflow (src/mRM/mo_mrm_pre_routing.f90:179-214) on a chunk's qOUT rows,
+// after the L1->L11 accumulation: per (member, routing step) the inflow
+// gauges in list order add their discharge to (headwater) or put it in place
+// of the node's runoff.  The discharge of a model step is the gauge's value
+// of day ceiling(tt / steps_day) (iDischargeTS); with `mean` (adaptive
+// routing whose routing step is not shorter than the model step) it is the
+// sum over the routing step's `win` model steps from 0, divided by tsf
+// (tsRoutFactorIn), src/mHM/mo_mhm_interface_run.f90:463-511.
+constexpr int kMaxInflow = 64;
+struct InflowArgs {
+    int32_t n_members, n_qsteps, n_nodes, n_inflow;
+    int32_t win, steps_day, day0, mean;
+    double tsf;
+    int64_t tt_base;             // model step (1-based) of the chunk's first step
+    const int32_t *member_step0; // member mode: member m's chunk step t is tt = member_step0[m] + step_shift + t + 1
+    int32_t step_shift;
+    const int32_t *pos;          // [n_inflow] routing position of each gauge's node
+    const int8_t *headwater;     // [n_inflow]
+    const double *q;             // [days][n_inflow] from day0
+    double *qout;                // [M][n_qsteps][n_nodes]
 };
 
 // Per-model-step L11 discharge from the routing steps (adaptive routing):

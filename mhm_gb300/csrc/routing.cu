@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
     const int flags = __ldg(a.pos_flags + pos);
     const bool is_link = flags & 1;
     const bool add_qout = flags & 2;
+    const bool cut = flags & 4; // mo_mrm_routing.f90:447-452
     double qtin[SUB];
 #pragma unroll
     for (int t = 0; t < SUB; ++t) qtin[t] = 0.0; // netNode_qTIN(:, IT) = 0
@@ -106,7 +107,8 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
         if (t < nt) {
             const size_t row = base + (size_t)t * L;
             if (is_link) {
-                const double qtr = qtr1 + c1 * (qtin1 - qtr1) + c2 * (qtin[t] - qtin1);
+                double qtr = qtr1 + c1 * (qtin1 - qtr1) + c2 * (qtin[t] - qtin1);
+                if (cut) qtr = 0.0;
                 a.qtr[row + pos] = qtr;
                 qtr1 = qtr;
             }
@@ -116,6 +118,45 @@ __global__ void __launch_bounds__(128) route_tick_kernel(const RouteArgs a)
     }
     a.qtin1[ms + pos] = qtin1;
     a.qtr1[ms + pos] = qtr1;
+}
+
+__global__ void inflow_kernel(const InflowArgs a)
+{
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (int64_t)a.n_members * a.n_qsteps) return;
+    const int m = (int)(gid / a.n_qsteps), s = (int)(gid - (int64_t)m * a.n_qsteps);
+    int64_t tt0 = a.tt_base;
+    if (a.member_step0) {
+        const int32_t b = a.member_step0[m];
+        if (b < 0) return; // idle member
+        tt0 = (int64_t)b + a.step_shift + 1;
+    }
+    tt0 += (int64_t)s * a.win; // first model step of routing step s
+    double *row = a.qout + ((size_t)m * a.n_qsteps + s) * a.n_nodes;
+    for (int g = 0; g < a.n_inflow; ++g) {
+        double Q;
+        if (a.mean) {
+            double acc = 0.0;
+            for (int j = 0; j < a.win; ++j) {
+                const int64_t day = (tt0 + j + a.steps_day - 1) / a.steps_day;
+                acc = acc + __ldg(a.q + (size_t)(day - a.day0) * a.n_inflow + g);
+            }
+            Q = acc / a.tsf;
+        } else {
+            const int64_t day = (tt0 + a.steps_day - 1) / a.steps_day;
+            Q = __ldg(a.q + (size_t)(day - a.day0) * a.n_inflow + g);
+        }
+        double *v = row + __ldg(a.pos + g);
+        *v = a.headwater[g] ? *v + Q : Q;
+    }
+}
+
+cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s)
+{
+    const int64_t n = (int64_t)a.n_members * a.n_qsteps;
+    if (n == 0 || a.n_inflow == 0) return cudaSuccess;
+    inflow_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 __global__ void qmod_step_kernel(const QmodStepArgs a)

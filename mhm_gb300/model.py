@@ -146,6 +146,20 @@ class MhmGpu:
         w = [np.ascontiguousarray(a, np.float64) for a in (pre, pet, temp)]
         self._check(self.L.mhm_set_meteo_weights(self.ctx, *[_d(a) for a in w]), "mhm_set_meteo_weights")
 
+    def set_inflow_gauges(self, node, headwater, q=None, day0: int = 1):
+        """Inflow gauges at the L11 nodes `node` (1-based) with headwater flags,
+        and optionally their daily discharge q[days][gauges] [m3 s-1] from
+        day0 (mhm_set_inflow_gauges / mhm_set_inflow_discharge)."""
+        n = np.ascontiguousarray(node, np.int32)
+        h = np.ascontiguousarray(np.asarray(headwater, bool).astype(np.int32))
+        self._check(self.L.mhm_set_inflow_gauges(self.ctx, n.size, _i(n), _i(h)), "mhm_set_inflow_gauges")
+        if q is not None:
+            self.set_inflow_discharge(q, day0)
+
+    def set_inflow_discharge(self, q, day0: int = 1):
+        a = np.ascontiguousarray(q, np.float64)
+        self._check(self.L.mhm_set_inflow_discharge(self.ctx, day0, a.shape[0], _d(a)), "mhm_set_inflow_discharge")
+
     def set_link_fpimp(self, ffp):
         """Floodplain impervious fraction of the links for a new land-cover scene."""
         a = np.ascontiguousarray(ffp, np.float64)
@@ -367,6 +381,15 @@ class MhmGpu:
 
     def snapshot_load(self, slot: int, member: int):
         self._check(self.L.mhm_snapshot_load(self.ctx, slot, member), "mhm_snapshot_load")
+
+    def member_status(self) -> np.ndarray:
+        """Per-member status since the last call (mhm_member_status): 0, or
+        MHM_ERR_NAN for a member whose states or runoff became non-finite."""
+        st = np.zeros(self.n_members, np.int32)
+        rc = self.L.mhm_member_status(self.ctx, _i(st))
+        if rc not in (0, _lib.MHM_ERR_NAN):
+            self._check(rc, "mhm_member_status")
+        return st
 
     def sync(self):
         self._check(self.L.mhm_sync(self.ctx), "mhm_sync")

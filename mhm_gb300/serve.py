@@ -27,6 +27,22 @@ Forcing: each basin has a device-resident window of `chunk` hourly rows that
 every chunk of every run reads (the synthetic forecast repeats every
 `chunk` steps), so admitting a run at any chunk boundary reads the same
 forcing it would alone.
+
+Failures stay with the request that caused them (the reference's only
+error path is error_message -> stop of the whole program,
+src/MPR/mo_multi_param_reg.f90:314,422):
+  * a request whose parameter vector has the wrong length or non-finite
+    entries, or whose basin alone exceeds the HBM budget, is rejected at
+    submission;
+  * a regionalisation that fails (MhmError) fails that request only;
+  * a member whose states or discharge turn non-finite during a chunk
+    (mhm_member_status) is failed and its slot freed at the chunk boundary;
+  * a request can be cancelled at any time; it leaves at the next chunk
+    boundary of its context;
+  * a request's `on_chunk` consumer (e.g. streaming each chunk's discharge
+    to a client) runs on a worker thread; if it raises, that request is
+    failed and its slot freed at the next boundary.
+The other requests continue and finish with the results they give alone.
 """
 from __future__ import annotations
 
@@ -36,9 +52,11 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from concurrent.futures import Future, ThreadPoolExecutor
+
 from . import params as gparams
 from . import synth
-from .model import MhmGpu
+from .model import MhmError, MhmGpu
 
 
 @dataclass
@@ -64,6 +82,11 @@ class Request:
     admitted: float | None = None
     done: float | None = None
     q: list = field(default_factory=list)
+    status: str = "pending"      # pending, running, done, failed, rejected, cancelled
+    error: str | None = None
+    on_chunk: object = None      # optional consumer f(request, discharge chunk [gauge, step])
+    cancelled: bool = False
+    futures: list = field(default_factory=list)
 
     def discharge(self) -> np.ndarray:
         """Outlet discharge [gauge, step] over the horizon."""
@@ -95,9 +118,11 @@ class Server:
 
     def __init__(self, basins: list[Basin], hbm_budget: float = 150e9, chunk: int = 240, max_slots: int = 16,
                  proc_sm: int = 1, proc_pet: int = 0, spinup_steps: int = 90 * 24, gamma_spinup=None,
-                 autotune: bool = False):
-        import torch
-        self.torch = torch
+                 autotune: bool = False, backend=MhmGpu, window_fn=None, workers: int = 4):
+        """`backend` builds a basin's context (MhmGpu); `window_fn(basin)`
+        gives its forcing window (default: the synthetic forecast window in
+        device memory)."""
+        self.backend = backend
         self.basins = basins
         self.budget = hbm_budget
         self.chunk = chunk
@@ -111,10 +136,12 @@ class Server:
         self.cell_steps = 0
         self.autotune = autotune
         self.tuned: dict[str, dict] = {}
+        self.failed: list[Request] = []      # failed, rejected or cancelled
+        self._cancel: set[int] = set()       # request ids to cancel (filled from any thread)
+        self.pool = ThreadPoolExecutor(max_workers=workers)
         for b in basins:
             if not b.window:
-                f = synth.make_forcing(b.dom, chunk, seed=2)
-                b.window = tuple(torch.from_numpy(f[k]).cuda() for k in ("pre", "temp", "pet"))
+                b.window = window_fn(b) if window_fn else device_window(b.dom, chunk)
             if b.restart is None:
                 b.restart = self._spin_up(b, spinup_steps, gamma_spinup)
 
@@ -122,7 +149,7 @@ class Server:
     def _spin_up(self, b: Basin, steps: int, gamma) -> dict:
         """Default states advanced `steps` hourly steps with the namelist
         parameters: the warm start every request of the basin begins from."""
-        g = MhmGpu(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=1)
+        g = self.backend(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=1)
         try:
             g.mpr_setup(b.l0)
             gam = gamma if gamma is not None else gparams.default_gamma(self.proc_sm, self.proc_pet, 1, b.l0.n_geo)
@@ -144,7 +171,8 @@ class Server:
         need = context_bytes(b, members, self.chunk)
         if self.used + need > self.budget:
             return False
-        g = MhmGpu(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=members, read_states=True)
+        g = self.backend(b.dom, proc_soilmoist=self.proc_sm, proc_pet=self.proc_pet, n_members=members,
+                         read_states=True)
         g.mpr_setup(b.l0)
         g.snapshot_alloc(1)
         g.set_state(b.restart, 0)
@@ -169,8 +197,72 @@ class Server:
         self.used -= c["bytes"]
 
     # ---- the loop ----
+    def _fail(self, r: Request, status: str, error: str | None):
+        r.status, r.error = status, error
+        r.done = (time.perf_counter() - self._t0) if hasattr(self, "_t0") else 0.0
+        self.failed.append(r)
+
     def submit(self, r: Request):
+        """Queue a request; malformed ones are rejected here."""
+        b = self.basins[r.basin] if 0 <= r.basin < len(self.basins) else None
+        if b is None:
+            return self._fail(r, "rejected", "unknown basin")
+        n_gamma = int(gparams.offsets(self.proc_sm, self.proc_pet, 1, b.l0.n_geo)[10])
+        g = np.asarray(r.gamma, np.float64)
+        if g.shape != (n_gamma,):
+            return self._fail(r, "rejected", f"parameter vector has shape {g.shape}, expected ({n_gamma},)")
+        if not np.all(np.isfinite(g)):
+            return self._fail(r, "rejected", "parameter vector has non-finite entries")
+        if r.horizon < 1:
+            return self._fail(r, "rejected", "horizon must be at least one step")
+        if context_bytes(b, 1, self.chunk) > self.budget:
+            return self._fail(r, "rejected", "the basin alone exceeds the HBM budget")
         self.waiting.append(r)
+
+    def cancel(self, rid: int):
+        """Cancel a request (callable from any thread, e.g. a consumer): the
+        loop drops a waiting request at its next pass and a running one at
+        its context's next chunk boundary."""
+        self._cancel.add(rid)
+
+    def _apply_cancels(self):
+        if not self._cancel:
+            return
+        rids = set(self._cancel)
+        self._cancel -= rids
+        still = []
+        for r in self.waiting:
+            if r.rid in rids:
+                r.cancelled = True
+                self._fail(r, "cancelled", None)
+            else:
+                still.append(r)
+        self.waiting = still
+        for c in self.ctx.values():
+            for r in c["slots"]:
+                if r is not None and r.rid in rids:
+                    r.cancelled = True
+
+    def _release(self, c: dict, m: int):
+        """Free slot m of a context whose chunk is not in flight."""
+        r = c["slots"][m]
+        c["slots"][m] = None
+        c["tt0"][m] = 0
+        return r
+
+    def _sweep(self, c: dict):
+        """At a chunk boundary: slots of cancelled requests and of requests
+        whose consumer raised are freed."""
+        for m, r in enumerate(c["slots"]):
+            if r is None:
+                continue
+            err = next((f.exception() for f in r.futures if f.done() and f.exception() is not None), None)
+            if r.cancelled:
+                self._release(c, m)
+                self._fail(r, "cancelled", None)
+            elif err is not None:
+                self._release(c, m)
+                self._fail(r, "failed", f"chunk consumer raised {type(err).__name__}: {err}")
 
     def _admit(self, now: float):
         still = []
@@ -199,11 +291,16 @@ class Server:
                 still.append(r)
                 continue
             g = c["g"]
-            g.mpr(r.gamma, member0=slot)
+            try:
+                g.mpr(r.gamma, member0=slot)
+            except MhmError as e:          # this request only
+                self._fail(r, "failed", f"regionalisation failed: {e}")
+                continue
             g.snapshot_load(0, slot)
             c["slots"][slot] = r
             c["tt0"][slot] = 1
             r.admitted = now
+            r.status = "running"
         self.waiting = still
 
     def step(self, now: float) -> bool:
@@ -213,6 +310,10 @@ class Server:
         completed (mhm_poll, no waiting) is finished and can take its next
         chunk and new requests at once -- a small basin is not held back by
         the chunk of a large one."""
+        self._apply_cancels()
+        for c in self.ctx.values():
+            if not c["busy"]:
+                self._sweep(c)
         self._admit(now)
         for bi, c in self.ctx.items():
             if c["busy"] or not any(s is not None for s in c["slots"]):
@@ -229,6 +330,7 @@ class Server:
             if not c["g"].poll():
                 continue
             c["g"].sync()                          # host side of the chunk (gauge series)
+            status = c["g"].member_status()        # non-finite members of this chunk
             c["busy"] = False
             progressed = True
             t_done = time.perf_counter()
@@ -236,11 +338,19 @@ class Server:
             for m, r in enumerate(c["slots"]):
                 if r is None or c["tt0_now"][m] <= 0:
                     continue
-                r.q.append(c["q"][m].copy())
+                if status[m] != 0:
+                    self._release(c, m)
+                    self._fail(r, "failed", "non-finite states or discharge")
+                    continue
+                chunk_q = c["q"][m].copy()
+                r.q.append(chunk_q)
+                if r.on_chunk is not None:
+                    r.futures.append(self.pool.submit(r.on_chunk, r, chunk_q))
                 self.cell_steps += n * self.chunk
                 c["tt0"][m] += self.chunk
                 if c["tt0"][m] - 1 >= r.horizon:
                     r.done = t_done - self._t0
+                    r.status = "done"
                     self.finished.append(r)
                     c["slots"][m] = None
         if not progressed:
@@ -251,9 +361,9 @@ class Server:
     def serve(self, requests: list[Request], timeout_s: float = 600.0) -> dict:
         """Run until every request is finished; arrivals follow their
         `arrival` offsets in wall-clock time."""
+        self._t0 = time.perf_counter()
         for r in requests:
             self.submit(r)
-        self._t0 = time.perf_counter()
         while (self.waiting or any(any(s is not None for s in c["slots"]) for c in self.ctx.values())):
             now = time.perf_counter() - self._t0
             if now > timeout_s:
@@ -264,11 +374,28 @@ class Server:
         wall = time.perf_counter() - self._t0
         for bi in list(self.ctx):
             self._close(bi)
-        return summarize(self.finished, wall, self.cell_steps)
+        # a consumer that raised on a request's last chunk fails it too
+        for r in list(self.finished):
+            err = next((f.exception() for f in r.futures if f.exception() is not None), None)
+            if err is not None:
+                self.finished.remove(r)
+                r.status, r.error = "failed", f"chunk consumer raised {type(err).__name__}: {err}"
+                self.failed.append(r)
+        out = summarize(self.finished, wall, self.cell_steps)
+        out["failed"] = len(self.failed)
+        return out
 
     def close(self):
         for bi in list(self.ctx):
             self._close(bi)
+        self.pool.shutdown(wait=True)
+
+
+def device_window(dom, chunk: int) -> tuple:
+    """The synthetic forecast window of a basin in device memory."""
+    import torch
+    f = synth.make_forcing(dom, chunk, seed=2)
+    return tuple(torch.from_numpy(f[k]).cuda() for k in ("pre", "temp", "pet"))
 
 
 def summarize(done: list[Request], wall: float, cell_steps: int) -> dict:

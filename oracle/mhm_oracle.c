@@ -558,10 +558,28 @@ void ora_L11_runoff_acc(int nCells, int nNodes, const double *qAll, const double
     }
 }
 
-/* src/mRM/mo_mrm_routing.f90:380-481 (no inflow gauges) */
-void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN,
-                     const int32_t *toN, const double *C1, const double *C2, const double *qOUT,
-                     double *qTIN, double *qTR, double *Qmod)
+/* add_inflow, src/mRM/mo_mrm_pre_routing.f90:179-214: gauges in list order;
+ * a headwater gauge adds its discharge to the node's runoff, any other one
+ * replaces it */
+void ora_add_inflow(int nInflowGauges, const int32_t *InflowHeadwater, const int32_t *InflowNodeList,
+                    const double *QInflow, double *qOut)
+{
+    for (int ii = 0; ii < nInflowGauges; ++ii) {
+        const int v = InflowNodeList[ii] - 1;
+        if (InflowHeadwater[ii])
+            qOut[v] = qOut[v] + QInflow[ii];
+        else
+            qOut[v] = QInflow[ii];
+    }
+}
+
+/* src/mRM/mo_mrm_routing.f90:380-481: links in netPerm order; the routed
+ * outflow of a link that drains into a non-headwater inflow gauge's node is
+ * cut (:447-452) */
+void ora_L11_routing_ex(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN, const int32_t *toN,
+                        const double *C1, const double *C2, const double *qOUT, int nInflowGauges,
+                        const int32_t *InflowHeadwater, const int32_t *InflowNodeList, double *qTIN, double *qTR,
+                        double *Qmod)
 {
     double *qTIN1 = qTIN, *qTIN2 = qTIN + nNodes; /* columns IT1 = 1, IT = 2 */
     double *qTR1 = qTR, *qTR2 = qTR + nNodes;
@@ -574,6 +592,9 @@ void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32
         qTIN2[iNode] = qTIN2[iNode] + qOUT[iNode];
         qTR2[iNode] = qTR1[iNode] + C1[i] * (qTIN1[iNode] - qTR1[iNode]) +
                       C2[i] * (qTIN2[iNode] - qTIN1[iNode]);
+        for (int g = 0; g < nInflowGauges; ++g)
+            if (tNode == InflowNodeList[g] - 1 && !InflowHeadwater[g])
+                qTR2[iNode] = 0.0;
         qTIN2[tNode] = qTIN2[tNode] + qTR2[iNode];
     }
     if (nLinks > 0) {
@@ -585,6 +606,14 @@ void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32
         qTR1[i] = qTR2[i];
         qTIN1[i] = qTIN2[i];
     }
+}
+
+/* src/mRM/mo_mrm_routing.f90:380-481 (no inflow gauges) */
+void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN,
+                     const int32_t *toN, const double *C1, const double *C2, const double *qOUT,
+                     double *qTIN, double *qTR, double *Qmod)
+{
+    ora_L11_routing_ex(nNodes, nLinks, netPerm, fromN, toN, C1, C2, qOUT, 0, NULL, NULL, qTIN, qTR, Qmod);
 }
 
 /* moveDownOneCell, src/mRM/mo_mrm_net_startup.f90:1768-1801 */
@@ -972,6 +1001,28 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
         free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
         return -2;
     }
+    /* inflow gauges: the step's InflowDischarge = InflowGauge%Q(iDischargeTS, :),
+     * iDischargeTS = ceiling(tt / nTstepDay) (src/mHM/mo_mhm_interface_run.f90:463-511);
+     * with a routing step of several model steps summed from 0 and divided by
+     * tsRoutFactorIn, then reset after routing (:602-611) */
+    const int nIn = (d->proc_rout >= 1) ? d->nInflow : 0;
+    const int32_t steps_day = 24 / d->timestep;
+    double qin[64], qin_acc[64];
+    if (nIn > 64) {
+        free(qacc); free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
+        return -5;
+    }
+    for (int g = 0; g < nIn; ++g) {
+        qin[g] = 0.0;
+        qin_acc[g] = 0.0;
+    }
+    if (nIn > 0) {
+        const int32_t day_a = (tt0 + steps_day - 1) / steps_day, day_b = (tt0 + nT - 1 + steps_day - 1) / steps_day;
+        if (day_a < d->inflow_day0 || day_b > d->inflow_day0 + d->inflow_ndays - 1) {
+            free(qacc); free(cal); free(pet_calc); free(temp_calc); free(prec_calc); free(tro);
+            return -5; /* inflow discharge does not cover the run */
+        }
+    }
 
     for (int32_t it = 0; it < nT; ++it) {
         const int32_t tt = tt0 + it;
@@ -1165,12 +1216,15 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
             memcpy(total_runoff_out + (size_t)it * N, tro, sizeof(double) * (size_t)N);
 
         /* mRM_routing, processCase 1 (mo_mrm_routing.f90:104-303): rout_loop = 1; case 2 below */
+        const double *qday = nIn > 0 ? d->inflow_q + (size_t)((tt + steps_day - 1) / steps_day - d->inflow_day0) * nIn
+                                     : NULL;
         if (d->proc_rout == 1) {
             ora_L11_runoff_acc(N, L, tro, d->l1_area_km2, d->l1_l11_id, d->l11_area_km2, d->l11_l1_id,
                                d->timestep, d->map_flag, s->qOUT);
+            ora_add_inflow(nIn, d->inflow_headwater, d->inflow_node, qday, s->qOUT);
             if (L > 1) {
-                ora_L11_routing(L, nLinks, d->net_perm, d->from_n, d->to_n, s->C1, s->C2, s->qOUT, s->qTIN,
-                                s->qTR, s->Qmod);
+                ora_L11_routing_ex(L, nLinks, d->net_perm, d->from_n, d->to_n, s->C1, s->C2, s->qOUT, nIn,
+                                   d->inflow_headwater, d->inflow_node, s->qTIN, s->qTR, s->Qmod);
                 /* L11_qMod = L11_qAcc / real(rout_loop): (0 + Qmod) / 1 */
                 for (int i = 0; i < L; ++i)
                     s->Qmod[i] = (0.0 + s->Qmod[i]) / 1.0;
@@ -1192,15 +1246,28 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
                 ts_rout = d->timestep * win;
                 run = s->run_to_rout;
             }
+            if (ts_factor < 1.0) {
+                for (int g = 0; g < nIn; ++g)
+                    qin[g] = qday[g];
+            } else { /* summed over the routing step, then a mean (:503-510) */
+                for (int g = 0; g < nIn; ++g)
+                    qin_acc[g] = qin_acc[g] + qday[g];
+                if (route_now)
+                    for (int g = 0; g < nIn; ++g)
+                        qin[g] = qin_acc[g] / ts_factor;
+            }
             if (route_now) {
                 ora_L11_runoff_acc(N, L, run, d->l1_area_km2, d->l1_l11_id, d->l11_area_km2, d->l11_l1_id,
                                    ts_rout, d->map_flag, s->qOUT);
+                ora_add_inflow(nIn, d->inflow_headwater, d->inflow_node, qin, s->qOUT);
+                for (int g = 0; g < nIn; ++g)
+                    qin_acc[g] = 0.0;
                 if (L > 1) {
                     for (int i = 0; i < L; ++i)
                         qacc[i] = 0.0;
                     for (int r = 0; r < rout_loop; ++r) { /* mo_mrm_routing.f90:238-277 */
-                        ora_L11_routing(L, nLinks, d->net_perm, d->from_n, d->to_n, s->C1, s->C2, s->qOUT,
-                                        s->qTIN, s->qTR, s->Qmod);
+                        ora_L11_routing_ex(L, nLinks, d->net_perm, d->from_n, d->to_n, s->C1, s->C2, s->qOUT,
+                                           nIn, d->inflow_headwater, d->inflow_node, s->qTIN, s->qTR, s->Qmod);
                         for (int i = 0; i < L; ++i)
                             qacc[i] = qacc[i] + s->Qmod[i];
                     }

@@ -89,6 +89,14 @@ void ora_L11_runoff_acc(int nCells, int nNodes, const double *qAll, const double
 void ora_L11_routing(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN,
                      const int32_t *toN, const double *C1, const double *C2, const double *qOUT,
                      double *qTIN, double *qTR, double *Qmod);
+/* src/mRM/mo_mrm_pre_routing.f90:179-214 */
+void ora_add_inflow(int nInflowGauges, const int32_t *InflowHeadwater, const int32_t *InflowNodeList,
+                    const double *QInflow, double *qOut);
+/* L11_routing with inflow gauges (src/mRM/mo_mrm_routing.f90:380-481) */
+void ora_L11_routing_ex(int nNodes, int nLinks, const int32_t *netPerm, const int32_t *fromN, const int32_t *toN,
+                        const double *C1, const double *C2, const double *qOUT, int nInflowGauges,
+                        const int32_t *InflowHeadwater, const int32_t *InflowNodeList, double *qTIN, double *qTR,
+                        double *Qmod);
 /* L11_set_network_topology: links from the L11 D8 directions (mRM codes). fDir11 and
  * the returned ids use the L11 grid packed column-major over the mask (cells 1..nCells),
  * cellCoor[k] = (row, col) 1-based.  Returns nLinks; fromN/toN sized nCells. */
@@ -139,6 +147,12 @@ typedef struct {
     /* read_meteo_weights: hourly weights L1_{pre,pet,temp}_weights(cell, month, hour),
      * [24][12][nCells]; NULL: day/night ratios */
     const double *pre_w, *pet_w, *temp_w;
+    /* inflow gauges (mRM InflowGauge): L11 node (1-based) and headwater flag of
+     * each, and their daily discharge [m3 s-1], inflow_q[(day - inflow_day0) * nInflow + g]
+     * for days inflow_day0 .. inflow_day0 + inflow_ndays - 1 (day = iDischargeTS) */
+    int32_t nInflow, inflow_day0, inflow_ndays, pad2_;
+    const int32_t *inflow_node, *inflow_headwater;
+    const double *inflow_q;
 } ora_domain;
 
 typedef struct {

@@ -37,6 +37,8 @@ class OraDomain(C.Structure):
         ("net_perm", _ip), ("from_n", _ip), ("to_n", _ip), ("length", _dp), ("slope", _dp),
         ("ffp_imp", _dp), ("rout_param", _dp), ("gauge_node", _ip), ("latitude", _dp), ("link_celerity", _dp),
         ("pre_w", _dp), ("pet_w", _dp), ("temp_w", _dp),
+        ("nInflow", C.c_int32), ("inflow_day0", C.c_int32), ("inflow_ndays", C.c_int32), ("pad2_", C.c_int32),
+        ("inflow_node", _ip), ("inflow_headwater", _ip), ("inflow_q", _dp),
     ]
 
 
@@ -164,6 +166,7 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_update_param_case2.restype = d
     L.ora_update_param_links.argtypes = [_dp, d, _dp, C.c_int, _dp, _dp]
     L.ora_update_param_links.restype = d
+    L.ora_add_inflow.argtypes = [C.c_int, _ip, _ip, _dp, _dp]
     L.ora_link_celerity.argtypes = [d, _dp, C.c_int]
     L.ora_link_celerity.restype = d
     L.ora_run.argtypes = [C.POINTER(OraDomain), C.POINTER(OraParams), C.POINTER(OraState),
@@ -212,7 +215,8 @@ class OracleRun:
     """The mhm_eval time loop of one basin on the CPU (oracle)."""
 
     def __init__(self, dom, params: dict, rout_param=None, proc_sm=1, proc_pet=0, proc_rout=1,
-                 hourly=True, read_states=False, kind="hmath", link_celerity=None, meteo_weights=None):
+                 hourly=True, read_states=False, kind="hmath", link_celerity=None, meteo_weights=None,
+                 inflow=None):
         self.L = load(kind)
         self.dom = dom
         self.keep = []
@@ -239,6 +243,14 @@ class OracleRun:
         d.rout_param = _d(rp)
         if link_celerity is not None:
             d.link_celerity = _d(k(link_celerity))
+        if inflow is not None:   # {"node": [G] 1-based L11 ids, "headwater": [G], "day0": d, "q": [days][G]}
+            d.nInflow = len(inflow["node"])
+            d.inflow_node = _i(k(inflow["node"], np.int32))
+            d.inflow_headwater = _i(k(inflow["headwater"], np.int32))
+            q = k(inflow["q"])
+            d.inflow_day0 = int(inflow.get("day0", 1))
+            d.inflow_ndays = q.shape[0]
+            d.inflow_q = _d(q)
         if meteo_weights is not None:   # {"pre", "pet", "temp"}: [24][12][n_cells] each
             for n in ("pre", "pet", "temp"):
                 setattr(d, n + "_w", _d(k(meteo_weights[n])))
