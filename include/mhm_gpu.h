@@ -254,6 +254,26 @@ int mhm_run_members_async(mhm_ctx *ctx, const int32_t *member_tt0, int32_t n_ste
  * in (variant, sub-chunk) order. */
 int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out);
 
+/* How a context launches its work (no counterpart in the reference). */
+typedef struct mhm_launch_config {
+    int32_t cell_blocks_per_sm; /* cell-chain register variant: 4, 6 or 8 resident blocks per SM */
+    int32_t route_sub_steps;    /* steps per routing wavefront sub-chunk, 1..16 */
+    int32_t chunk_steps;        /* most time steps per chunk (0: the device-memory budget decides) */
+    int32_t pad_;
+} mhm_launch_config;
+int mhm_set_launch_config(mhm_ctx *ctx, const mhm_launch_config *cfg);
+int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg);
+/* mhm_autotune over one more knob, the time-chunk length: each of the
+ * n_chunk_choices chunk lengths (0 = as the memory budget allows; at most 8)
+ * is tried with every register variant and routing sub-chunk.  A run is
+ * split into chunks whose routing overlaps the next chunk's cell chain, so
+ * shorter chunks trade launches for overlap.  n_chunk_choices = 0 keeps the
+ * context's chunk length.  ms_out (may be NULL) receives 9 trial times per
+ * chunk length, in (chunk length, variant, sub-chunk) order; best_out the
+ * configuration kept. */
+int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_choices,
+                    const int32_t *chunk_choices, mhm_launch_config *best_out, double *ms_out);
+
 /* Device-resident restart states: n_slots snapshot slots per context (each
  * one member's cell and routing states); save/load copy on the device,
  * ordered after the context's enqueued work (warm starts without a host
@@ -494,7 +514,8 @@ int64_t mhm_kernel_launch_count(void);
 
 /* Elementary-function check: evaluates hmath log/exp/pow of n inputs on the
  * device (where == 1) or the host (where == 0): op 0 log(x), 1 exp(x),
- * 2 pow(x, y).  Used by the tests to show host and device bit-equality. */
+ * 2 pow(x, y), 3 x / y.  Used by the tests to show host and device
+ * bit-equality. */
 int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const double *y, double *out);
 
 /* FP64 issue-rate probe: dependent DFMA chains on every SM for `iters`

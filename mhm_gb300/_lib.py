@@ -76,6 +76,12 @@ class L0Desc(C.Structure):
     ]
 
 
+class LaunchConfig(C.Structure):
+    """mhm_launch_config."""
+    _fields_ = [("cell_blocks_per_sm", C.c_int32), ("route_sub_steps", C.c_int32), ("chunk_steps", C.c_int32),
+                ("pad_", C.c_int32)]
+
+
 class OutputConfig(C.Structure):
     """mhm_output_config: aggregated flux/state (or Qrouted) outputs."""
     _fields_ = [
@@ -97,7 +103,7 @@ EXPORTS = [
     "mhm_enable_flux_state_outputs", "mhm_read_flux_state_outputs", "mhm_enable_routed_outputs",
     "mhm_read_routed_outputs", "mhm_set_output_weights", "mhm_set_link_celerity", "mhm_network_topology",
     "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
-    "mhm_member_status",
+    "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
 ]
 
 _LIB = None
@@ -177,5 +183,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_set_inflow_gauges.argtypes = [vp, C.c_int32, _ip, _ip]
     L.mhm_set_inflow_discharge.argtypes = [vp, C.c_int32, C.c_int32, _dp]
     L.mhm_member_status.argtypes = [vp, _ip]
+    L.mhm_set_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
+    L.mhm_get_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
+    L.mhm_autotune_ex.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _ip, C.POINTER(LaunchConfig), _dp]
     _LIB = L
     return L

@@ -188,6 +188,7 @@ struct mhm_ctx {
     bool route_graphs_on = true;
     std::vector<RouteGraph> route_graphs; // most recently used last
     int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
+    int32_t chunk_cap = 0; // most time steps per chunk (0: the device-memory budget decides)
     // routing case 2: per-member routing time step [s] and the link lengths
     std::vector<double> ts_rout, length_h;
     DevBuf<double> qmod_sub;
@@ -1089,6 +1090,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     // chunk length from the total-runoff budget (two slots)
     const size_t per_step = M * N * sizeof(double);
     int32_t Tc = (int32_t)std::max<size_t>(1, std::min<size_t>((size_t)n_steps, ctx->chunk_bytes / (2 * per_step)));
+    if (ctx->chunk_cap > 0) Tc = std::min(Tc, ctx->chunk_cap);
     if (!on_device) Tc = std::max<int32_t>(stride, Tc / stride * stride); // whole forcing rows per chunk
     // routing case 2: routing time step shorter than the model step -> R routing
     // passes per step; longer -> one pass per window of F steps
@@ -1678,9 +1680,37 @@ int mhm_snapshot_save(mhm_ctx *ctx, int32_t member, int32_t slot) { return snaps
 
 int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member) { return snapshot_copy(ctx, member, slot, false); }
 
-int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out)
+int mhm_set_launch_config(mhm_ctx *ctx, const mhm_launch_config *cfg)
 {
-    if (!ctx || n_steps < 1) return MHM_ERR_INVALID;
+    if (!ctx || !cfg) return MHM_ERR_INVALID;
+    if (cfg->cell_blocks_per_sm != 4 && cfg->cell_blocks_per_sm != 6 && cfg->cell_blocks_per_sm != 8)
+        return fail(ctx, MHM_ERR_INVALID, "cell_blocks_per_sm must be 4, 6 or 8");
+    if (cfg->route_sub_steps < 1 || cfg->route_sub_steps > 16)
+        return fail(ctx, MHM_ERR_INVALID, "route_sub_steps must be 1..16");
+    if (cfg->chunk_steps < 0) return fail(ctx, MHM_ERR_INVALID, "chunk_steps must be >= 0");
+    if (int rc = mhm_sync(ctx)) return rc;
+    ctx->cell_occ = cfg->cell_blocks_per_sm;
+    ctx->route_sub = cfg->route_sub_steps;
+    ctx->chunk_cap = cfg->chunk_steps;
+    return MHM_OK;
+}
+
+int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg)
+{
+    if (!ctx || !cfg) return MHM_ERR_INVALID;
+    cfg->cell_blocks_per_sm = ctx->cell_occ;
+    cfg->route_sub_steps = ctx->route_sub;
+    cfg->chunk_steps = ctx->chunk_cap;
+    cfg->pad_ = 0;
+    return MHM_OK;
+}
+
+int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_choices, const int32_t *chunk_choices,
+                    mhm_launch_config *best_out, double *ms_out)
+{
+    if (!ctx || n_steps < 1 || n_chunk_choices < 0 || n_chunk_choices > 8 ||
+        (n_chunk_choices > 0 && !chunk_choices))
+        return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t N = ctx->N, M = ctx->M, L = ctx->L, ns = n_state_planes(ctx->H);
@@ -1705,22 +1735,37 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
     ctx->out_tro = ctx->out_qmod = ctx->out_flux = 0;
     const bool fso_on = ctx->fso.on, qro_on = ctx->qro.on; // trials add nothing to the outputs
     ctx->fso.on = ctx->qro.on = false;
-    const int32_t occ0 = ctx->cell_occ, sub0 = ctx->route_sub;
+    const int32_t occ0 = ctx->cell_occ, sub0 = ctx->route_sub, cap0 = ctx->chunk_cap;
     int rc = copy_states(true);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int occs[3] = {4, 6, 8}, subs[3] = {4, 8, 16};
+    std::vector<int32_t> caps = {cap0};
+    for (int i = 0; i < n_chunk_choices; ++i) caps.push_back(std::max<int32_t>(0, chunk_choices[i]));
+    if (n_chunk_choices > 0) caps.erase(caps.begin());
+    const int nc = (int)caps.size(), n_trials = 9 * nc;
     float best = 1e30f;
-    int best_occ = occ0, best_sub = sub0;
+    int best_occ = occ0, best_sub = sub0, best_cap = cap0;
     // untimed warm-ups first, so that no timed trial pays a first use: module
     // loading of each kernel variant and the capture of each routing graph
-    const int warm[5] = {0, 1, 2, 3, 6}; // (4,4) (4,8) (4,16) (6,4) (8,4)
-    for (int trial = -5; rc == MHM_OK && trial < 9; ++trial) {
-        const int ti = trial < 0 ? warm[trial + 5] : trial;
-        ctx->cell_occ = occs[ti / 3];
-        ctx->route_sub = rout ? subs[ti % 3] : sub0;
-        if (!rout && ti % 3 != 0) continue;
+    // (every routing sub-chunk with every chunk length)
+    std::vector<int> warm;
+    for (int c = 0; c < nc; ++c)
+        for (int j = 0; j < 3; ++j) warm.push_back(c * 9 + j);     // (4, sub) for each chunk length
+    warm.push_back(3);                                            // (6, 4)
+    warm.push_back(6);                                            // (8, 4)
+    const int nw = (int)warm.size();
+    for (int trial = -nw; rc == MHM_OK && trial < n_trials; ++trial) {
+        const int ti = trial < 0 ? warm[trial + nw] : trial;
+        const int c = ti / 9, v = ti % 9;
+        ctx->cell_occ = occs[v / 3];
+        ctx->route_sub = rout ? subs[v % 3] : sub0;
+        ctx->chunk_cap = caps[c];
+        if (!rout && v % 3 != 0) {
+            if (trial >= 0 && ms_out) ms_out[trial] = -1.0;
+            continue;
+        }
         if ((rc = copy_states(false))) break;
         cudaEventRecord(e0, ctx->stream);
         if ((rc = run_enqueue(ctx, tt0, n_steps, nullptr))) break;
@@ -1737,12 +1782,14 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
             best = ms;
             best_occ = ctx->cell_occ;
             best_sub = ctx->route_sub;
+            best_cap = ctx->chunk_cap;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx->cell_occ = rc == MHM_OK ? best_occ : occ0;
     ctx->route_sub = rc == MHM_OK ? best_sub : sub0;
+    ctx->chunk_cap = rc == MHM_OK ? best_cap : cap0;
     ctx->out_tro = out_t;
     ctx->out_qmod = out_q;
     ctx->out_flux = out_f;
@@ -1750,8 +1797,17 @@ int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, i
     ctx->qro.on = qro_on;
     if (int r2 = copy_states(false)) rc = rc ? rc : r2;
     if (int r3 = mhm_sync(ctx)) rc = rc ? rc : r3;
-    if (occ_out) *occ_out = ctx->cell_occ;
-    if (sub_out) *sub_out = ctx->route_sub;
+    if (best_out) mhm_get_launch_config(ctx, best_out);
+    return rc;
+}
+
+int mhm_autotune(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *occ_out, int32_t *sub_out, double *ms_out)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    mhm_launch_config b{};
+    const int rc = mhm_autotune_ex(ctx, tt0, n_steps, 0, nullptr, &b, ms_out);
+    if (occ_out) *occ_out = b.cell_blocks_per_sm;
+    if (sub_out) *sub_out = b.route_sub_steps;
     return rc;
 }
 

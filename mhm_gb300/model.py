@@ -373,6 +373,28 @@ class MhmGpu:
         self._check(self.L.mhm_autotune(self.ctx, tt0, n_steps, C.byref(occ), C.byref(sub), _d(ms)), "mhm_autotune")
         return {"cell_blocks_per_sm": occ.value, "route_sub_steps": sub.value, "trial_ms": ms.tolist()}
 
+    def autotune_ex(self, tt0: int, n_steps: int, chunk_choices=()) -> dict:
+        """The autotuner over register variant x routing sub-chunk x time-chunk
+        length (mhm_autotune_ex); returns the configuration kept."""
+        ch = np.ascontiguousarray(chunk_choices, np.int32)
+        nc = max(1, ch.size)
+        ms = np.zeros(9 * nc)
+        best = _lib.LaunchConfig()
+        self._check(self.L.mhm_autotune_ex(self.ctx, tt0, n_steps, ch.size, _i(ch) if ch.size else None,
+                                           C.byref(best), _d(ms)), "mhm_autotune_ex")
+        return {"cell_blocks_per_sm": best.cell_blocks_per_sm, "route_sub_steps": best.route_sub_steps,
+                "chunk_steps": best.chunk_steps, "trial_ms": ms.tolist()}
+
+    def set_launch_config(self, cell_blocks_per_sm: int = 4, route_sub_steps: int = 8, chunk_steps: int = 0):
+        cfg = _lib.LaunchConfig(cell_blocks_per_sm, route_sub_steps, chunk_steps, 0)
+        self._check(self.L.mhm_set_launch_config(self.ctx, C.byref(cfg)), "mhm_set_launch_config")
+
+    def get_launch_config(self) -> dict:
+        cfg = _lib.LaunchConfig()
+        self._check(self.L.mhm_get_launch_config(self.ctx, C.byref(cfg)), "mhm_get_launch_config")
+        return {"cell_blocks_per_sm": cfg.cell_blocks_per_sm, "route_sub_steps": cfg.route_sub_steps,
+                "chunk_steps": cfg.chunk_steps}
+
     def snapshot_alloc(self, n_slots: int):
         self._check(self.L.mhm_snapshot_alloc(self.ctx, n_slots), "mhm_snapshot_alloc")
 
