@@ -473,10 +473,12 @@ def run_serving(args) -> dict:
 def run_uneven(args) -> dict:
     """Batched uneven basins: 64 basins with cell counts log-uniform in
     1e3..2.5e5, 2-6 soil horizons, 90..730-day hourly horizons, each with its
-    own D8 network, all submitted at once; every basin's context is
-    autotuned (register variant, routing sub-chunk) on its first chunk.  The
-    server runs the basins' contexts side by side on their own streams
-    within the 150 GB budget; the plain path runs them one after another."""
+    own D8 network, all submitted at once.  Fused (the headline): rounds of
+    one chunk, each ONE persistent cell-chain launch over every basin still
+    running (a device work queue of tiles), routing per basin on its own
+    streams (serve.run_batched).  Side by side: the serving loop, one launch
+    per basin context (autotuned per basin).  Plain: the basins one after
+    another."""
     import torch
     from mhm_gb300 import serve
     torch.cuda.set_device(0)
@@ -489,18 +491,33 @@ def run_uneven(args) -> dict:
         days = int(rng.integers(90, 731))
         reqs.append(serve.Request(rid=i, basin=i, gamma=g, horizon=24 * days))
         reqs_p.append(serve.Request(rid=i, basin=i, gamma=g, horizon=24 * days))
+    def fresh():
+        return [serve.Request(rid=r.rid, basin=r.basin, gamma=r.gamma, horizon=r.horizon) for r in reqs]
+
+    # fused: rounds of one persistent cell-chain launch over every basin
+    # still running (a device work queue of tiles), routing per basin
+    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=1, spinup_steps=0)   # spin-up / windows
+    srv.close()
+    fused = serve.run_batched(basins, reqs, 240)
+    # side by side: the serving loop, one launch per basin context on its own streams
+    reqs_s = fresh()
     srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=1, spinup_steps=0, autotune=True)
-    batched = srv.serve(reqs, timeout_s=3000)
+    streams = srv.serve(reqs_s, timeout_s=3000)
+    tuned = srv.tuned
+    srv.close()
     plain = serve.serve_plain(basins, reqs_p, 240)
-    same = all(np.array_equal(a.discharge(), b.discharge()) for a, b in zip(reqs, reqs_p))
+    same = all(np.array_equal(a.discharge(), b.discharge()) and np.array_equal(a.discharge(), c.discharge())
+               for a, b, c in zip(reqs, reqs_p, reqs_s))
     cells = [b.n_cells for b in basins]
     return {"metric": "batched uneven basins: cell-timesteps/s (mHM+mRM, FP64)", "unit": UNIT,
             "basins": len(basins), "cells_min": int(min(cells)), "cells_max": int(max(cells)),
+            "horizons": [b.dom.n_horizons for b in basins],
             "routing_levels": [b.dom.depth_stats()[0] for b in basins],
-            "value": batched["throughput"], "plain_value": plain["throughput"],
-            "speedup_vs_plain": batched["throughput"] / plain["throughput"],
-            "makespan_s": batched["wall_s"], "plain_makespan_s": plain["wall_s"], "results_identical": bool(same),
-            "autotune": srv.tuned}
+            "value": fused["throughput"], "plain_value": plain["throughput"],
+            "speedup_vs_plain": fused["throughput"] / plain["throughput"],
+            "side_by_side_value": streams["throughput"],
+            "makespan_s": fused["wall_s"], "side_by_side_makespan_s": streams["wall_s"],
+            "plain_makespan_s": plain["wall_s"], "results_identical": bool(same), "autotune_side_by_side": tuned}
 
 
 def traffic_from_profiles_ops():

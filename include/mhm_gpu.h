@@ -290,6 +290,28 @@ int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_
  * others continue. */
 int mhm_member_status(mhm_ctx *ctx, int32_t *status);
 
+/* Batches of contexts (no counterpart in the reference, whose farm of
+ * parameter sets and domains runs them one after another or on separate MPI
+ * ranks, src/common/mo_common_MPI_tools.F90:39-69): one call enqueues a
+ * chunk of per-member steps on each of n contexts -- each exactly as
+ * mhm_run_members_async(ctxs[i], member_tt0[i], n_steps, q_gauge[i]) -- with
+ * the cell chain of all of them in ONE persistent launch on the batch's
+ * stream: the resident blocks take 128-item tiles of all contexts from a
+ * device work queue (tiles of contexts with more soil horizons first), so
+ * basins of very different sizes fill the GPU together; accumulation and
+ * routing then run on each context's own streams.  Every context must live
+ * on the batch's device, use device forcing, take the call in one chunk and
+ * have no per-step or aggregated outputs enabled; all must share the process
+ * cases' code path (PET input with the Feddes stress, or not).  Results are
+ * bit-identical to the contexts' own launches.  Poll or synchronise each
+ * context as after mhm_run_members_async; q_gauge may be NULL or hold NULLs. */
+typedef struct mhm_batch mhm_batch;
+int mhm_batch_create(int32_t device, mhm_batch **out);
+int mhm_batch_destroy(mhm_batch *b);
+const char *mhm_batch_last_error(const mhm_batch *b);
+int mhm_batch_run_members(mhm_batch *b, int32_t n, mhm_ctx *const *ctxs, const int32_t *const *member_tt0,
+                          int32_t n_steps, double *const *q_gauge);
+
 int mhm_snapshot_alloc(mhm_ctx *ctx, int32_t n_slots);
 int mhm_snapshot_save(mhm_ctx *ctx, int32_t member, int32_t slot);
 int mhm_snapshot_load(mhm_ctx *ctx, int32_t slot, int32_t member);

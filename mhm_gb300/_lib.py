@@ -104,6 +104,7 @@ EXPORTS = [
     "mhm_read_routed_outputs", "mhm_set_output_weights", "mhm_set_link_celerity", "mhm_network_topology",
     "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
+    "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
 ]
 
 _LIB = None
@@ -186,5 +187,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_set_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
     L.mhm_get_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
     L.mhm_autotune_ex.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _ip, C.POINTER(LaunchConfig), _dp]
+    L.mhm_batch_create.argtypes = [C.c_int32, C.POINTER(vp)]
+    L.mhm_batch_destroy.argtypes = [vp]
+    L.mhm_batch_last_error.argtypes = [vp]
+    L.mhm_batch_last_error.restype = C.c_char_p
+    L.mhm_batch_run_members.argtypes = [vp, C.c_int32, C.POINTER(vp), C.POINTER(_ip), C.c_int32, C.POINTER(_dp)]
     _LIB = L
     return L

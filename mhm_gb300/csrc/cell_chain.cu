@@ -33,6 +33,30 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
     return cudaGetLastError();
 }
 
+// The persistent multi-context launch: hl = horizon planes of the shared
+// layout (6 or 8, at least every context's horizon count), `lean` as the
+// contexts' common code path.  One resident wave of blocks takes the tiles.
+cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, cudaStream_t s)
+{
+    if (f.n_tiles <= 0) return cudaSuccess;
+    const int block = 128;
+    const size_t smem = (size_t)HS_PLANES * hl * block * sizeof(double);
+    void (*k)(const FusedCellArgs) = nullptr;
+    if (hl == 6) k = lean ? cell_chain_fused_kernel<6, true> : cell_chain_fused_kernel<6, false>;
+    else if (hl == 8) k = lean ? cell_chain_fused_kernel<8, true> : cell_chain_fused_kernel<8, false>;
+    else return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, nb = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem)) != cudaSuccess) return e;
+    const int64_t wave = (int64_t)(nb < 1 ? 1 : nb) * sms;
+    const unsigned grid = (unsigned)(f.n_tiles < wave ? f.n_tiles : wave);
+    k<<<grid, block, smem, s>>>(f);
+    return cudaGetLastError();
+}
+
 // occ = resident blocks per SM the kernel's registers are sized for (4, 6, 8)
 cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s)
 {

@@ -117,10 +117,16 @@ enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, H
 // cases 1, 4) only -- the configurations of the throughput workloads -- so that
 // the Hargreaves / Priestley-Taylor / Penman-Monteith and Jarvis code is not in
 // the instruction stream and the register allocation.
-template <int H, int MINB, bool FLUX, bool LEAN>
-__global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
+//
+// cell_chain_item advances work item `gid` (member gid / n_cells, cell
+// gid % n_cells) of the launch described by `a`.  HL sizes the shared-memory
+// horizon planes; DYN takes the horizon count from a.n_horizons (<= HL) at
+// run time, so that one launch can serve contexts with different horizon
+// counts (the fused multi-context launch); otherwise it is HL.
+template <int HL, bool FLUX, bool LEAN, bool DYN>
+__device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t gid)
 {
-    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int H = DYN ? a.n_horizons : HL;
     const int64_t N = a.n_cells;
     if (gid >= N * a.n_members) return;
     const int m = (int)(gid / N);
@@ -144,7 +150,7 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
 
     extern __shared__ double hsm[];
     const int tb = threadIdx.x, B = blockDim.x;
-    auto hs = [&](int plane, int h) -> double & { return hsm[(plane * H + h) * B + tb]; };
+    auto hs = [&](int plane, int h) -> double & { return hsm[(plane * HL + h) * B + tb]; };
     const bool feddes = LEAN || (a.proc_sm == 1 || a.proc_sm == 4);
     CellRegs c;
     const double c2 = a.c2TSTu;
@@ -518,6 +524,38 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
         chk(smh);
     }
     if (a.nonfinite && (nonfin >> 63)) atomicOr(a.nonfinite + m, 1);
+}
+
+template <int H, int MINB, bool FLUX, bool LEAN>
+__global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
+{
+    cell_chain_item<H, FLUX, LEAN, false>(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The cell chain of several contexts in one persistent launch: a work queue
+// of tiles (128 consecutive work items of one context), taken in queue order
+// by the resident blocks with one atomic increment per tile.  Each block
+// copies the tile's context description into shared memory and runs the same
+// per-item code as cell_chain_kernel, so every item's arithmetic -- and
+// result -- is that of the context's own launch.  No block waits on another:
+// a block returns when the queue is empty.
+template <int HL, bool LEAN>
+__global__ void __launch_bounds__(128, 4) cell_chain_fused_kernel(const FusedCellArgs f)
+{
+    __shared__ CellArgs sa;
+    __shared__ int32_t tile;
+    for (;;) {
+        if (threadIdx.x == 0) tile = atomicAdd(f.queue, 1);
+        __syncthreads();
+        const int32_t t = tile;
+        if (t >= f.n_tiles) return;
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(f.args + __ldg(f.tile_ctx + t));
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
+        for (int w = threadIdx.x; w < (int)(sizeof(CellArgs) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
+        __syncthreads();
+        cell_chain_item<HL, false, LEAN, true>(sa, __ldg(f.tile_item0 + t) + threadIdx.x);
+        __syncthreads(); // the next tile may overwrite sa and the horizon planes
+    }
 }
 
 // Launch with H as a template parameter (shared-memory size, loop bounds);

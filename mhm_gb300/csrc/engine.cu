@@ -37,6 +37,7 @@ cudaError_t launch_hmath_eval(int op, int64_t n, const double *x, const double *
 cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *sink, cudaStream_t s);
 cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s);
 cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s);
+cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, cudaStream_t s);
 } // namespace mhm
 
 using namespace mhm;
@@ -213,6 +214,24 @@ struct mhm_ctx {
     DevBuf<int32_t> mpr_nhor, mpr_ntill, mpr_nsub;
     DevBuf<uint32_t> mpr_code;
     DevBuf<double> mpr_soil, mpr_se, mpr_asp, mpr_lai, mpr_frac, mpr_lut, mpr_gamma, mpr_table, mpr_petlai;
+    std::string err;
+};
+
+// A batch of contexts whose cell chains run in one persistent launch.
+struct mhm_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_done = nullptr, ev_staged = nullptr;
+    bool staged = false;
+    std::vector<cudaEvent_t> ev_pre;
+    DevBuf<CellArgs> args;
+    DevBuf<int32_t> tile_ctx, queue;
+    DevBuf<int64_t> tile_item0;
+    CellArgs *h_args = nullptr;
+    int32_t *h_tile_ctx = nullptr;
+    int64_t *h_item0 = nullptr;
+    size_t cap_ctx = 0, cap_tiles = 0;
+    int64_t rounds = 0, tiles_total = 0;
     std::string err;
 };
 
@@ -1025,8 +1044,18 @@ static int finish_gauge_stage(mhm_ctx *ctx, mhm_ctx::GaugeStage &st)
     return MHM_OK;
 }
 
+// A context's part in a fused multi-context launch of the cell chain
+// (mhm_batch_run_members): phase 1 runs run_enqueue up to the cell chain of
+// the call's single chunk and returns its launch description; phase 2 runs
+// the whole call with the cell chain replaced by a wait for the fused launch.
+struct FusedStage {
+    int phase = 0;
+    CellArgs args{};
+    cudaEvent_t ev_fused = nullptr;
+};
+
 static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge,
-                       const int32_t *member_tt0 = nullptr)
+                       const int32_t *member_tt0 = nullptr, FusedStage *fs = nullptr)
 {
     if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
@@ -1160,6 +1189,9 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
     }
     if (ctx->out_qmod) ctx->host_qmod.assign(M * (size_t)n_steps * L, 0.0);
     const int nchunks = (n_steps + Tc - 1) / Tc;
+    if (fs && (nchunks != 1 || !members))
+        return fail(ctx, MHM_ERR_UNSUPPORTED, "a fused launch takes one chunk of per-member steps per context ("
+                                              "n_steps " + std::to_string(n_steps) + " > chunk " + std::to_string(Tc) + ")");
     auto chunk_rows = [&](int c, int32_t &r0, int32_t &r1) { // forcing rows iMeteoTS of the chunk
         const int64_t t0 = (int64_t)tt0 + c * Tc, t1 = (int64_t)tt0 + std::min(n_steps, (c + 1) * Tc) - 1;
         r0 = (int32_t)((t0 + stride - 1) / stride);
@@ -1201,17 +1233,19 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             g_launches++;
             ctx->steps_all_filled = cap;
         }
-        const int r = (int)(ctx->member_calls & 3);
-        if (!ctx->ev_members_done[r]) {
-            CK(cudaEventCreateWithFlags(&ctx->ev_members_done[r], cudaEventDisableTiming), "event");
-        } else {
-            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_members_done[r], 0), "wait member table");
+        if (!(fs && fs->phase == 2)) { // phase 2 reuses the table phase 1 uploaded
+            const int r = (int)(ctx->member_calls & 3);
+            if (!ctx->ev_members_done[r]) {
+                CK(cudaEventCreateWithFlags(&ctx->ev_members_done[r], cudaEventDisableTiming), "event");
+            } else {
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_members_done[r], 0), "wait member table");
+            }
+            CK(ctx->member_s0[r].ensure(M), "member steps");
+            CK(cudaMemcpyAsync(ctx->member_s0[r].p, ctx->member_s0_h.data(), M * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, ctx->stream),
+               "member steps");
+            ctx->member_s0_cur = ctx->member_s0[r].p;
         }
-        CK(ctx->member_s0[r].ensure(M), "member steps");
-        CK(cudaMemcpyAsync(ctx->member_s0[r].p, ctx->member_s0_h.data(), M * sizeof(int32_t), cudaMemcpyHostToDevice,
-                           ctx->stream),
-           "member steps");
-        ctx->member_s0_cur = ctx->member_s0[r].p;
     }
     if (ctx->timing && !ctx->run_a) {
         cudaEventCreate(&ctx->run_a);
@@ -1283,6 +1317,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.latitude = ctx->latitude.p;
         a.tab = ctx->tab;
         a.nonfinite = ctx->nonfinite.p;
+        a.n_horizons = H;
         if (ctx->out_flux) {
             a.flux_aet = ctx->flux_d[0].p;
             a.flux_loss = ctx->flux_d[1].p;
@@ -1306,7 +1341,13 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             o.w_sms = ctx->w_sms.p;
             out_advance(ctx->fso, ctx->jul_start, ctx->timestep, (int64_t)tt0 + s0, nT, true);
         }
-        {
+        if (fs && fs->phase == 1) {
+            fs->args = a; // everything up to the cell chain is enqueued; the rest follows in phase 2
+            return MHM_OK;
+        }
+        if (fs) {
+            CK(cudaStreamWaitEvent(ctx->stream, fs->ev_fused, 0), "wait fused cell chain");
+        } else {
             Bracket br(ctx, 0, ctx->stream);
             CK(launch_cell_chain(a, H, ctx->cell_occ, ctx->stream), "cell chain launch");
             br.done();
@@ -2472,6 +2513,163 @@ int mhm_hmath_eval(int32_t op, int32_t where, int64_t n, const double *x, const 
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
     cleanup();
     return e == cudaSuccess ? MHM_OK : MHM_ERR_CUDA;
+}
+
+int mhm_batch_create(int32_t device, mhm_batch **out)
+{
+    if (!out) return MHM_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MHM_ERR_CUDA;
+    int cur = 0;
+    if (device < 0 && cudaGetDevice(&cur) != cudaSuccess) cur = 0;
+    if (device >= ndev) return MHM_ERR_INVALID;
+    mhm_batch *b = new mhm_batch();
+    b->device = device >= 0 ? device : cur;
+    DeviceGuard dg(b->device);
+    if (dg.err != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_staged, cudaEventDisableTiming) != cudaSuccess ||
+        b->queue.ensure(1) != cudaSuccess) {
+        mhm_batch_destroy(b);
+        return MHM_ERR_CUDA;
+    }
+    *out = b;
+    return MHM_OK;
+}
+
+int mhm_batch_destroy(mhm_batch *b)
+{
+    if (!b) return MHM_OK;
+    DeviceGuard dg(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (cudaEvent_t e : b->ev_pre)
+        if (e) cudaEventDestroy(e);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
+    if (b->ev_staged) cudaEventDestroy(b->ev_staged);
+    if (b->h_args) cudaFreeHost(b->h_args);
+    if (b->h_tile_ctx) cudaFreeHost(b->h_tile_ctx);
+    if (b->h_item0) cudaFreeHost(b->h_item0);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return MHM_OK;
+}
+
+const char *mhm_batch_last_error(const mhm_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int mhm_batch_run_members(mhm_batch *b, int32_t n, mhm_ctx *const *ctxs, const int32_t *const *member_tt0,
+                          int32_t n_steps, double *const *q_gauge)
+{
+    if (!b || n < 1 || !ctxs || !member_tt0 || n_steps < 1) return MHM_ERR_INVALID;
+    auto bfail = [&](int code, const std::string &m) {
+        b->err = m;
+        return code;
+    };
+    DeviceGuard dg(b->device);
+    if (dg.err != cudaSuccess) return bfail(MHM_ERR_CUDA, "set device");
+    bool lean = false;
+    int hmax = 1;
+    for (int32_t i = 0; i < n; ++i) {
+        mhm_ctx *c = ctxs[i];
+        if (!c || !member_tt0[i]) return bfail(MHM_ERR_INVALID, "context or member steps missing");
+        for (int32_t j = 0; j < i; ++j)
+            if (ctxs[j] == c) return bfail(MHM_ERR_INVALID, "a context appears twice");
+        if (c->device != b->device) return bfail(MHM_ERR_INVALID, "context on another device than the batch");
+        if (c->out_tro || c->out_qmod || c->out_flux || c->fso.on || c->qro.on)
+            return bfail(MHM_ERR_UNSUPPORTED, "per-step or aggregated outputs in a fused launch");
+        const bool l = (c->proc_pet == 0 || c->proc_pet == -1) && (c->proc_sm == 1 || c->proc_sm == 4);
+        if (i > 0 && l != lean) return bfail(MHM_ERR_UNSUPPORTED, "contexts with different process code paths");
+        lean = l;
+        hmax = std::max(hmax, c->H);
+    }
+    const int hl = hmax <= 6 ? 6 : 8;
+    if ((int)b->ev_pre.size() < n) {
+        const size_t old = b->ev_pre.size();
+        b->ev_pre.resize(n, nullptr);
+        for (size_t i = old; i < (size_t)n; ++i)
+            if (cudaEventCreateWithFlags(&b->ev_pre[i], cudaEventDisableTiming) != cudaSuccess)
+                return bfail(MHM_ERR_CUDA, "event");
+    }
+    // phase 1: every context enqueues its call up to the cell chain
+    std::vector<FusedStage> fs(n);
+    for (int32_t i = 0; i < n; ++i) {
+        mhm_ctx *c = ctxs[i];
+        fs[i].phase = 1;
+        if (int rc = run_enqueue(c, 1, n_steps, q_gauge ? q_gauge[i] : nullptr, member_tt0[i], &fs[i]))
+            return bfail(rc, "context " + std::to_string(i) + ": " + c->err);
+        if (cudaEventRecord(b->ev_pre[i], c->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(b->stream, b->ev_pre[i], 0) != cudaSuccess)
+            return bfail(MHM_ERR_CUDA, "event");
+    }
+    // the work queue: tiles of 128 items, contexts with more horizons first
+    std::vector<int32_t> order(n);
+    for (int32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return ctxs[x]->H > ctxs[y]->H ||
+               (ctxs[x]->H == ctxs[y]->H && (int64_t)ctxs[x]->N * ctxs[x]->M > (int64_t)ctxs[y]->N * ctxs[y]->M);
+    });
+    size_t n_tiles = 0;
+    for (int32_t i = 0; i < n; ++i) n_tiles += ((size_t)ctxs[i]->N * ctxs[i]->M + 127) / 128;
+    if (n_tiles > (size_t)INT32_MAX) return bfail(MHM_ERR_UNSUPPORTED, "too many tiles");
+    if (b->staged && cudaEventSynchronize(b->ev_staged) != cudaSuccess) return bfail(MHM_ERR_CUDA, "staging");
+    if (b->cap_ctx < (size_t)n) {
+        if (b->h_args) cudaFreeHost(b->h_args);
+        b->h_args = nullptr;
+        b->cap_ctx = 0;
+        if (cudaMallocHost((void **)&b->h_args, (size_t)n * sizeof(CellArgs)) != cudaSuccess)
+            return bfail(MHM_ERR_OOM, "staging");
+        b->cap_ctx = n;
+    }
+    if (b->cap_tiles < n_tiles) {
+        if (b->h_tile_ctx) cudaFreeHost(b->h_tile_ctx);
+        if (b->h_item0) cudaFreeHost(b->h_item0);
+        b->h_tile_ctx = nullptr;
+        b->h_item0 = nullptr;
+        b->cap_tiles = 0;
+        if (cudaMallocHost((void **)&b->h_tile_ctx, n_tiles * sizeof(int32_t)) != cudaSuccess ||
+            cudaMallocHost((void **)&b->h_item0, n_tiles * sizeof(int64_t)) != cudaSuccess)
+            return bfail(MHM_ERR_OOM, "staging");
+        b->cap_tiles = n_tiles;
+    }
+    size_t t = 0;
+    for (int32_t oi = 0; oi < n; ++oi) {
+        const int32_t i = order[oi];
+        b->h_args[i] = fs[i].args;
+        const int64_t items = (int64_t)ctxs[i]->N * ctxs[i]->M;
+        for (int64_t it = 0; it < items; it += 128, ++t) {
+            b->h_tile_ctx[t] = i;
+            b->h_item0[t] = it;
+        }
+    }
+    if (b->args.ensure(n) != cudaSuccess || b->tile_ctx.ensure(n_tiles) != cudaSuccess ||
+        b->tile_item0.ensure(n_tiles) != cudaSuccess)
+        return bfail(MHM_ERR_OOM, "batch tables");
+    if (cudaMemcpyAsync(b->args.p, b->h_args, (size_t)n * sizeof(CellArgs), cudaMemcpyHostToDevice, b->stream) ||
+        cudaMemcpyAsync(b->tile_ctx.p, b->h_tile_ctx, n_tiles * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream) ||
+        cudaMemcpyAsync(b->tile_item0.p, b->h_item0, n_tiles * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream) ||
+        cudaMemsetAsync(b->queue.p, 0, sizeof(int32_t), b->stream) || cudaEventRecord(b->ev_staged, b->stream))
+        return bfail(MHM_ERR_CUDA, "batch tables upload");
+    b->staged = true;
+    FusedCellArgs f{};
+    f.args = b->args.p;
+    f.tile_ctx = b->tile_ctx.p;
+    f.tile_item0 = b->tile_item0.p;
+    f.n_tiles = (int32_t)n_tiles;
+    f.queue = b->queue.p;
+    if (cudaError_t e = launch_cell_chain_fused(f, hl, lean, b->stream))
+        return bfail(MHM_ERR_CUDA, std::string("fused cell chain: ") + cudaGetErrorString(e));
+    g_launches++;
+    if (cudaEventRecord(b->ev_done, b->stream) != cudaSuccess) return bfail(MHM_ERR_CUDA, "event");
+    b->rounds += 1;
+    b->tiles_total += (int64_t)n_tiles;
+    // phase 2: the rest of every context's call, after the fused cell chain
+    for (int32_t i = 0; i < n; ++i) {
+        fs[i].phase = 2;
+        fs[i].ev_fused = b->ev_done;
+        if (int rc = run_enqueue(ctxs[i], 1, n_steps, q_gauge ? q_gauge[i] : nullptr, member_tt0[i], &fs[i]))
+            return bfail(rc, "context " + std::to_string(i) + ": " + ctxs[i]->err);
+    }
+    return MHM_OK;
 }
 
 int mhm_probe_fp64(int64_t iters, double *flops)

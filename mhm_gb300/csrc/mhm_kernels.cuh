@@ -130,6 +130,18 @@ struct CellArgs {
     // per-member failure flag: bit 0 set when the member's total runoff of a
     // step or a state at the chunk's end is not finite (nullptr = not checked)
     int32_t *nonfinite;
+    int32_t n_horizons; // the context's horizon count (read by the fused multi-context launch)
+};
+
+// One persistent launch of the cell chain over several contexts (with the
+// same process cases' code path): tile t covers work items
+// tile_item0[t] .. + 127 of context tile_ctx[t].
+struct FusedCellArgs {
+    const CellArgs *args;       // [n_contexts]
+    const int32_t *tile_ctx;    // [n_tiles]
+    const int64_t *tile_item0;  // [n_tiles]
+    int32_t n_tiles;
+    int32_t *queue;             // next tile to take (0 before the launch)
 };
 
 struct AccArgs {

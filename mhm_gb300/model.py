@@ -497,3 +497,45 @@ class MhmGpu:
     @property
     def stream(self) -> int:
         return int(self.L.mhm_ctx_stream(self.ctx) or 0)
+
+
+class MhmBatch:
+    """Contexts whose cell chains run in one persistent launch per call
+    (mhm_batch_run_members): each call enqueues one chunk of per-member
+    steps on every context given, as MhmGpu.run_members_async would."""
+
+    def __init__(self, device: int = -1):
+        self.L = _lib.load()
+        b = C.c_void_p()
+        rc = self.L.mhm_batch_create(device, C.byref(b))
+        if rc != 0:
+            raise MhmError(f"mhm_batch_create failed ({rc})")
+        self.b = b
+
+    def run_members(self, ctxs: list, member_tt0s: list, n_steps: int, q_outs: list | None = None):
+        n = len(ctxs)
+        vp = C.c_void_p
+        cs = (vp * n)(*[g.ctx.value for g in ctxs])
+        t0s = [np.ascontiguousarray(t, np.int32) for t in member_tt0s]
+        tp = (C.POINTER(C.c_int32) * n)(*[_i(t) for t in t0s])
+        qp = None
+        if q_outs is not None:
+            qp = (C.POINTER(C.c_double) * n)(*[_d(q) if q is not None else None for q in q_outs])
+        for g, t in zip(ctxs, t0s):
+            g._t0_keep = t
+            g._last_steps = n_steps
+        rc = self.L.mhm_batch_run_members(self.b, n, cs, tp, n_steps, qp)
+        if rc != 0:
+            raise MhmError(f"mhm_batch_run_members failed ({rc}): "
+                           f"{self.L.mhm_batch_last_error(self.b).decode(errors='replace')}")
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.mhm_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

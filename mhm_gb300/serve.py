@@ -118,11 +118,17 @@ class Server:
 
     def __init__(self, basins: list[Basin], hbm_budget: float = 150e9, chunk: int = 240, max_slots: int = 16,
                  proc_sm: int = 1, proc_pet: int = 0, spinup_steps: int = 90 * 24, gamma_spinup=None,
-                 autotune: bool = False, backend=MhmGpu, window_fn=None, workers: int = 4):
+                 autotune: bool = False, backend=MhmGpu, window_fn=None, workers: int = 4, fused: bool = False):
         """`backend` builds a basin's context (MhmGpu); `window_fn(basin)`
         gives its forcing window (default: the synthetic forecast window in
-        device memory)."""
+        device memory).  `fused`: the chunks enqueued in one pass of the loop
+        run their cell chains in one persistent launch (MhmBatch) -- every
+        context whose chunk fits one launch chunk; the others run alone."""
         self.backend = backend
+        self.batch = None
+        if fused and backend is MhmGpu:
+            from .model import MhmBatch
+            self.batch = MhmBatch()
         self.basins = basins
         self.budget = hbm_budget
         self.chunk = chunk
@@ -186,7 +192,7 @@ class Server:
                 g.snapshot_load(0, m)
             t = g.autotune(1, self.chunk)
             self.tuned[b.name] = {k: t[k] for k in ("cell_blocks_per_sm", "route_sub_steps")}
-        self.ctx[bi] = {"g": g, "slots": [None] * members, "tt0": np.zeros(members, np.int32), "bytes": need,
+        self.ctx[bi] = {"g": g, "bi": bi, "slots": [None] * members, "tt0": np.zeros(members, np.int32), "bytes": need,
                         "q": np.zeros((members, len(b.dom.gauge_node), self.chunk)), "busy": False}
         self.used += need
         return True
@@ -315,13 +321,21 @@ class Server:
             if not c["busy"]:
                 self._sweep(c)
         self._admit(now)
-        for bi, c in self.ctx.items():
-            if c["busy"] or not any(s is not None for s in c["slots"]):
-                continue
+        ready = [c for c in self.ctx.values() if not c["busy"] and any(s is not None for s in c["slots"])]
+        together = []
+        for c in ready:
             tt0 = np.where([s is not None for s in c["slots"]], c["tt0"], 0).astype(np.int32)
             c["tt0_now"] = tt0
-            c["g"].run_members_async(tt0, self.chunk, c["q"])
+            # one launch chunk covers the call when its two runoff slots fit the library's budget
+            fits = 2 * len(c["slots"]) * self.basins[c["bi"]].n_cells * 8 * self.chunk <= 8 * 2 ** 30
+            if self.batch is not None and fits:
+                together.append(c)
+            else:
+                c["g"].run_members_async(tt0, self.chunk, c["q"])
             c["busy"] = True
+        if together:
+            self.batch.run_members([c["g"] for c in together], [c["tt0_now"] for c in together], self.chunk,
+                                   [c["q"] for c in together])
         busy = [(bi, c) for bi, c in self.ctx.items() if c["busy"]]
         if not busy:
             return False
@@ -389,6 +403,9 @@ class Server:
         for bi in list(self.ctx):
             self._close(bi)
         self.pool.shutdown(wait=True)
+        if self.batch is not None:
+            self.batch.close()
+            self.batch = None
 
 
 def device_window(dom, chunk: int) -> tuple:
@@ -449,6 +466,52 @@ def serve_plain(basins: list[Basin], requests: list[Request], chunk: int, proc_s
             cell_steps += b.n_cells * chunk * math.ceil(r.horizon / chunk)
         wall = time.perf_counter() - t0
     finally:
+        for g in ctxs.values():
+            g.close()
+    return summarize(requests, wall, cell_steps)
+
+
+def run_batched(basins: list[Basin], requests: list[Request], chunk: int, proc_sm: int = 1,
+                proc_pet: int = 0) -> dict:
+    """Many whole runs at once (the uneven-basins workload): one context per
+    request, all advanced in rounds of one chunk; each round is ONE
+    persistent cell-chain launch over every run still active (MhmBatch, a
+    device work queue of tiles), then each run's accumulation and routing on
+    its own streams.  Rounds are enqueued without waiting: the library keeps
+    two chunks per context in flight (the cell chain of round k overlaps the
+    routing of round k-1).  Context set-up (MPR, warm start) is inside the
+    timed region, as in serve_plain.  Results equal run_alone's."""
+    from .model import MhmBatch
+    t0 = time.perf_counter()
+    ctxs: dict[int, MhmGpu] = {}
+    batch = MhmBatch()
+    cell_steps = 0
+    try:
+        for r in requests:
+            b = basins[r.basin]
+            g = MhmGpu(b.dom, proc_soilmoist=proc_sm, proc_pet=proc_pet, n_members=1, read_states=True)
+            g.mpr_setup(b.l0)
+            g.mpr(r.gamma)
+            g.set_state(b.restart, 0)
+            g.set_meteo(1, *b.window, on_device=True)
+            ctxs[r.rid] = g
+            r.q = []
+        rounds = max(math.ceil(r.horizon / chunk) for r in requests)
+        for k in range(rounds):
+            active = [r for r in requests if k * chunk < r.horizon]
+            qs = [np.zeros((1, len(basins[r.basin].dom.gauge_node), chunk)) for r in active]
+            batch.run_members([ctxs[r.rid] for r in active], [np.array([1 + k * chunk], np.int32)] * len(active),
+                              chunk, qs)
+            for r, q in zip(active, qs):
+                r.q.append(q[0])
+                cell_steps += basins[r.basin].n_cells * chunk
+        for r in requests:
+            ctxs[r.rid].sync()
+            r.done = time.perf_counter() - t0
+            r.status = "done"
+        wall = time.perf_counter() - t0
+    finally:
+        batch.close()
         for g in ctxs.values():
             g.close()
     return summarize(requests, wall, cell_steps)
