@@ -416,6 +416,45 @@ int mhm_network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int3
                          const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n,
                          int32_t *n_links);
 
+/* mRM's network start-up from level-0 flow data (host code, once per basin;
+ * src/mRM/mo_mrm_net_startup.f90): the L11 grid over the L0 mask
+ * (init_lowres_level, src/common/mo_grid.f90:58-183), L11_flow_direction
+ * (:227-629, L11 coarser than L0), L11_set_network_topology (:630-727),
+ * L11_routing_order (:728-886), L11_link_location (:887-1087),
+ * L11_stream_features (:1233-1509: link length and slope >= 1e-4 along the
+ * L0 river, the floodplain within deltaH = 5 m) and
+ * L11_fraction_sealed_floodplain (:1510-1594), for cartesian grids
+ * (iFlag_cordinate_sys = 0).  L0 grids use mHM's (x, y) order: nrows0 cells
+ * west to east, ncols0 north to south, mask0[(j-1)*nrows0 + (i-1)], data
+ * packed over the mask in that order; flow directions are mRM's codes
+ * (1 E, 2 SE, 4 S, 8 SW, 16 W, 32 NW, 64 N, 128 NE as moveDownOneCell moves
+ * on that grid).  lcover0 is [n_lc_scenes][n_cells0]; lc_class_imp the
+ * sealed class (2). */
+typedef struct mhm_l0_flow {
+    int32_t nrows0, ncols0, factor, n_cells0;
+    const uint8_t *mask0;
+    const int32_t *fdir0, *facc0;
+    const double *elev0;
+    double cellsize0;
+    int32_t n_lc_scenes, lc_class_imp;
+    const int32_t *lcover0;
+} mhm_l0_flow;
+/* Outputs, allocated by the caller: n_nodes from mhm_l11_network_size; every
+ * array [n_nodes] except frac_fp_imp [n_lc_scenes][n_nodes]; link arrays
+ * (length, slope, a_floodplain, frac_fp_imp) valid for links 1..n_links,
+ * from_n/to_n/net_perm/r_order as L11_fromN/L11_toN/L11_netPerm/L11_rOrder
+ * (1-based; -9999 past the links), fdir11 packed over the L11 mask,
+ * cell_row11/cell_col11 the L11 cells' grid coordinates, row_out/col_out
+ * each L11 cell's outlet cell on the L0 grid (L11_rowOut / L11_colOut).
+ * Any pointer may be NULL. */
+typedef struct mhm_l11_network_out {
+    int32_t n_nodes, n_outlets, n_links, nrows11, ncols11, n_l0_outlets;
+    int32_t *fdir11, *cell_row11, *cell_col11, *from_n, *to_n, *net_perm, *r_order, *row_out, *col_out;
+    double *length, *slope, *a_floodplain, *frac_fp_imp;
+} mhm_l11_network_out;
+int mhm_l11_network_size(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, int32_t factor, int32_t *n_nodes);
+int mhm_l11_network(const mhm_l0_flow *in, mhm_l11_network_out *out);
+
 /* Routing order of an L11 network (host computation, no device needed):
  * replaces L11_routing_order (src/mRM/mo_mrm_net_startup.f90:728-886) with an
  * O(nLinks x sweeps) algorithm giving the same ranks.  Inputs fromN/toN

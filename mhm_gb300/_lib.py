@@ -82,6 +82,23 @@ class LaunchConfig(C.Structure):
                 ("pad_", C.c_int32)]
 
 
+class L0Flow(C.Structure):
+    """mhm_l0_flow: level-0 flow data of a basin."""
+    _fields_ = [("nrows0", C.c_int32), ("ncols0", C.c_int32), ("factor", C.c_int32), ("n_cells0", C.c_int32),
+                ("mask0", C.POINTER(C.c_uint8)), ("fdir0", _ip), ("facc0", _ip), ("elev0", _dp),
+                ("cellsize0", C.c_double), ("n_lc_scenes", C.c_int32), ("lc_class_imp", C.c_int32),
+                ("lcover0", _ip)]
+
+
+class L11Network(C.Structure):
+    """mhm_l11_network: the network mRM's start-up derives."""
+    _fields_ = [("n_nodes", C.c_int32), ("n_outlets", C.c_int32), ("n_links", C.c_int32), ("nrows11", C.c_int32),
+                ("ncols11", C.c_int32), ("n_l0_outlets", C.c_int32)] + \
+               [(n, _ip) for n in ("fdir11", "cell_row11", "cell_col11", "from_n", "to_n", "net_perm", "r_order",
+                                   "row_out", "col_out")] + \
+               [(n, _dp) for n in ("length", "slope", "a_floodplain", "frac_fp_imp")]
+
+
 class OutputConfig(C.Structure):
     """mhm_output_config: aggregated flux/state (or Qrouted) outputs."""
     _fields_ = [
@@ -105,6 +122,7 @@ EXPORTS = [
     "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
+    "mhm_l11_network_size", "mhm_l11_network",
 ]
 
 _LIB = None
@@ -192,5 +210,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_batch_last_error.argtypes = [vp]
     L.mhm_batch_last_error.restype = C.c_char_p
     L.mhm_batch_run_members.argtypes = [vp, C.c_int32, C.POINTER(vp), C.POINTER(_ip), C.c_int32, C.POINTER(_dp)]
+    L.mhm_l11_network_size.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int32, _ip]
+    L.mhm_l11_network.argtypes = [C.POINTER(L0Flow), C.POINTER(L11Network)]
     _LIB = L
     return L

@@ -22,7 +22,8 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = BUILD / "libmhm_gpu.so"
 
-SOURCES = ["cell_chain.cu", "cell_chain_o6.cu", "cell_chain_o8.cu", "routing.cu", "probes.cu", "mpr.cu", "engine.cu", "network.cpp", "mpr_host.cpp"]
+SOURCES = ["cell_chain.cu", "cell_chain_o6.cu", "cell_chain_o8.cu", "routing.cu", "probes.cu", "mpr.cu", "engine.cu",
+           "network.cpp", "netbuild.cpp", "mpr_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

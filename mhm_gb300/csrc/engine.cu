@@ -2158,6 +2158,72 @@ int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n,
     return MHM_OK;
 }
 
+int mhm_l11_network_size(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, int32_t factor, int32_t *n_nodes)
+{
+    if (nrows0 < 1 || ncols0 < 1 || factor < 1 || !mask0 || !n_nodes) return MHM_ERR_INVALID;
+    const int32_t nr11 = (nrows0 + factor - 1) / factor, nc11 = (ncols0 + factor - 1) / factor;
+    std::vector<char> m((size_t)nr11 * nc11, 0);
+    for (int32_t j = 0; j < ncols0; ++j)
+        for (int32_t i = 0; i < nrows0; ++i)
+            if (mask0[(size_t)j * nrows0 + i]) m[(size_t)(j / factor) * nr11 + i / factor] = 1;
+    int32_t n = 0;
+    for (char c : m) n += c ? 1 : 0;
+    *n_nodes = n;
+    return MHM_OK;
+}
+
+int mhm_l11_network(const mhm_l0_flow *in, mhm_l11_network_out *out)
+{
+    if (!in || !out || !in->mask0 || !in->fdir0 || !in->facc0 || !in->elev0 || in->n_cells0 < 1 ||
+        !(in->cellsize0 > 0.0) || in->n_lc_scenes < 0 || (in->n_lc_scenes > 0 && !in->lcover0))
+        return MHM_ERR_INVALID;
+    L0FlowInput li;
+    li.nrows0 = in->nrows0;
+    li.ncols0 = in->ncols0;
+    li.factor = in->factor;
+    li.n_cells0 = in->n_cells0;
+    li.mask0 = in->mask0;
+    li.fdir0 = in->fdir0;
+    li.facc0 = in->facc0;
+    li.elev0 = in->elev0;
+    li.cellsize0 = in->cellsize0;
+    li.n_lc_scenes = in->n_lc_scenes;
+    li.lc_class_imp = in->lc_class_imp;
+    li.lcover0 = in->lcover0;
+    L11NetworkOut o;
+    std::string err;
+    if (!build_l11_network(li, o, err)) {
+        std::fprintf(stderr, "mhm_l11_network: %s\n", err.c_str());
+        return MHM_ERR_INVALID;
+    }
+    out->n_nodes = o.n_nodes;
+    out->n_outlets = o.n_outlets;
+    out->n_links = o.n_links;
+    out->nrows11 = o.nrows11;
+    out->ncols11 = o.ncols11;
+    out->n_l0_outlets = o.n_l0_outlets;
+    auto put_i = [](int32_t *dst, const std::vector<int32_t> &v) {
+        if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(int32_t));
+    };
+    auto put_d = [](double *dst, const std::vector<double> &v) {
+        if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(double));
+    };
+    put_i(out->fdir11, o.fdir11);
+    put_i(out->cell_row11, o.cell_row11);
+    put_i(out->cell_col11, o.cell_col11);
+    put_i(out->from_n, o.from_n);
+    put_i(out->to_n, o.to_n);
+    put_i(out->net_perm, o.net_perm);
+    put_i(out->r_order, o.r_order);
+    put_i(out->row_out, o.row_out);
+    put_i(out->col_out, o.col_out);
+    put_d(out->length, o.length);
+    put_d(out->slope, o.slope);
+    put_d(out->a_floodplain, o.a_floodplain);
+    put_d(out->frac_fp_imp, o.frac_fp_imp);
+    return MHM_OK;
+}
+
 int mhm_network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
                          const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n,
                          int32_t *n_links)

@@ -45,4 +45,32 @@ bool network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t
                       const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n, int32_t *n_links,
                       std::string &err);
 
+// Level-0 flow data of one basin for mRM's network start-up.
+struct L0FlowInput {
+    int32_t nrows0 = 0, ncols0 = 0; // L0 grid (mHM's (x, y) order, column-major)
+    int32_t factor = 0;             // L11 cell size / L0 cell size
+    int32_t n_cells0 = 0;           // cells of the mask
+    const uint8_t *mask0 = nullptr; // [ncols0][nrows0]
+    const int32_t *fdir0 = nullptr, *facc0 = nullptr; // [n_cells0] packed over the mask
+    const double *elev0 = nullptr;  // [n_cells0]
+    double cellsize0 = 0.0;         // [m], cartesian coordinates
+    int32_t n_lc_scenes = 0, lc_class_imp = 2;
+    const int32_t *lcover0 = nullptr; // [n_lc_scenes][n_cells0]
+};
+
+// The L11 network mRM derives from it (arrays over the L11 cells; link
+// arrays valid for 1..n_links).
+struct L11NetworkOut {
+    int32_t n_nodes = 0, n_outlets = 0, n_links = 0, nrows11 = 0, ncols11 = 0, n_l0_outlets = 0;
+    std::vector<int32_t> fdir11, cell_row11, cell_col11, from_n, to_n, net_perm, r_order, row_out, col_out;
+    std::vector<double> length, slope, a_floodplain;
+    std::vector<double> frac_fp_imp; // [n_lc_scenes][n_nodes]
+};
+
+// L11_flow_direction, L11_set_network_topology, L11_routing_order,
+// L11_link_location, L11_stream_features and L11_fraction_sealed_floodplain
+// (src/mRM/mo_mrm_net_startup.f90:227-1594) for an L11 grid coarser than L0,
+// cartesian coordinates (iFlag_cordinate_sys = 0).
+bool build_l11_network(const L0FlowInput &in, L11NetworkOut &out, std::string &err);
+
 } // namespace mhm
