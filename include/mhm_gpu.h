@@ -454,6 +454,13 @@ typedef struct mhm_l11_network_out {
 } mhm_l11_network_out;
 int mhm_l11_network_size(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, int32_t factor, int32_t *n_nodes);
 int mhm_l11_network(const mhm_l0_flow *in, mhm_l11_network_out *out);
+/* L11_L1_mapping (src/mRM/mo_mrm_net_startup.f90:61-226): for the L1 and
+ * L11 grids at factors factor1 and factor11 of the L0 grid (integer
+ * multiples of each other; sizes from mhm_l11_network_size with each
+ * factor), L1_L11_Id [L1 cells] (the L11 cell containing each L1 cell) and
+ * L11_L1_Id [L11 cells] (when L11 is finer), -9999 otherwise. */
+int mhm_l1_l11_mapping(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, int32_t factor1, int32_t factor11,
+                       int32_t *l1_l11_id, int32_t *l11_l1_id);
 
 /* Routing order of an L11 network (host computation, no device needed):
  * replaces L11_routing_order (src/mRM/mo_mrm_net_startup.f90:728-886) with an

@@ -122,7 +122,7 @@ EXPORTS = [
     "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
-    "mhm_l11_network_size", "mhm_l11_network",
+    "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping",
 ]
 
 _LIB = None
@@ -212,5 +212,6 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_batch_run_members.argtypes = [vp, C.c_int32, C.POINTER(vp), C.POINTER(_ip), C.c_int32, C.POINTER(_dp)]
     L.mhm_l11_network_size.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int32, _ip]
     L.mhm_l11_network.argtypes = [C.POINTER(L0Flow), C.POINTER(L11Network)]
+    L.mhm_l1_l11_mapping.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.c_int32, C.c_int32, _ip, _ip]
     _LIB = L
     return L

@@ -2224,6 +2224,21 @@ int mhm_l11_network(const mhm_l0_flow *in, mhm_l11_network_out *out)
     return MHM_OK;
 }
 
+int mhm_l1_l11_mapping(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, int32_t factor1, int32_t factor11,
+                       int32_t *l1_l11_id, int32_t *l11_l1_id)
+{
+    if (!mask0) return MHM_ERR_INVALID;
+    std::vector<int32_t> a, b;
+    std::string err;
+    if (!l1_l11_mapping(nrows0, ncols0, mask0, factor1, factor11, a, b, err)) {
+        std::fprintf(stderr, "mhm_l1_l11_mapping: %s\n", err.c_str());
+        return MHM_ERR_INVALID;
+    }
+    if (l1_l11_id) std::memcpy(l1_l11_id, a.data(), a.size() * sizeof(int32_t));
+    if (l11_l1_id) std::memcpy(l11_l1_id, b.data(), b.size() * sizeof(int32_t));
+    return MHM_OK;
+}
+
 int mhm_network_topology(int32_t nrows, int32_t ncols, const int32_t *id2d, int32_t n_cells, const int32_t *cell_row,
                          const int32_t *cell_col, const int32_t *fdir, int32_t *from_n, int32_t *to_n,
                          int32_t *n_links)

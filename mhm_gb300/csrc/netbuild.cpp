@@ -311,11 +311,10 @@ bool build_l11_network(const L0FlowInput &in, L11NetworkOut &out, std::string &e
         slope[ii] = (slope[ii] - elev0(fr, fc)) / length[ii];
         if (slope[ii] < 0.0001) slope[ii] = 0.0001;
         // the floodplain area: the cells marked for this link (a later link
-        // may take some of them over, so sum now), in packed order
-        std::vector<int32_t> &m = mark;
-        std::sort(m.begin(), m.end());
+        // may take some of them over, so sum now); cartesian cells have
+        // equal areas, so the sum order does not matter
         double s = 0.0;
-        for (int32_t id : m) (void)id, s = s + in.cellsize0 * in.cellsize0;
+        for (size_t q = 0; q < mark.size(); ++q) s = s + in.cellsize0 * in.cellsize0;
         afp[ii] = s;
     }
     // L11_fraction_sealed_floodplain (:1510-1594): per land-cover scene, the
@@ -351,6 +350,69 @@ bool build_l11_network(const L0FlowInput &in, L11NetworkOut &out, std::string &e
     out.cell_row11 = rows11;
     out.cell_col11 = cols11;
     out.n_l0_outlets = (int32_t)oi.size();
+    return true;
+}
+
+// L11_L1_mapping (src/mRM/mo_mrm_net_startup.f90:61-226): the L1 and L11
+// grids over the L0 mask at factors f1 and f11; every L1 cell gets the id of
+// the L11 cell that contains it (L11 not finer than L1), or every L11 cell
+// that of its L1 cell (L11 finer), -9999 otherwise.
+bool l1_l11_mapping(int32_t nr0, int32_t nc0, const uint8_t *mask0, int32_t f1, int32_t f11,
+                    std::vector<int32_t> &l1_l11, std::vector<int32_t> &l11_l1, std::string &err)
+{
+    if (nr0 < 1 || nc0 < 1 || f1 < 1 || f11 < 1 || (f11 % f1 != 0 && f1 % f11 != 0)) {
+        err = "the L1 and L11 cell sizes must be integer multiples of each other";
+        return false;
+    }
+    auto lowres = [&](int32_t f, Grid2<int32_t> &id, int32_t &n) {
+        const int32_t nr = (nr0 + f - 1) / f, nc = (nc0 + f - 1) / f;
+        Grid2<int32_t> m;
+        m.init(nr, nc, 0);
+        for (int32_t j = 1; j <= nc0; ++j)
+            for (int32_t i = 1; i <= nr0; ++i)
+                if (mask0[(size_t)(j - 1) * nr0 + (i - 1)]) m((i + f - 1) / f, (j + f - 1) / f) = 1;
+        id.init(nr, nc, kNodata);
+        n = 0;
+        for (int32_t j = 1; j <= nc; ++j)
+            for (int32_t i = 1; i <= nr; ++i)
+                if (m(i, j)) id(i, j) = ++n;
+    };
+    Grid2<int32_t> id1, id11;
+    int32_t n1 = 0, n11 = 0;
+    lowres(f1, id1, n1);
+    lowres(f11, id11, n11);
+    Grid2<int32_t> on1, on11; // L11 id on the L1 grid, L1 id on the L11 grid
+    on1.init(id1.nr, id1.nc, kNodata);
+    on11.init(id11.nr, id11.nc, kNodata);
+    if (f11 < f1) { // cellFactorRbyH < 1
+        const int32_t inv = f1 / f11;
+        for (int32_t jcc = 1; jcc <= id1.nc; ++jcc)
+            for (int32_t icc = 1; icc <= id1.nr; ++icc) {
+                if (id1(icc, jcc) < 1) continue;
+                const int32_t u = (icc - 1) * inv + 1, d = std::min(icc * inv, id11.nr);
+                const int32_t l = (jcc - 1) * inv + 1, r = std::min(jcc * inv, id11.nc);
+                for (int32_t j = l; j <= r; ++j)
+                    for (int32_t i = u; i <= d; ++i) on11(i, j) = id11(i, j) > 0 ? id1(icc, jcc) : kNodata;
+            }
+    } else {
+        const int32_t fac = f11 / f1;
+        for (int32_t jcc = 1; jcc <= id11.nc; ++jcc)
+            for (int32_t icc = 1; icc <= id11.nr; ++icc) {
+                if (id11(icc, jcc) < 1) continue;
+                const int32_t u = std::max(1, (icc - 1) * fac + 1), d = std::min(icc * fac, id1.nr);
+                const int32_t l = std::max(1, (jcc - 1) * fac + 1), r = std::min(jcc * fac, id1.nc);
+                for (int32_t j = l; j <= r; ++j)
+                    for (int32_t i = u; i <= d; ++i) on1(i, j) = id1(i, j) > 0 ? id11(icc, jcc) : kNodata;
+            }
+    }
+    l1_l11.clear();
+    l11_l1.clear();
+    for (int32_t j = 1; j <= id1.nc; ++j)
+        for (int32_t i = 1; i <= id1.nr; ++i)
+            if (id1(i, j) > 0) l1_l11.push_back(on1(i, j));
+    for (int32_t j = 1; j <= id11.nc; ++j)
+        for (int32_t i = 1; i <= id11.nr; ++i)
+            if (id11(i, j) > 0) l11_l1.push_back(on11(i, j));
     return true;
 }
 

@@ -73,4 +73,10 @@ struct L11NetworkOut {
 // cartesian coordinates (iFlag_cordinate_sys = 0).
 bool build_l11_network(const L0FlowInput &in, L11NetworkOut &out, std::string &err);
 
+// L11_L1_mapping (src/mRM/mo_mrm_net_startup.f90:61-226) for L1 and L11
+// grids at factors f1 and f11 of the L0 grid: L1_L11_Id [L1 cells] and
+// L11_L1_Id [L11 cells].
+bool l1_l11_mapping(int32_t nr0, int32_t nc0, const uint8_t *mask0, int32_t f1, int32_t f11,
+                    std::vector<int32_t> &l1_l11, std::vector<int32_t> &l11_l1, std::string &err);
+
 } // namespace mhm

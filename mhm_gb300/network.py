@@ -11,10 +11,26 @@ import numpy as np
 from . import _lib
 
 
+# rotate_fdir_variable (src/mRM/mo_mrm_read_data.f90:527-597): flow
+# directions of an ESRI-style grid file become mRM's codes on the transposed
+# (x, y) grid
+_ROTATE = {1: 4, 2: 2, 4: 1, 8: 128, 16: 64, 32: 32, 64: 16, 128: 8}
+
+
+def rotate_fdir(fdir):
+    """mRM's internal flow-direction codes from those read from a grid file."""
+    f = np.asarray(fdir, np.int32)
+    out = f.copy()
+    for a, b in _ROTATE.items():
+        out[f == a] = b
+    return out
+
+
 def l11_network(nrows0: int, ncols0: int, mask0, fdir0, facc0, elev0, cellsize0: float, factor: int,
                 lcover0=None, lc_class_imp: int = 2) -> dict:
-    """mask0 [ncols0 * nrows0] (mHM's column-major (x, y) order), fdir0 /
-    facc0 / elev0 packed over the mask, lcover0 [scenes][cells] or None.
+    """mask0 [ncols0 * nrows0] (mHM's column-major (x, y) order), fdir0 (mRM's
+    internal codes: rotate_fdir of a grid file's) / facc0 / elev0 packed over
+    the mask, lcover0 [scenes][cells] or None.
     Returns the L11 arrays (1-based link and node indexes as mRM's)."""
     L = _lib.load()
     m = np.ascontiguousarray(mask0, np.uint8)
@@ -51,3 +67,20 @@ def l11_network(nrows0: int, ncols0: int, mask0, fdir0, facc0, elev0, cellsize0:
         res[k] = res[k][:nl]
     res["frac_fp_imp"] = res["frac_fp_imp"][:ns, :nl]
     return res
+
+
+def l1_l11_mapping(nrows0: int, ncols0: int, mask0, factor1: int, factor11: int):
+    """(L1_L11_Id, L11_L1_Id) of mhm_l1_l11_mapping."""
+    L = _lib.load()
+    m = np.ascontiguousarray(mask0, np.uint8)
+    mp = m.ctypes.data_as(C.POINTER(C.c_uint8))
+    n1, n11 = C.c_int32(), C.c_int32()
+    if L.mhm_l11_network_size(nrows0, ncols0, mp, factor1, C.byref(n1)) or \
+            L.mhm_l11_network_size(nrows0, ncols0, mp, factor11, C.byref(n11)):
+        raise ValueError("grid sizes")
+    a = np.zeros(n1.value, np.int32)
+    b = np.zeros(n11.value, np.int32)
+    ip = C.POINTER(C.c_int32)
+    if L.mhm_l1_l11_mapping(nrows0, ncols0, mp, factor1, factor11, a.ctypes.data_as(ip), b.ctypes.data_as(ip)):
+        raise ValueError("mhm_l1_l11_mapping failed (see stderr)")
+    return a, b
