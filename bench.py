@@ -347,6 +347,8 @@ def run_gpu(args) -> dict:
         out["batched"] = run_ensemble(args, device)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(dom, l0, gamma, hf, chunk, args)
+    if rank == 0 and not args.no_serving:
+        out["serving"] = run_serving(args)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
@@ -451,15 +453,20 @@ def run_serving(args) -> dict:
     import torch
     from mhm_gb300 import serve
     torch.cuda.set_device(0)
+    t_start = time.perf_counter()
     basins = serve.make_catalogue(args.serve_basins, seed=11)
+    cells = [b.n_cells for b in basins]
     out = {"metric": "serving: p50/p99 latency [s] and cell-timesteps/s (mHM+mRM, FP64)", "unit": "s",
-           "catalogue": [b.name for b in basins], "hbm_budget_gb": 150, "rates": []}
-    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16)
+           "catalogue": [b.name for b in basins], "cells_min": int(min(cells)), "cells_max": int(max(cells)),
+           "hbm_budget_gb": 150, "requests_per_rate": args.serve_requests,
+           "horizon_days": [30, 365], "rates": []}
+    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16)   # spin-ups, forcing windows
     srv.close()
     for rate in args.serve_rates:
         reqs = serve.make_requests(basins, args.serve_requests, rate, seed=int(rate))
-        srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16)
-        batched = srv.serve(reqs)
+        srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=16, fused=True)
+        batched = srv.serve(reqs, timeout_s=1800)
+        srv.close()
         plain_reqs = serve.make_requests(basins, args.serve_requests, rate, seed=int(rate))
         plain = serve.serve_plain(basins, plain_reqs, 240)
         same = all(np.array_equal(a.discharge(), b.discharge()) for a, b in zip(
@@ -467,6 +474,7 @@ def run_serving(args) -> dict:
         out["rates"].append({"rate_per_s": rate, "batched": batched, "plain": plain,
                              "throughput_ratio": batched["throughput"] / plain["throughput"],
                              "results_identical": bool(same)})
+    out["wall_s"] = time.perf_counter() - t_start
     return out
 
 
@@ -639,9 +647,10 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the kernel variant of MHM_CELL_OCC / MHM_ROUTE_SUB (for profiling)")
     ap.add_argument("--serve", action="store_true", help="measure the serving loop instead (p50/p99 latency)")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0, 500.0])
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0])
+    ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-basins", type=int, default=12)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement of the default run")
     ap.add_argument("--uneven", action="store_true", help="measure the batched uneven-basins workload instead")
     ap.add_argument("--uneven-basins", type=int, default=64)
     args = ap.parse_args()

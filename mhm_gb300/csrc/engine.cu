@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "fp64i.h"
 #include "hmath.h"
 #include "mhm_gpu.h"
@@ -276,6 +278,15 @@ struct DeviceGuard {
     DeviceGuard &operator=(const DeviceGuard &) = delete;
 };
 
+// An NVTX range over a host phase (shown by Nsight Systems / ncu's NVTX
+// filters; free when no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // First statement of every context entry point that touches the GPU.
 #define ON_CTX_DEVICE(ctx)                                                                                         \
     DeviceGuard dev_guard_((ctx)->device);                                                                         \
@@ -526,6 +537,7 @@ void *mhm_ctx_stream(mhm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr;
 
 int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
 {
+    NvtxRange nvtx_("mhm: context create");
     if (!d || !out) return MHM_ERR_INVALID;
     *out = nullptr;
     mhm_ctx *ctx = new mhm_ctx();
@@ -1057,6 +1069,7 @@ struct FusedStage {
 static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gauge,
                        const int32_t *member_tt0 = nullptr, FusedStage *fs = nullptr)
 {
+    NvtxRange nvtx_("mhm: enqueue run");
     if (tt0 < 1 || n_steps < 1) return fail(ctx, MHM_ERR_INVALID, "tt0 >= 1 and n_steps >= 1 required");
     const size_t N = ctx->N, M = ctx->M, L = ctx->L;
     const int H = ctx->H;
@@ -1369,6 +1382,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         CK(cudaEventRecord(ctx->ev_cell_done[slot], ctx->stream), "record cell done");
         ctx->slot_used[slot] = true;
         // ---- routing of this chunk on route_stream ----
+        NvtxRange nvtx_route("mhm: routing chunk");
         cudaStream_t rs = ctx->route_stream;
         CK(cudaStreamWaitEvent(rs, ctx->ev_cell_done[slot], 0), "wait cell");
         if (ctx->proc_rout >= 1) {
@@ -1621,6 +1635,7 @@ int mhm_poll(mhm_ctx *ctx, int32_t *done)
 
 int mhm_sync(mhm_ctx *ctx)
 {
+    NvtxRange nvtx_("mhm: sync");
     if (!ctx) return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (ctx->timing && ctx->run_a) {
@@ -1749,6 +1764,7 @@ int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg)
 int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_choices, const int32_t *chunk_choices,
                     mhm_launch_config *best_out, double *ms_out)
 {
+    NvtxRange nvtx_("mhm: autotune");
     if (!ctx || n_steps < 1 || n_chunk_choices < 0 || n_chunk_choices > 8 ||
         (n_chunk_choices > 0 && !chunk_choices))
         return MHM_ERR_INVALID;
@@ -2174,6 +2190,7 @@ int mhm_l11_network_size(int32_t nrows0, int32_t ncols0, const uint8_t *mask0, i
 
 int mhm_l11_network(const mhm_l0_flow *in, mhm_l11_network_out *out)
 {
+    NvtxRange nvtx_("mhm: network start-up");
     if (!in || !out || !in->mask0 || !in->fdir0 || !in->facc0 || !in->elev0 || in->n_cells0 < 1 ||
         !(in->cellsize0 > 0.0) || in->n_lc_scenes < 0 || (in->n_lc_scenes > 0 && !in->lcover0))
         return MHM_ERR_INVALID;
@@ -2280,6 +2297,7 @@ int mhm_gamma_layout(int32_t proc_soilmoist, int32_t proc_pet, int32_t proc_rout
 
 int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
 {
+    NvtxRange nvtx_("mhm: MPR set-up");
     if (!ctx || !l0) return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
@@ -2327,6 +2345,7 @@ int mhm_mpr_setup(mhm_ctx *ctx, const mhm_l0_desc *l0)
 
 int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int32_t n_gamma)
 {
+    NvtxRange nvtx_("mhm: MPR");
     if (!ctx || !gammas) return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the parameters
@@ -2430,6 +2449,7 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
 // begins on the device.
 int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n_gamma)
 {
+    NvtxRange nvtx_("mhm: MPR (static scratch)");
     if (!ctx || !gamma) return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (!ctx->mpr_ready) return fail(ctx, MHM_ERR_INVALID, "mhm_mpr_setup has not been called");
@@ -2641,6 +2661,7 @@ const char *mhm_batch_last_error(const mhm_batch *b) { return b ? b->err.c_str()
 int mhm_batch_run_members(mhm_batch *b, int32_t n, mhm_ctx *const *ctxs, const int32_t *const *member_tt0,
                           int32_t n_steps, double *const *q_gauge)
 {
+    NvtxRange nvtx_("mhm: fused batch round");
     if (!b || n < 1 || !ctxs || !member_tt0 || n_steps < 1) return MHM_ERR_INVALID;
     auto bfail = [&](int code, const std::string &m) {
         b->err = m;
