@@ -454,7 +454,7 @@ def run_serving(args) -> dict:
     from mhm_gb300 import serve
     torch.cuda.set_device(0)
     t_start = time.perf_counter()
-    basins = serve.make_catalogue(args.serve_basins, seed=11)
+    basins = serve.make_catalogue(args.serve_basins, seed=11, include_max=True)   # up to 1e6 cells
     cells = [b.n_cells for b in basins]
     out = {"metric": "serving: p50/p99 latency [s] and cell-timesteps/s (mHM+mRM, FP64)", "unit": "s",
            "catalogue": [b.name for b in basins], "cells_min": int(min(cells)), "cells_max": int(max(cells)),

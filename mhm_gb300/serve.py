@@ -518,13 +518,16 @@ def run_batched(basins: list[Basin], requests: list[Request], chunk: int, proc_s
 
 
 def make_catalogue(n: int, seed: int = 11, n_min: float = 1e3, n_max: float = 1e6, l0_factor: int = 2,
-                   h_min: int = 2, h_max: int = 6) -> list[Basin]:
+                   h_min: int = 2, h_max: int = 6, include_max: bool = False) -> list[Basin]:
     """Basins with cell counts log-uniform in [n_min, n_max] (square-ish L1
-    grids), h_min..h_max soil horizons, their own fractal DEM / D8 network."""
+    grids), h_min..h_max soil horizons, their own fractal DEM / D8 network;
+    with include_max the last basin has n_max cells."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
         cells = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        if include_max and i == n - 1:
+            cells = n_max
         nr = max(8, int(round(math.sqrt(cells))))
         nc = max(8, int(round(cells / nr)))
         H = int(rng.integers(h_min, h_max + 1))
