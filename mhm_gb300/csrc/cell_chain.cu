@@ -35,16 +35,23 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
 
 // The persistent multi-context launch: hl = horizon planes of the shared
 // layout (6 or 8, at least every context's horizon count), `lean` as the
-// contexts' common code path.  One resident wave of blocks takes the tiles.
-cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, cudaStream_t s)
+// contexts' common code path, occ = resident blocks per SM the registers are
+// sized for (4 or 8).  One resident wave of blocks takes the tiles.
+cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, int occ, cudaStream_t s)
 {
     if (f.n_tiles <= 0) return cudaSuccess;
     const int block = 128;
-    const size_t smem = (size_t)HS_PLANES * hl * block * sizeof(double);
+    const size_t smem = (size_t)hs_planes(hl) * hl * block * sizeof(double);
     void (*k)(const FusedCellArgs) = nullptr;
-    if (hl == 6) k = lean ? cell_chain_fused_kernel<6, true> : cell_chain_fused_kernel<6, false>;
-    else if (hl == 8) k = lean ? cell_chain_fused_kernel<8, true> : cell_chain_fused_kernel<8, false>;
-    else return cudaErrorInvalidValue;
+    const bool o8 = occ >= 8;
+    if (hl == 6)
+        k = lean ? (o8 ? cell_chain_fused_kernel<6, true, 8> : cell_chain_fused_kernel<6, true, 4>)
+                 : (o8 ? cell_chain_fused_kernel<6, false, 8> : cell_chain_fused_kernel<6, false, 4>);
+    else if (hl == 8)
+        k = lean ? (o8 ? cell_chain_fused_kernel<8, true, 8> : cell_chain_fused_kernel<8, true, 4>)
+                 : (o8 ? cell_chain_fused_kernel<8, false, 8> : cell_chain_fused_kernel<8, false, 4>);
+    else
+        return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, nb = 0;

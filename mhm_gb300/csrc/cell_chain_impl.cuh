@@ -87,10 +87,11 @@ __device__ double pet_penman(double net_rad, double tavg, double act_vap, double
            (slope + kPsychro * 1.0 / 1.0 * (1.0 + rs / ra));
 }
 
-// Per-thread scalars live in registers; the per-horizon parameters and soil
-// moisture live in shared memory, [plane][H][blockDim] (consecutive threads
-// -> consecutive words), so the horizon loop stays rolled: fewer registers
-// (more warps per SM) and a smaller instruction footprint.
+// Per-thread scalars live in registers; the soil moisture of each horizon
+// and two reciprocals per horizon live in shared memory, [plane][H][blockDim]
+// (consecutive threads -> consecutive words), so the horizon loop stays
+// rolled: fewer registers (more warps per SM) and a smaller instruction
+// footprint.
 struct CellRegs {
     // states
     double interc, snow, seal, unsat, sat;
@@ -110,7 +111,15 @@ struct CellRegs {
 // and each division runs hm_div_r -- the same correctly rounded quotient as
 // hm_div at about half its integer instructions.  HS_RSMS / HS_RDEN hold the
 // reciprocals' bits.
-enum HorizonPlane : int { HS_SMS = 0, HS_FROOTS, HS_FC, HS_PW, HS_BETA, HS_SM, HS_RSMS, HS_RDEN, HS_PLANES };
+//
+// The read-only per-horizon parameters (fRoots, SMs, FC, PW, beta) are copied
+// to shared memory too when that costs no occupancy -- up to 3 horizons,
+// where 8 planes of 8 blocks fit the SM -- and are read from the parameter
+// planes in global memory (L1/L2-cached, coalesced) otherwise: with 6
+// horizons they would take 48 KB per block and cap the SM at 4 blocks.
+enum HorizonPlane : int { HS_SM = 0, HS_RSMS, HS_RDEN, HS_PAR0, HS_PLANES_ALL = HS_PAR0 + 5 };
+__host__ __device__ constexpr bool hs_params_shared(int HL) { return HL <= 3; }
+__host__ __device__ constexpr int hs_planes(int HL) { return hs_params_shared(HL) ? HS_PLANES_ALL : HS_PAR0; }
 
 
 // LEAN: compiled for PET input (cases -1, 0) and the Feddes stress (soil-moisture
@@ -151,6 +160,11 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
     extern __shared__ double hsm[];
     const int tb = threadIdx.x, B = blockDim.x;
     auto hs = [&](int plane, int h) -> double & { return hsm[(plane * HL + h) * B + tb]; };
+    // the per-horizon parameters, groups 0..4 = fRoots, SMs, FC, PW, beta
+    auto hp = [&](int g, int h) -> double {
+        if constexpr (hs_params_shared(HL)) return hs(HS_PAR0 + g, h);
+        else return __ldg(P + (size_t)(P_HORIZON + g * H + h) * N);
+    };
     const bool feddes = LEAN || (a.proc_sm == 1 || a.proc_sm == 4);
     CellRegs c;
     const double c2 = a.c2TSTu;
@@ -177,13 +191,10 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
     c.r_jarvis = hm_recip_of(c.jarvis);
 #pragma unroll 1
     for (int h = 0; h < H; ++h) {
-        const double fr = par(P_HORIZON + h), sms = par(P_HORIZON + H + h), fc = par(P_HORIZON + 2 * H + h);
-        const double pw = par(P_HORIZON + 3 * H + h);
-        hs(HS_FROOTS, h) = fr;
-        hs(HS_SMS, h) = sms;
-        hs(HS_FC, h) = fc;
-        hs(HS_PW, h) = pw;
-        hs(HS_BETA, h) = par(P_HORIZON + 4 * H + h);
+        if constexpr (hs_params_shared(HL)) {
+            for (int g = 0; g < 5; ++g) hs(HS_PAR0 + g, h) = __ldg(P + (size_t)(P_HORIZON + g * H + h) * N);
+        }
+        const double sms = hp(1, h), fc = hp(2, h), pw = hp(3, h);
         hs(HS_RSMS, h) = hm_b2d(hm_recip_of(sms));
         hs(HS_RDEN, h) = hm_b2d(hm_recip_of(feddes ? fc - pw : sms - pw)); // mo_soil_moisture.f90:358, :435
         hs(HS_SM, h) = reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
@@ -371,12 +382,12 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
 #pragma unroll 1
             for (int h = 0; h < H; ++h) {
                 const double pin = infil;
-                const double sms = hs(HS_SMS, h);
+                const double sms = hp(1, h);
                 double smh = hs(HS_SM, h);
                 if (!hm_gt(smh, sms)) { // else the horizon passes its input on: infil stays pin
                     double frac_runoff = 0.0;
                     if (hm_gt(smh, kEps))
-                        frac_runoff = hm_exp(hs(HS_BETA, h) * hm_log(hm_div_r(smh, sms, hm_d2b(hs(HS_RSMS, h)))));
+                        frac_runoff = hm_exp(hp(4, h) * hm_log(hm_div_r(smh, sms, hm_d2b(hs(HS_RSMS, h)))));
                     const double tmp = pin * (1.0 - frac_runoff);
                     const double filled = smh + tmp;
                     const bool over = hm_gt(filled, sms);
@@ -385,14 +396,14 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
                 }
                 // demand minus the positive aet above (x - (+0) == x: no test for h == 0)
                 double aet = demand - aet_above;
-                const double froots = hs(HS_FROOTS, h), pw = hs(HS_PW, h);
+                const double froots = hp(0, h), pw = hp(3, h), fc = hp(2, h);
                 double stress;
                 if (feddes) {
-                    const bool wet = hm_ge(smh, hs(HS_FC, h));
+                    const bool wet = hm_ge(smh, fc);
                     stress = hm_sel(wet, froots, 0.0);
                     // mo_soil_moisture.f90:358
                     if (!wet && hm_gt(smh, pw))
-                        stress = hm_div_r(froots * (smh - pw), hs(HS_FC, h) - pw, hm_d2b(hs(HS_RDEN, h)));
+                        stress = hm_div_r(froots * (smh - pw), fc - pw, hm_d2b(hs(HS_RDEN, h)));
                 } else {
                     // with SMs == PW the quotient can be NaN (0 / 0): IEEE
                     // comparisons then leave the stress at 0 as the oracle does
@@ -467,7 +478,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
                 if (pl[OF_SM] >= 0 || pl[OF_SM_ALL] >= 0) {
                     double ssm = 0.0, ssat = 0.0;
                     for (int h = 0; h < H; ++h) {
-                        const double sat_h = ow ? o.w_sms[((size_t)m * H + h) * N + k] : hs(HS_SMS, h);
+                        const double sat_h = ow ? o.w_sms[((size_t)m * H + h) * N + k] : hp(1, h);
                         if (pl[OF_SM] >= 0) oadd(pl[OF_SM] + h, hs(HS_SM, h) / sat_h);
                         ssm = ssm + hs(HS_SM, h);
                         ssat = ssat + sat_h;
@@ -539,8 +550,8 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
 // per-item code as cell_chain_kernel, so every item's arithmetic -- and
 // result -- is that of the context's own launch.  No block waits on another:
 // a block returns when the queue is empty.
-template <int HL, bool LEAN>
-__global__ void __launch_bounds__(128, 4) cell_chain_fused_kernel(const FusedCellArgs f)
+template <int HL, bool LEAN, int MINB>
+__global__ void __launch_bounds__(128, MINB) cell_chain_fused_kernel(const FusedCellArgs f)
 {
     __shared__ CellArgs sa;
     __shared__ int32_t tile;
@@ -566,7 +577,7 @@ cudaError_t launch_cell_chain_h(const CellArgs &a, int H, cudaStream_t s)
     const int64_t n = (int64_t)a.n_cells * a.n_members;
     const int block = 128;
     const unsigned grid = (unsigned)((n + block - 1) / block);
-    const size_t smem = (size_t)HS_PLANES * H * block * sizeof(double);
+    const size_t smem = (size_t)hs_planes(H) * H * block * sizeof(double);
     switch (H) {
 #define MHM_CASE(HH)                                                                                               \
     case HH:                                                                                                       \

@@ -39,7 +39,7 @@ cudaError_t launch_hmath_eval(int op, int64_t n, const double *x, const double *
 cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *sink, cudaStream_t s);
 cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s);
 cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s);
-cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, cudaStream_t s);
+cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, int occ, cudaStream_t s);
 } // namespace mhm
 
 using namespace mhm;
@@ -234,6 +234,7 @@ struct mhm_batch {
     int64_t *h_item0 = nullptr;
     size_t cap_ctx = 0, cap_tiles = 0;
     int64_t rounds = 0, tiles_total = 0;
+    int32_t occ = 8; // register variant of the fused launch: 4 or 8 resident blocks per SM
     std::string err;
 };
 
@@ -2627,6 +2628,7 @@ int mhm_batch_create(int32_t device, mhm_batch **out)
     if (device >= ndev) return MHM_ERR_INVALID;
     mhm_batch *b = new mhm_batch();
     b->device = device >= 0 ? device : cur;
+    if (const char *s = std::getenv("MHM_FUSED_OCC")) b->occ = std::atoi(s) >= 8 ? 8 : 4;
     DeviceGuard dg(b->device);
     if (dg.err != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) != cudaSuccess ||
@@ -2758,7 +2760,7 @@ int mhm_batch_run_members(mhm_batch *b, int32_t n, mhm_ctx *const *ctxs, const i
     f.tile_item0 = b->tile_item0.p;
     f.n_tiles = (int32_t)n_tiles;
     f.queue = b->queue.p;
-    if (cudaError_t e = launch_cell_chain_fused(f, hl, lean, b->stream))
+    if (cudaError_t e = launch_cell_chain_fused(f, hl, lean, b->occ, b->stream))
         return bfail(MHM_ERR_CUDA, std::string("fused cell chain: ") + cudaGetErrorString(e));
     g_launches++;
     if (cudaEventRecord(b->ev_done, b->stream) != cudaSuccess) return bfail(MHM_ERR_CUDA, "event");
