@@ -282,7 +282,7 @@ def run_gpu(args) -> dict:
     ms, value = replica_throughput(ms, float(N) * chunk * args.steps, world, device)
 
     # ---- e2e: host forcing (pinned), H2D + compute + D2H of the gauge series per step ----
-    e2e_steps = max(1, min(args.steps, 8))
+    e2e_steps = max(1, min(args.steps, 16))
     step(args.warmup + args.steps, on_device=False)  # warm the staging buffers
     g.sync()
     barrier()
