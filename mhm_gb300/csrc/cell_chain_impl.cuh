@@ -127,19 +127,16 @@ __host__ __device__ constexpr int hs_planes(int HL) { return hs_params_shared(HL
 // the Hargreaves / Priestley-Taylor / Penman-Monteith and Jarvis code is not in
 // the instruction stream and the register allocation.
 //
-// cell_chain_item advances work item `gid` (member gid / n_cells, cell
-// gid % n_cells) of the launch described by `a`.  HL sizes the shared-memory
-// horizon planes; DYN takes the horizon count from a.n_horizons (<= HL) at
-// run time, so that one launch can serve contexts with different horizon
-// counts (the fused multi-context launch); otherwise it is HL.
+// cell_chain_item advances cell k of member m (both in range) of the launch
+// described by `a`.  HL sizes the shared-memory horizon planes; DYN takes the
+// horizon count from a.n_horizons (<= HL) at run time, so that one launch can
+// serve contexts with different horizon counts (the fused multi-context
+// launch); otherwise it is HL.
 template <int HL, bool FLUX, bool LEAN, bool DYN>
-__device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t gid)
+__device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, const int k)
 {
     const int H = DYN ? a.n_horizons : HL;
     const int64_t N = a.n_cells;
-    if (gid >= N * a.n_members) return;
-    const int m = (int)(gid / N);
-    const int k = (int)(gid - (int64_t)m * N);
     const StepInfo *steps = a.steps;
     bool reset_sm = a.reset_sm != 0;
     if (a.member_step0) {
@@ -339,12 +336,12 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
             const bool warm = hm_gt(temp, c.tthresh);
             const double rain = hm_sel(warm, throughfall, 0.0);
             const double snowf = hm_sel(warm, 0.0, throughfall);
-            const bool low = dd_thr_ok && hm_le(prec, c.dd_thr);
-            const double dd = hm_sel(low, c.ddnopre_s + c.ddinc * prec, c.ddmax_s);
             melt = 0.0;
             if (warm) {
                 double snow_left = 0.0;
-                if (hm_gt0(c.snow)) {
+                if (hm_gt0(c.snow)) { // the degree-day factor only matters here
+                    const bool low = dd_thr_ok && hm_le(prec, c.dd_thr);
+                    const double dd = hm_sel(low, c.ddnopre_s + c.ddinc * prec, c.ddmax_s);
                     const double aux = dd * (temp - c.tthresh);
                     const bool all = hm_gt(aux, c.snow);
                     melt = hm_sel(all, c.snow, aux);
@@ -391,7 +388,9 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
                     const double tmp = pin * (1.0 - frac_runoff);
                     const double filled = smh + tmp;
                     const bool over = hm_gt(filled, sms);
-                    infil = hm_sel(over, pin + (smh - sms), pin - tmp);
+                    // pin + (smh - sms) or pin - tmp, as one addition: pin - tmp is
+                    // pin + (-tmp) exactly, so the select picks the second operand
+                    infil = pin + hm_sel(over, smh - sms, hm_neg(tmp));
                     smh = hm_sel(over, sms, filled);
                 }
                 // demand minus the positive aet above (x - (+0) == x: no test for h == 0)
@@ -416,10 +415,12 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
                 }
                 aet = aet * stress;
                 aet = hm_sel(hm_lt0(aet), 0.0, aet);
+                // enough: storage smh - aet, aet kept; else aet = smh - eps and
+                // storage eps -- one subtraction serves both cases
                 const bool enough = hm_gt(smh, aet);
-                const double left = smh - aet;
-                aet = hm_sel(enough, aet, smh - kEps);
-                smh = hm_sel(enough, left, kEps);
+                const double d = smh - hm_sel(enough, aet, kEps);
+                aet = hm_sel(enough, aet, d);
+                smh = hm_sel(enough, d, kEps);
                 smh = hm_sel(hm_lt(smh, kEps), kEps, smh);
                 hs(HS_SM, h) = smh;
                 aet_above = hm_sel(hm_gt0(aet), aet_above + aet, aet_above);
@@ -537,10 +538,33 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int64_t
     if (a.nonfinite && (nonfin >> 63)) atomicOr(a.nonfinite + m, 1);
 }
 
+// Work items of a launch, by block: one member's 128 consecutive cells, or --
+// when the members come in groups of 4 -- 32 consecutive cells of 4 members
+// (one member per warp, so a warp still walks 32 neighbouring cells of one
+// parameter set).  The blocks of one cell tile are consecutive in launch order
+// and start together, so the forcing rows every member reads come from L1/L2
+// after the first member group instead of from DRAM once per member.
+__host__ __device__ constexpr bool member_tiles(int64_t n_members) { return n_members > 1 && n_members % 4 == 0; }
+
 template <int H, int MINB, bool FLUX, bool LEAN>
 __global__ void __launch_bounds__(128, MINB) cell_chain_kernel(const CellArgs a)
 {
-    cell_chain_item<H, FLUX, LEAN, false>(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    const int64_t N = a.n_cells;
+    int m, k;
+    if (member_tiles(a.n_members)) {
+        const int64_t n_groups = a.n_members / 4;
+        const int64_t tile = blockIdx.x / n_groups;
+        m = (int)(blockIdx.x - tile * n_groups) * 4 + (int)(threadIdx.x >> 5);
+        const int64_t kk = tile * 32 + (threadIdx.x & 31);
+        if (kk >= N) return;
+        k = (int)kk;
+    } else {
+        const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (gid >= N * a.n_members) return;
+        m = (int)(gid / N);
+        k = (int)(gid - (int64_t)m * N);
+    }
+    cell_chain_item<H, FLUX, LEAN, false>(a, m, k);
 }
 
 // The cell chain of several contexts in one persistent launch: a work queue
@@ -564,7 +588,12 @@ __global__ void __launch_bounds__(128, MINB) cell_chain_fused_kernel(const Fused
         uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
         for (int w = threadIdx.x; w < (int)(sizeof(CellArgs) / 4); w += blockDim.x) dst[w] = __ldg(src + w);
         __syncthreads();
-        cell_chain_item<HL, false, LEAN, true>(sa, __ldg(f.tile_item0 + t) + threadIdx.x);
+        const int64_t gid = __ldg(f.tile_item0 + t) + threadIdx.x;
+        const int64_t N = sa.n_cells;
+        if (gid < N * sa.n_members) {
+            const int m = (int)(gid / N);
+            cell_chain_item<HL, false, LEAN, true>(sa, m, (int)(gid - (int64_t)m * N));
+        }
         __syncthreads(); // the next tile may overwrite sa and the horizon planes
     }
 }
@@ -576,7 +605,9 @@ cudaError_t launch_cell_chain_h(const CellArgs &a, int H, cudaStream_t s)
 {
     const int64_t n = (int64_t)a.n_cells * a.n_members;
     const int block = 128;
-    const unsigned grid = (unsigned)((n + block - 1) / block);
+    const unsigned grid = member_tiles(a.n_members)
+                              ? (unsigned)(((int64_t)a.n_cells + 31) / 32 * (a.n_members / 4))
+                              : (unsigned)((n + block - 1) / block);
     const size_t smem = (size_t)hs_planes(H) * H * block * sizeof(double);
     switch (H) {
 #define MHM_CASE(HH)                                                                                               \

@@ -45,6 +45,18 @@ HM_FN int hm_lt0(double x) { return hm_okey(x) < 0; }
 /* c ? a : b as a select of the bit patterns: a select of doubles is issued
  * as an FP64-pipe move on this GPU (measured), an integer select is not */
 HM_FN double hm_sel(int c, double a, double b) { return hm_b2d(c ? hm_d2b(a) : hm_d2b(b)); }
+/* -x as a flip of the sign bit on the integer pipe (inline PTX on the device,
+ * so that it is not turned into an FP64 negation); a + (-b) is exactly a - b */
+HM_FN double hm_neg(double x)
+{
+#if defined(__CUDA_ARCH__)
+    uint64_t r;
+    asm("xor.b64 %0, %1, 0x8000000000000000;" : "=l"(r) : "l"(hm_d2b(x)));
+    return hm_b2d(r);
+#else
+    return hm_b2d(hm_d2b(x) ^ 0x8000000000000000ULL);
+#endif
+}
 /* min/max with the selection rules of the reference's (a < b ? a : b) */
 HM_FN double hm_min_sel(double a, double b) { return hm_sel(hm_lt(a, b), a, b); }
 
