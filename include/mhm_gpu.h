@@ -259,7 +259,10 @@ typedef struct mhm_launch_config {
     int32_t cell_blocks_per_sm; /* cell-chain register variant: 4, 6 or 8 resident blocks per SM */
     int32_t route_sub_steps;    /* steps per routing wavefront sub-chunk, 1..16 */
     int32_t chunk_steps;        /* most time steps per chunk (0: the device-memory budget decides) */
-    int32_t pad_;
+    int32_t route_cluster;      /* routing of a chunk: 0 = one launch per wavefront tick (replayed
+                                   from a CUDA graph); 4, 8 or 16 = all ticks in one launch, each
+                                   thread-block cluster of that many CTAs walking the wavefront of
+                                   its members with a hardware cluster barrier between ticks */
 } mhm_launch_config;
 int mhm_set_launch_config(mhm_ctx *ctx, const mhm_launch_config *cfg);
 int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg);
@@ -273,6 +276,11 @@ int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg);
  * configuration kept. */
 int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_choices,
                     const int32_t *chunk_choices, mhm_launch_config *best_out, double *ms_out);
+/* The routing launch mode by timing n_steps from tt0 with the context's
+ * other settings (states restored afterwards): route_cluster 0, 4, 8 and 16
+ * in that order (ms_out, may be NULL: 4 trial times); the fastest is kept and
+ * written to *cluster_out (may be NULL).  Contexts without routing keep 0. */
+int mhm_autotune_route(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *cluster_out, double *ms_out);
 
 /* Device-resident restart states: n_slots snapshot slots per context (each
  * one member's cell and routing states); save/load copy on the device,

@@ -79,7 +79,7 @@ class L0Desc(C.Structure):
 class LaunchConfig(C.Structure):
     """mhm_launch_config."""
     _fields_ = [("cell_blocks_per_sm", C.c_int32), ("route_sub_steps", C.c_int32), ("chunk_steps", C.c_int32),
-                ("pad_", C.c_int32)]
+                ("route_cluster", C.c_int32)]
 
 
 class L0Flow(C.Structure):
@@ -122,7 +122,7 @@ EXPORTS = [
     "mhm_poll", "mhm_set_meteo_weights", "mhm_set_inflow_gauges", "mhm_set_inflow_discharge",
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
-    "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping",
+    "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping", "mhm_autotune_route",
 ]
 
 _LIB = None
@@ -205,6 +205,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_set_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
     L.mhm_get_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
     L.mhm_autotune_ex.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _ip, C.POINTER(LaunchConfig), _dp]
+    L.mhm_autotune_route.argtypes = [vp, C.c_int32, C.c_int32, _ip, _dp]
     L.mhm_batch_create.argtypes = [C.c_int32, C.POINTER(vp)]
     L.mhm_batch_destroy.argtypes = [vp]
     L.mhm_batch_last_error.argtypes = [vp]

@@ -29,6 +29,7 @@ cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t j
                               int32_t stride, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
 cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
+cudaError_t launch_route_walk(const RouteArgs &a, const RouteWalk &w, int cs, cudaStream_t s);
 cudaError_t launch_qmod_step(const QmodStepArgs &a, cudaStream_t s);
 cudaError_t launch_gauge_gather(const GaugeArgs &a, cudaStream_t s);
 cudaError_t launch_qrouted(const QroutArgs &a, cudaStream_t s);
@@ -190,6 +191,10 @@ struct mhm_ctx {
     int32_t route_sub = 8; // steps per wavefront sub-chunk (4, 8 or 16)
     bool route_graphs_on = true;
     std::vector<RouteGraph> route_graphs; // most recently used last
+    // 0: one launch per wavefront tick (replayed from a CUDA graph); 4, 8, 16:
+    // the whole wavefront of a chunk in one launch of clusters of that many CTAs
+    int32_t route_cluster = 0;
+    DevBuf<int32_t> level_ptr_d;
     int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
     int32_t chunk_cap = 0; // most time steps per chunk (0: the device-memory budget decides)
     // routing case 2: per-member routing time step [s] and the link lengths
@@ -693,6 +698,7 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         for (int l = 0; l < net.n_levels; ++l)
             for (int p = net.level_ptr[l]; p < net.level_ptr[l + 1]; ++p) plev[p] = l;
         ok = ok && ck(upload(ctx->pos_level, plev.data(), L, ctx->stream), "levels");
+        ok = ok && ck(upload(ctx->level_ptr_d, net.level_ptr.data(), net.level_ptr.size(), ctx->stream), "level ptr");
         ok = ok && ck(upload(ctx->up_ptr, net.up_ptr.data(), L + 1, ctx->stream), "up ptr");
         ok = ok && ck(upload(ctx->up_pos, net.up_pos.data(), net.up_pos.size(), ctx->stream), "up pos");
         ok = ok && ck(upload(ctx->pos_flags, net.pos_flags.data(), L, ctx->stream), "flags");
@@ -729,6 +735,10 @@ int mhm_ctx_create(const mhm_domain_desc *d, int32_t device, mhm_ctx **out)
         if (v == 4 || v == 6 || v == 8) ctx->cell_occ = v;
     }
     if (const char *s = std::getenv("MHM_ROUTE_GRAPH")) ctx->route_graphs_on = std::atoi(s) != 0;
+    if (const char *s = std::getenv("MHM_ROUTE_CLUSTER")) {
+        int v = std::atoi(s);
+        if (v == 0 || v == 4 || v == 8 || v == 16) ctx->route_cluster = v;
+    }
     *out = ctx;
     return MHM_OK;
 }
@@ -1464,6 +1474,15 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             const int n_sub = (n_rsteps + r.sub - 1) / r.sub;
             const int n_ticks = D + n_sub - 1;
             auto enqueue_ticks = [&]() -> int {
+                if (ctx->route_cluster > 0) { // all ticks in one launch
+                    RouteWalk w{};
+                    w.level_ptr = ctx->level_ptr_d.p;
+                    w.n_levels = D;
+                    w.n_sub = n_sub;
+                    w.n_ticks = n_ticks;
+                    CK(launch_route_walk(r, w, ctx->route_cluster, rs), "route walk launch");
+                    return MHM_OK;
+                }
                 for (int k = 0; k < n_ticks; ++k) {
                     const int lo = std::max(0, k - n_sub + 1), hi = std::min(k, D - 1);
                     r.tick = k;
@@ -1473,7 +1492,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
                 }
                 return MHM_OK;
             };
-            if (ctx->route_graphs_on) {
+            if (ctx->route_graphs_on && ctx->route_cluster == 0) {
                 auto &cache = ctx->route_graphs;
                 auto it = std::find_if(cache.begin(), cache.end(),
                                        [&](const RouteGraph &g) { return same_route_shape(g.key, r); });
@@ -1507,7 +1526,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             } else if (int rc = enqueue_ticks()) {
                 return rc;
             }
-            g_launches += n_ticks;
+            g_launches += ctx->route_cluster > 0 ? 1 : n_ticks;
             if (R > 1 || F > 1) {
                 QmodStepArgs qs{};
                 qs.n_members = ctx->M;
@@ -1745,10 +1764,13 @@ int mhm_set_launch_config(mhm_ctx *ctx, const mhm_launch_config *cfg)
     if (cfg->route_sub_steps < 1 || cfg->route_sub_steps > 16)
         return fail(ctx, MHM_ERR_INVALID, "route_sub_steps must be 1..16");
     if (cfg->chunk_steps < 0) return fail(ctx, MHM_ERR_INVALID, "chunk_steps must be >= 0");
+    if (cfg->route_cluster != 0 && cfg->route_cluster != 4 && cfg->route_cluster != 8 && cfg->route_cluster != 16)
+        return fail(ctx, MHM_ERR_INVALID, "route_cluster must be 0, 4, 8 or 16");
     if (int rc = mhm_sync(ctx)) return rc;
     ctx->cell_occ = cfg->cell_blocks_per_sm;
     ctx->route_sub = cfg->route_sub_steps;
     ctx->chunk_cap = cfg->chunk_steps;
+    ctx->route_cluster = cfg->route_cluster;
     return MHM_OK;
 }
 
@@ -1758,9 +1780,85 @@ int mhm_get_launch_config(mhm_ctx *ctx, mhm_launch_config *cfg)
     cfg->cell_blocks_per_sm = ctx->cell_occ;
     cfg->route_sub_steps = ctx->route_sub;
     cfg->chunk_steps = ctx->chunk_cap;
-    cfg->pad_ = 0;
+    cfg->route_cluster = ctx->route_cluster;
     return MHM_OK;
 }
+
+// The autotuners' trial runs: every trial starts from the same states (a
+// device copy taken first and put back after each trial and at the end), the
+// outputs are switched off while trials run, and a trial is timed with events
+// from its first enqueue to the join of all streams.
+struct TuneScope {
+    mhm_ctx *ctx;
+    DevBuf<double> keep;
+    size_t n_cells_st = 0, n_rt = 0;
+    bool rout = false;
+    int32_t out_t = 0, out_q = 0, out_f = 0;
+    bool fso_on = false, qro_on = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+
+    explicit TuneScope(mhm_ctx *c) : ctx(c)
+    {
+        out_t = ctx->out_tro;
+        out_q = ctx->out_qmod;
+        out_f = ctx->out_flux;
+        ctx->out_tro = ctx->out_qmod = ctx->out_flux = 0;
+        fso_on = ctx->fso.on; // trials add nothing to the outputs
+        qro_on = ctx->qro.on;
+        ctx->fso.on = ctx->qro.on = false;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+    }
+    ~TuneScope()
+    {
+        ctx->out_tro = out_t;
+        ctx->out_qmod = out_q;
+        ctx->out_flux = out_f;
+        ctx->fso.on = fso_on;
+        ctx->qro.on = qro_on;
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+    int copy_states(bool save)
+    {
+        const size_t M = ctx->M, L = ctx->L;
+        if (save) {
+            rout = ctx->proc_rout >= 1 && L > 0;
+            n_cells_st = M * n_state_planes(ctx->H) * ctx->N;
+            n_rt = rout ? 4 * M * L : 0;
+            CK(keep.ensure(n_cells_st + n_rt), "autotune state copy");
+        }
+        double *const rt[4] = {ctx->qtin1.p, ctx->qtr1.p, ctx->qout_last.p, ctx->qmod_last.p};
+        CK(cudaMemcpyAsync(save ? keep.p : ctx->states.p, save ? ctx->states.p : keep.p, n_cells_st * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream),
+           "state copy");
+        for (int i = 0; rout && i < 4; ++i)
+            CK(cudaMemcpyAsync(save ? keep.p + n_cells_st + i * M * L : rt[i],
+                               save ? rt[i] : keep.p + n_cells_st + i * M * L, M * L * sizeof(double),
+                               cudaMemcpyDeviceToDevice, ctx->stream),
+               "state copy");
+        return MHM_OK;
+    }
+    // one trial from the kept states; *ms = its duration
+    int trial(int32_t tt0, int32_t n_steps, float *ms)
+    {
+        if (int rc = copy_states(false)) return rc;
+        cudaEventRecord(e0, ctx->stream);
+        if (int rc = run_enqueue(ctx, tt0, n_steps, nullptr)) return rc;
+        if (int rc = mhm_sync(ctx)) return rc;
+        cudaEventRecord(e1, ctx->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return fail(ctx, MHM_ERR_CUDA, "autotune timing");
+        cudaEventElapsedTime(ms, e0, e1);
+        return MHM_OK;
+    }
+    // the states as they were, once all trials are done
+    int finish(int rc)
+    {
+        if (int r2 = copy_states(false)) rc = rc ? rc : r2;
+        if (int r3 = mhm_sync(ctx)) rc = rc ? rc : r3;
+        return rc;
+    }
+};
 
 int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_choices, const int32_t *chunk_choices,
                     mhm_launch_config *best_out, double *ms_out)
@@ -1771,33 +1869,10 @@ int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_
         return MHM_ERR_INVALID;
     ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
-    const size_t N = ctx->N, M = ctx->M, L = ctx->L, ns = n_state_planes(ctx->H);
-    // every trial starts from the same states: keep a device copy
-    DevBuf<double> keep;
-    const bool rout = ctx->proc_rout >= 1 && L > 0;
-    const size_t n_cells_st = M * ns * N, n_rt = rout ? 4 * M * L : 0;
-    CK(keep.ensure(n_cells_st + n_rt), "autotune state copy");
-    double *const rt[4] = {ctx->qtin1.p, ctx->qtr1.p, ctx->qout_last.p, ctx->qmod_last.p};
-    auto copy_states = [&](bool save) -> int {
-        CK(cudaMemcpyAsync(save ? keep.p : ctx->states.p, save ? ctx->states.p : keep.p, n_cells_st * sizeof(double),
-                           cudaMemcpyDeviceToDevice, ctx->stream),
-           "state copy");
-        for (int i = 0; rout && i < 4; ++i)
-            CK(cudaMemcpyAsync(save ? keep.p + n_cells_st + i * M * L : rt[i],
-                               save ? rt[i] : keep.p + n_cells_st + i * M * L, M * L * sizeof(double),
-                               cudaMemcpyDeviceToDevice, ctx->stream),
-               "state copy");
-        return MHM_OK;
-    };
-    const int32_t out_t = ctx->out_tro, out_q = ctx->out_qmod, out_f = ctx->out_flux;
-    ctx->out_tro = ctx->out_qmod = ctx->out_flux = 0;
-    const bool fso_on = ctx->fso.on, qro_on = ctx->qro.on; // trials add nothing to the outputs
-    ctx->fso.on = ctx->qro.on = false;
+    const bool rout = ctx->proc_rout >= 1 && ctx->L > 0;
     const int32_t occ0 = ctx->cell_occ, sub0 = ctx->route_sub, cap0 = ctx->chunk_cap;
-    int rc = copy_states(true);
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    TuneScope ts(ctx);
+    int rc = ts.copy_states(true);
     const int occs[3] = {4, 6, 8}, subs[3] = {4, 8, 16};
     std::vector<int32_t> caps = {cap0};
     for (int i = 0; i < n_chunk_choices; ++i) caps.push_back(std::max<int32_t>(0, chunk_choices[i]));
@@ -1824,17 +1899,8 @@ int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_
             if (trial >= 0 && ms_out) ms_out[trial] = -1.0;
             continue;
         }
-        if ((rc = copy_states(false))) break;
-        cudaEventRecord(e0, ctx->stream);
-        if ((rc = run_enqueue(ctx, tt0, n_steps, nullptr))) break;
-        if ((rc = mhm_sync(ctx))) break;
-        cudaEventRecord(e1, ctx->stream);
-        if (cudaEventSynchronize(e1) != cudaSuccess) {
-            rc = fail(ctx, MHM_ERR_CUDA, "autotune timing");
-            break;
-        }
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
+        if ((rc = ts.trial(tt0, n_steps, &ms))) break;
         if (trial >= 0 && ms_out) ms_out[trial] = ms;
         if (trial >= 0 && ms < best) {
             best = ms;
@@ -1843,19 +1909,45 @@ int mhm_autotune_ex(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t n_chunk_
             best_cap = ctx->chunk_cap;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     ctx->cell_occ = rc == MHM_OK ? best_occ : occ0;
     ctx->route_sub = rc == MHM_OK ? best_sub : sub0;
     ctx->chunk_cap = rc == MHM_OK ? best_cap : cap0;
-    ctx->out_tro = out_t;
-    ctx->out_qmod = out_q;
-    ctx->out_flux = out_f;
-    ctx->fso.on = fso_on;
-    ctx->qro.on = qro_on;
-    if (int r2 = copy_states(false)) rc = rc ? rc : r2;
-    if (int r3 = mhm_sync(ctx)) rc = rc ? rc : r3;
+    rc = ts.finish(rc);
     if (best_out) mhm_get_launch_config(ctx, best_out);
+    return rc;
+}
+
+int mhm_autotune_route(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *cluster_out, double *ms_out)
+{
+    NvtxRange nvtx_("mhm: autotune routing");
+    if (!ctx || n_steps < 1) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc;
+    const int32_t modes[4] = {0, 4, 8, 16};
+    const int32_t mode0 = ctx->route_cluster;
+    int rc = MHM_OK;
+    int32_t best_mode = mode0;
+    if (ctx->proc_rout >= 1 && ctx->L > 1) {
+        TuneScope ts(ctx);
+        rc = ts.copy_states(true);
+        float best = 1e30f;
+        for (int trial = -4; rc == MHM_OK && trial < 4; ++trial) { // one untimed pass over the modes first
+            ctx->route_cluster = modes[trial < 0 ? trial + 4 : trial];
+            float ms = 0.f;
+            if ((rc = ts.trial(tt0, n_steps, &ms))) break;
+            if (trial < 0) continue;
+            if (ms_out) ms_out[trial] = ms;
+            if (ms < best) {
+                best = ms;
+                best_mode = ctx->route_cluster;
+            }
+        }
+        ctx->route_cluster = rc == MHM_OK ? best_mode : mode0;
+        rc = ts.finish(rc);
+    } else if (ms_out) {
+        for (int i = 0; i < 4; ++i) ms_out[i] = -1.0;
+    }
+    if (cluster_out) *cluster_out = ctx->route_cluster;
     return rc;
 }
 

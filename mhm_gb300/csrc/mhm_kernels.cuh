@@ -183,6 +183,14 @@ struct RouteArgs {
     const int32_t *member_step0; // member mode: < 0 marks an idle member (skipped)
 };
 
+// The wavefront of a chunk walked in one launch (route_walk_kernel): tick k
+// spans levels max(0, k - n_sub + 1) .. min(k, n_levels - 1), i.e. positions
+// level_ptr[lo] .. level_ptr[hi + 1] - 1.
+struct RouteWalk {
+    const int32_t *level_ptr; // [n_levels + 1] first routing position of each level
+    int32_t n_levels, n_sub, n_ticks;
+};
+
 // add_inflow (src/mRM/mo_mrm_pre_routing.f90:179-214) on a chunk's qOUT rows,
 // after the L1->L11 accumulation: per (member, routing step) the inflow
 // gauges in list order add their discharge to (headwater) or put it in place

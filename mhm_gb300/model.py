@@ -364,14 +364,26 @@ class MhmGpu:
         sm = None if soil_moist_sat is None else np.ascontiguousarray(soil_moist_sat, np.float64)
         self._check(self.L.mhm_set_output_weights(self.ctx, member, tt, _d(fs), _d(sm)), "mhm_set_output_weights")
 
-    def autotune(self, tt0: int, n_steps: int) -> dict:
+    def autotune(self, tt0: int, n_steps: int, route: bool = True) -> dict:
         """Pick the fastest cell-chain register variant and routing sub-chunk
-        by timing n_steps from tt0 (states restored afterwards)."""
+        by timing n_steps from tt0 (states restored afterwards), then, with
+        `route`, the routing launch mode (per-tick graph or cluster walk)."""
         occ = C.c_int32()
         sub = C.c_int32()
         ms = np.zeros(9)
         self._check(self.L.mhm_autotune(self.ctx, tt0, n_steps, C.byref(occ), C.byref(sub), _d(ms)), "mhm_autotune")
-        return {"cell_blocks_per_sm": occ.value, "route_sub_steps": sub.value, "trial_ms": ms.tolist()}
+        out = {"cell_blocks_per_sm": occ.value, "route_sub_steps": sub.value, "trial_ms": ms.tolist()}
+        if route:
+            out.update(self.autotune_route(tt0, n_steps))
+        return out
+
+    def autotune_route(self, tt0: int, n_steps: int) -> dict:
+        """mhm_autotune_route: route_cluster 0 (per-tick graph), 4, 8, 16 timed;
+        the fastest is kept."""
+        cl = C.c_int32()
+        ms = np.zeros(4)
+        self._check(self.L.mhm_autotune_route(self.ctx, tt0, n_steps, C.byref(cl), _d(ms)), "mhm_autotune_route")
+        return {"route_cluster": cl.value, "route_trial_ms": ms.tolist()}
 
     def autotune_ex(self, tt0: int, n_steps: int, chunk_choices=()) -> dict:
         """The autotuner over register variant x routing sub-chunk x time-chunk
@@ -383,17 +395,18 @@ class MhmGpu:
         self._check(self.L.mhm_autotune_ex(self.ctx, tt0, n_steps, ch.size, _i(ch) if ch.size else None,
                                            C.byref(best), _d(ms)), "mhm_autotune_ex")
         return {"cell_blocks_per_sm": best.cell_blocks_per_sm, "route_sub_steps": best.route_sub_steps,
-                "chunk_steps": best.chunk_steps, "trial_ms": ms.tolist()}
+                "chunk_steps": best.chunk_steps, "route_cluster": best.route_cluster, "trial_ms": ms.tolist()}
 
-    def set_launch_config(self, cell_blocks_per_sm: int = 4, route_sub_steps: int = 8, chunk_steps: int = 0):
-        cfg = _lib.LaunchConfig(cell_blocks_per_sm, route_sub_steps, chunk_steps, 0)
+    def set_launch_config(self, cell_blocks_per_sm: int = 4, route_sub_steps: int = 8, chunk_steps: int = 0,
+                          route_cluster: int = 0):
+        cfg = _lib.LaunchConfig(cell_blocks_per_sm, route_sub_steps, chunk_steps, route_cluster)
         self._check(self.L.mhm_set_launch_config(self.ctx, C.byref(cfg)), "mhm_set_launch_config")
 
     def get_launch_config(self) -> dict:
         cfg = _lib.LaunchConfig()
         self._check(self.L.mhm_get_launch_config(self.ctx, C.byref(cfg)), "mhm_get_launch_config")
         return {"cell_blocks_per_sm": cfg.cell_blocks_per_sm, "route_sub_steps": cfg.route_sub_steps,
-                "chunk_steps": cfg.chunk_steps}
+                "chunk_steps": cfg.chunk_steps, "route_cluster": cfg.route_cluster}
 
     def snapshot_alloc(self, n_slots: int):
         self._check(self.L.mhm_snapshot_alloc(self.ctx, n_slots), "mhm_snapshot_alloc")

@@ -18,8 +18,9 @@
   nodes in 1478 levels, spatially correlated precipitation, L0 = L1/2,
   default parameters) for one 240-step chunk -- the instantiation the bench
   times (PET input with the Feddes stress, lean variant) in all three
-  register variants: gauge discharge, total runoff and every restart state
-  bit for bit against the hmath oracle.
+  register variants, and with the routing wavefront walked by one 16-CTA
+  cluster launch: gauge discharge, total runoff and every restart state bit
+  for bit against the hmath oracle.
 """
 import numpy as np
 import pytest
@@ -143,12 +144,13 @@ def large():
     return dom, l0, gam, off, f, oracle
 
 
-@pytest.mark.parametrize("occ", ["4", "6", "8"])
-def test_large_domain_one_chunk_bitwise(large, occ, monkeypatch):
+@pytest.mark.parametrize("occ,cluster", [("4", "0"), ("6", "0"), ("8", "0"), ("8", "16")])
+def test_large_domain_one_chunk_bitwise(large, occ, cluster, monkeypatch):
     from mhm_gb300.model import MhmGpu
     dom, l0, gam, off, f, oracle = large
     assert dom.n_cells == 1_000_000 and dom.n_nodes == 62_500 and dom.depth_stats()[0] == 1478
     monkeypatch.setenv("MHM_CELL_OCC", occ)
+    monkeypatch.setenv("MHM_ROUTE_CLUSTER", cluster)   # 16: the routing wavefront in one cluster launch
     g = MhmGpu(dom)
     try:
         g.mpr_setup(l0)
@@ -162,7 +164,7 @@ def test_large_domain_one_chunk_bitwise(large, occ, monkeypatch):
         p = g.get_eff_params(0)
     finally:
         g.close()
-    key = "o_" + occ
+    key = f"o_{occ}_c{cluster}"
     if not hasattr(test_large_domain_one_chunk_bitwise, "ref"):
         # the oracle time loop from the device's effective parameters (the
         # regionalisation itself is pinned bit for bit by tests/test_mpr.py)
