@@ -141,18 +141,24 @@ def measured_peaks() -> dict:
     return {}
 
 
-def traffic_from_profiles(name: str):
-    """DRAM bytes per cell-step of the cell-chain kernel from the committed ncu summary."""
+def profile_figure(key: str, name: str = "cell_chain_kernel_H6_hourly.md"):
+    """A per-cell-step figure ("<key>: <value>") of the cell-chain kernel from
+    the committed ncu summary."""
     f = ROOT / "profiles" / name
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.strip().startswith("dram_bytes_per_cell_step:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def traffic_from_profiles(name: str):
+    """DRAM bytes per cell-step of the cell-chain kernel from the committed ncu summary."""
+    return profile_figure("dram_bytes_per_cell_step", name)
 
 
 def build_workload(cfg_name: str, order=None):
@@ -315,6 +321,18 @@ def run_gpu(args) -> dict:
         flops = ops * N * chunk / per_launch_s
         fp64_line.update({"achieved": flops / 1e12, "frac": flops / fp64_peak, "flop_per_cell_step": ops,
                           "kernel": "cell_chain_kernel<6>"})
+    # the roof that binds the kernel: warp instructions issued (4 schedulers per SM,
+    # one instruction each per cycle) at the SM clock sampled under load
+    wi = profile_figure("warp_inst_per_cell_step")
+    n_sm = torch.cuda.get_device_properties(device).multi_processor_count
+    sm_mhz = clk.summary().get("sm_mhz") or None
+    issue_line = None
+    if wi and sm_mhz:
+        ach = wi * N * chunk / per_launch_s
+        peak = 4.0 * n_sm * sm_mhz * 1e6
+        issue_line = {"achieved": ach, "peak": peak, "unit": "warp-inst/s", "frac": ach / peak,
+                      "warp_inst_per_cell_step": wi, "kernel": "cell_chain_kernel<6>",
+                      "peak_source": f"{n_sm} SMs x 4 issue slots x sampled SM clock {sm_mhz:.0f} MHz"}
     cfg = workload_config(args.config, dom, chunk)
     if world > 1:
         cfg["parallelism"] = f"replicas x{world}"
@@ -335,6 +353,7 @@ def run_gpu(args) -> dict:
                      if peaks else "of fallback",
                      "binding_roof": "fp64+integer issue (roofline_fp64); HBM is not the limit"},
         "roofline_fp64": fp64_line,
+        "roofline_issue": issue_line,
         "kernel_time_ms": {"cell_chain": t_cell, "runoff_acc": t_acc, "routing": t_rt,
                            "timed_region": ms},
         "clocks": clk.summary(),
@@ -529,16 +548,7 @@ def run_uneven(args) -> dict:
 
 
 def traffic_from_profiles_ops():
-    f = ROOT / "profiles" / "cell_chain_kernel_H6_hourly.md"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        if line.strip().startswith("fp64_flop_per_cell_step:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+    return profile_figure("fp64_flop_per_cell_step")
 
 
 class OracleArm:
