@@ -40,9 +40,11 @@ def test_oracle_add_inflow_in_list_order(ora_hmath):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cluster", ["0", "8"])   # per-tick graph, cluster walk
 @pytest.mark.parametrize("proc_rout,cellsize,l11", [(1, 1000.0, 2), (2, 250.0, 2), (2, 3000.0, 4)])
-def test_gpu_inflow_gauges_bitwise(proc_rout, cellsize, l11):
+def test_gpu_inflow_gauges_bitwise(proc_rout, cellsize, l11, cluster, monkeypatch):
     from mhm_gb300.model import MhmGpu
+    monkeypatch.setenv("MHM_ROUTE_CLUSTER", cluster)
     from oracle import oracle
     dom = synth.make_domain(12, 10, 3, l11_factor=l11, seed=1, cellsize_m=cellsize)
     p = synth.make_eff_params(dom, seed=3)

@@ -35,8 +35,10 @@ def test_oracle_routing_step_choice(cellsize, l11_factor, ts_expect):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cluster", ["0", "16"])   # per-tick graph, cluster walk
 @pytest.mark.parametrize("cellsize,l11_factor", [(250.0, 2), (3000.0, 4)])
-def test_gpu_routing_case2_bitwise(cellsize, l11_factor):
+def test_gpu_routing_case2_bitwise(cellsize, l11_factor, cluster, monkeypatch):
+    monkeypatch.setenv("MHM_ROUTE_CLUSTER", cluster)
     from mhm_gb300.model import MhmGpu
     dom = _domain(cellsize, l11_factor)
     p = synth.make_eff_params(dom, seed=3)
