@@ -657,7 +657,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the kernel variant of MHM_CELL_OCC / MHM_ROUTE_SUB (for profiling)")
     ap.add_argument("--serve", action="store_true", help="measure the serving loop instead (p50/p99 latency)")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50.0, 100.0])
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-basins", type=int, default=12)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement of the default run")
