@@ -43,6 +43,7 @@ extern "C" {
 #define MHM_ERR_TIMEOUT (-4)     /* a bounded device wait ran out */
 #define MHM_ERR_NAN (-5)         /* non-finite state or forcing detected */
 #define MHM_ERR_UNSUPPORTED (-6) /* process option not implemented */
+#define MHM_ERR_BOUNDS (-7)      /* bounds-checked build: an index taken from data was out of range */
 
 /* forcing kinds for mhm_set_forcing (the reference's L1_pre, L1_temp, L1_pet,
  * L1_tmin, L1_tmax of src/meteo/mo_meteo_handler.f90) */
@@ -297,6 +298,28 @@ int mhm_autotune_route(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, int32_t *clus
  * or one bad request of a serving loop can be failed on its own while the
  * others continue. */
 int mhm_member_status(mhm_ctx *ctx, int32_t *status);
+
+/* Bounds-checked build (the library built with -DMHM_BOUNDS_CHECK, loaded as
+ * libmhm_gpu_bc.so): every index a kernel takes from data -- forcing rows,
+ * the member step table, network tables, L1 <-> L11 mappings, gauge and
+ * inflow positions, inflow days, soil keys, LAI classes and geology units of
+ * the L0 codes -- is tested before the access; a failed test records (site,
+ * index) in a device status word (the first one wins) and skips the access,
+ * never trapping.  The status words belong to the device: the next
+ * mhm_sync or mhm_device_status on that device reports MHM_ERR_BOUNDS.
+ * mhm_bounds_checked() is 1 in that build, 0 otherwise.  mhm_device_status
+ * waits for the context's work and returns MHM_OK or MHM_ERR_BOUNDS with
+ * the site (1 forcing row, 2 member step row, 3 L1 cell of a node, 4 L1 cell
+ * of an L11 cell, 5 upstream position, 6 qOUT row, 7 gauge position,
+ * 8 inflow gauge position, 9 inflow day, 10 soil key, 11 LAI class,
+ * 12 geology unit, 99 self-test) and index; both may be NULL.
+ * mhm_bounds_selftest runs one failing test with no access behind it (site
+ * 99, index 7) so a caller can check the reporting path; MHM_ERR_UNSUPPORTED
+ * in other builds.  (No reference counterpart: the reference's debug builds
+ * use the Fortran compilers' run-time checks, src/CMakeLists.txt:71.) */
+int mhm_bounds_checked(void);
+int mhm_device_status(mhm_ctx *ctx, int32_t *site, int64_t *index);
+int mhm_bounds_selftest(mhm_ctx *ctx);
 
 /* Batches of contexts (no counterpart in the reference, whose farm of
  * parameter sets and domains runs them one after another or on separate MPI

@@ -18,6 +18,7 @@ MHM_ERR_OOM = -3
 MHM_ERR_TIMEOUT = -4
 MHM_ERR_NAN = -5
 MHM_ERR_UNSUPPORTED = -6
+MHM_ERR_BOUNDS = -7
 
 FORC_PRE, FORC_TEMP, FORC_PET, FORC_TMIN, FORC_TMAX, FORC_NETRAD, FORC_EABS, FORC_WINDSPEED = range(8)
 
@@ -123,13 +124,19 @@ EXPORTS = [
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
     "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping", "mhm_autotune_route",
+    "mhm_bounds_checked", "mhm_device_status", "mhm_bounds_selftest",
 ]
 
 _LIB = None
 
 
+def bounds_checked_requested() -> bool:
+    """MHM_BOUNDS_CHECK=1 selects the bounds-checked build (libmhm_gpu_bc.so)."""
+    return os.environ.get("MHM_BOUNDS_CHECK", "0") not in ("", "0")
+
+
 def lib_path() -> Path:
-    return _build.LIB
+    return _build.LIB_BC if bounds_checked_requested() else _build.LIB
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -138,8 +145,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     if _LIB is not None:
         return _LIB
     path = lib_path()
-    if build_if_missing and (not path.exists() or _build._stale()):
-        _build.build()
+    if build_if_missing and (not path.exists() or _build._stale(path)):
+        _build.build(bounds_check=bounds_checked_requested())
     if not path.exists():
         raise RuntimeError(f"libmhm_gpu.so not found at {path}: run mhm_gb300.build.build()")
     L = C.CDLL(str(path), mode=os.RTLD_NOW | getattr(os, "RTLD_GLOBAL", 0))
@@ -206,6 +213,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_get_launch_config.argtypes = [vp, C.POINTER(LaunchConfig)]
     L.mhm_autotune_ex.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _ip, C.POINTER(LaunchConfig), _dp]
     L.mhm_autotune_route.argtypes = [vp, C.c_int32, C.c_int32, _ip, _dp]
+    L.mhm_bounds_checked.argtypes = []
+    L.mhm_device_status.argtypes = [vp, _ip, C.POINTER(C.c_int64)]
+    L.mhm_bounds_selftest.argtypes = [vp]
     L.mhm_batch_create.argtypes = [C.c_int32, C.POINTER(vp)]
     L.mhm_batch_destroy.argtypes = [vp]
     L.mhm_batch_last_error.argtypes = [vp]

@@ -21,6 +21,9 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = BUILD / "libmhm_gpu.so"
+# the bounds-checked variant (-DMHM_BOUNDS_CHECK): index tests before every
+# data-derived access, failures reported through a device status word
+LIB_BC = BUILD / "libmhm_gpu_bc.so"
 
 SOURCES = ["cell_chain.cu", "cell_chain_o6.cu", "cell_chain_o8.cu", "routing.cu", "probes.cu", "mpr.cu", "engine.cu",
            "network.cpp", "netbuild.cpp", "mpr_host.cpp"]
@@ -46,25 +49,28 @@ def _flags(verbose_ptxas: bool) -> list[str]:
     return f + extra
 
 
-def _stale() -> bool:
-    if not LIB.exists():
+def _stale(lib: Path = LIB) -> bool:
+    if not lib.exists():
         return True
-    t = LIB.stat().st_mtime
+    t = lib.stat().st_mtime
     deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + \
         list(CSRC.glob("*.cpp")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps)
 
 
-def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True) -> Path:
-    """Compile every translation unit for sm_103a and link libmhm_gpu.so."""
-    if not force and not _stale():
-        return LIB
-    BUILD.mkdir(parents=True, exist_ok=True)
+def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True, bounds_check: bool = False) -> Path:
+    """Compile every translation unit for sm_103a and link libmhm_gpu.so
+    (with bounds_check: libmhm_gpu_bc.so, objects under _build/bc/)."""
+    lib = LIB_BC if bounds_check else LIB
+    if not force and not _stale(lib):
+        return lib
+    odir = BUILD / "bc" if bounds_check else BUILD
+    odir.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
-    flags = _flags(verbose_ptxas)
+    flags = _flags(verbose_ptxas) + (["-DMHM_BOUNDS_CHECK"] if bounds_check else [])
 
     def compile_one(src: str) -> tuple[str, str]:
-        obj = BUILD / (Path(src).stem + ".o")
+        obj = odir / (Path(src).stem + ".o")
         cmd = [cc, *flags, "-c", str(CSRC / src), "-o", str(obj)]
         if src.endswith(".cpp"):
             cmd = [cc, "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
@@ -80,15 +86,15 @@ def build(force: bool = False, verbose_ptxas: bool = False, quiet: bool = True) 
         for _, log in results:
             if log.strip():
                 print(log, file=sys.stderr)
-    tmp = BUILD / "libmhm_gpu.so.tmp"
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *[o for o, _ in results]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, quiet=False)
-    print(LIB)
+    bc = "--bounds-check" in sys.argv
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, quiet=False, bounds_check=bc))

@@ -78,3 +78,5 @@ cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s)
 }
 
 } // namespace mhm
+
+MHM_BC_ACCESSOR(bc_take_cell_chain)

@@ -17,6 +17,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "bounds.cuh"
 #include "calendar.h"
 #include "fp64i.h"
 #include "hmath.h"
@@ -145,6 +146,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
             for (int t = 0; t < a.n_steps; ++t) a.tro[(size_t)t * a.n_members * N + (size_t)m * N + k] = 0.0;
             return;
         }
+        if (!bc_ok(BC_STEP_ROW, (long long)b + a.step_shift + a.n_steps - 1, a.n_step_rows)) return;
         steps += b + a.step_shift;
         reset_sm = a.reset_ok && (b + a.step_shift == 0);
     }
@@ -249,6 +251,9 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
             if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = par(P_PETLAI + month - 1);
             if (!LEAN && a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
         }
+        if (kBoundsChecked && !bc_ok(BC_FORCING_ROW, a.member_step0 ? a.step_shift + t : si.row - a.row_base,
+                                     a.n_forc_rows))
+            break;
         const size_t f = (size_t)(a.member_step0 ? a.step_shift + t : si.row - a.row_base) * N + k;
         // output weights: write_output runs after the calendar has advanced, so
         // it reads fSealed / soilMoistSat of the NEXT step's land-cover scene

@@ -11,3 +11,5 @@ cudaError_t launch_cell_chain_o8(const CellArgs &a, int H, cudaStream_t s)
 }
 
 } // namespace mhm
+
+MHM_BC_ACCESSOR(bc_take_cell_chain_o8)

@@ -19,6 +19,7 @@
 #include "hmath.h"
 #include "mhm_gpu.h"
 #include "mhm_kernels.cuh"
+#include "bounds.cuh"
 #include "calendar.h"
 #include "mpr_host.h"
 #include "network.h"
@@ -41,6 +42,13 @@ cudaError_t launch_fp64_probe(int64_t iters, int blocks, int threads, double *si
 cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s);
 cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s);
 cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, int occ, cudaStream_t s);
+cudaError_t launch_bc_selftest(cudaStream_t s);
+// the bounds-checked build's status words, one per translation unit with checked kernels
+cudaError_t bc_take_cell_chain(unsigned long long *out);
+cudaError_t bc_take_cell_chain_o6(unsigned long long *out);
+cudaError_t bc_take_cell_chain_o8(unsigned long long *out);
+cudaError_t bc_take_routing(unsigned long long *out);
+cudaError_t bc_take_mpr(unsigned long long *out);
 } // namespace mhm
 
 using namespace mhm;
@@ -1303,12 +1311,17 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         const double *fp[kForcKinds] = {};
         if (on_device) {
             a.row_base = row0_all;
+            a.n_forc_rows = INT32_MAX;
             for (int k = 0; k < kForcKinds; ++k)
-                if (need[k]) fp[k] = ctx->forc[k].ptr;
+                if (need[k]) {
+                    fp[k] = ctx->forc[k].ptr;
+                    a.n_forc_rows = std::min(a.n_forc_rows, ctx->forc[k].n_rows);
+                }
         } else {
             int32_t r0, r1;
             chunk_rows(c, r0, r1);
             a.row_base = r0;
+            a.n_forc_rows = r1 - r0 + 1;
             for (int k = 0; k < kForcKinds; ++k)
                 if (need[k]) fp[k] = ctx->stage[k][slot].p;
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[slot], 0), "wait copied");
@@ -1330,6 +1343,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.steps = ctx->steps.p;
         if (members) {
             a.steps = ctx->steps_all.p;
+            a.n_step_rows = (int32_t)std::min<int64_t>(ctx->steps_all_filled, INT32_MAX);
             a.member_step0 = ctx->member_s0_cur;
             a.step_shift = s0;
             a.reset_ok = !ctx->read_states;
@@ -1441,6 +1455,7 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             ia.pos = ctx->inflow_pos_d.p;
             ia.headwater = ctx->inflow_hw_d.p;
             ia.q = ctx->inflow_q.p;
+            ia.n_days = ctx->inflow_ndays;
             ia.qout = ctx->qout.p;
             CK(launch_inflow(ia, rs), "inflow launch");
             g_launches++;
@@ -1653,6 +1668,54 @@ int mhm_poll(mhm_ctx *ctx, int32_t *done)
     return MHM_OK;
 }
 
+// The bounds-checked build's verdict on the work that has completed on the
+// context's device: MHM_OK, or MHM_ERR_BOUNDS with the site and index of the
+// first failed index test (status words read and cleared).
+static int take_bounds_status(mhm_ctx *ctx, int32_t *site, int64_t *index)
+{
+    if (site) *site = 0;
+    if (index) *index = 0;
+    if (!kBoundsChecked) return MHM_OK;
+    cudaError_t (*const readers[])(unsigned long long *) = {bc_take_cell_chain, bc_take_cell_chain_o6,
+                                                            bc_take_cell_chain_o8, bc_take_routing, bc_take_mpr};
+    unsigned long long first = 0;
+    for (auto rd : readers) {
+        unsigned long long v = 0;
+        CK(rd(&v), "bounds status");
+        if (v && !first) first = v;
+    }
+    if (!first) return MHM_OK;
+    const int32_t st = (int32_t)(first >> 48);
+    const int64_t ix = (int64_t)(first & 0xffffffffffffULL);
+    if (site) *site = st;
+    if (index) *index = ix;
+    return fail(ctx, MHM_ERR_BOUNDS,
+                "index out of range at check site " + std::to_string(st) + " (index " + std::to_string(ix) + ")");
+}
+
+int mhm_bounds_checked(void) { return kBoundsChecked ? 1 : 0; }
+
+int mhm_device_status(mhm_ctx *ctx, int32_t *site, int64_t *index)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    ON_CTX_DEVICE(ctx);
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    CK(cudaStreamSynchronize(ctx->route_stream), "sync");
+    CK(cudaStreamSynchronize(ctx->copy_stream), "sync");
+    return take_bounds_status(ctx, site, index);
+}
+
+int mhm_bounds_selftest(mhm_ctx *ctx)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (!kBoundsChecked) return fail(ctx, MHM_ERR_UNSUPPORTED, "not a bounds-checked build");
+    ON_CTX_DEVICE(ctx);
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    CK(launch_bc_selftest(ctx->stream), "self-test launch");
+    CK(cudaStreamSynchronize(ctx->stream), "sync");
+    return MHM_OK;
+}
+
 int mhm_sync(mhm_ctx *ctx)
 {
     NvtxRange nvtx_("mhm: sync");
@@ -1673,6 +1736,7 @@ int mhm_sync(mhm_ctx *ctx)
     for (auto &st : ctx->qg_stage)
         if (int rc = finish_gauge_stage(ctx, st)) return rc;
     harvest_timing(ctx);
+    if (int rc = take_bounds_status(ctx, nullptr, nullptr)) return rc;
     if (ctx->pending_outputs && ctx->out_qmod) { // routing-level positions -> node order
         const size_t L = ctx->L;
         std::vector<double> row(L);

@@ -131,6 +131,10 @@ struct CellArgs {
     // step or a state at the chunk's end is not finite (nullptr = not checked)
     int32_t *nonfinite;
     int32_t n_horizons; // the context's horizon count (read by the fused multi-context launch)
+    // extents the bounds-checked build tests its data-derived indexes against:
+    // forcing rows from row_base (or window rows in member mode) and, in member
+    // mode, the rows of the member step table
+    int32_t n_forc_rows, n_step_rows;
 };
 
 // One persistent launch of the cell chain over several contexts (with the
@@ -210,6 +214,7 @@ struct InflowArgs {
     const int32_t *pos;          // [n_inflow] routing position of each gauge's node
     const int8_t *headwater;     // [n_inflow]
     const double *q;             // [days][n_inflow] from day0
+    int32_t n_days;              // rows of q
     double *qout;                // [M][n_qsteps][n_nodes]
 };
 

@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "hmath.h"
+#include "bounds.cuh"
 #include "mhm_kernels.cuh"
 #include "mpr_host.h"
 
@@ -232,7 +233,9 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
     for (int h = 0; h < H; ++h) {
         double s_sms = 0.0, s_beta = 0.0, s_pw = 0.0, s_fc = 0.0, s_fr = 0.0;
         for (int j = 0; j < ns; ++j) {
-            const double *row = tab + (size_t)(__ldg(code + (size_t)j * N) & kMprKeyMask) * ts;
+            const uint32_t key = __ldg(code + (size_t)j * N) & kMprKeyMask;
+            if (!bc_ok(BC_MPR_KEY, key, a.n_keys)) continue;
+            const double *row = tab + (size_t)key * ts;
             s_sms = s_sms + __ldg(row + MT_INV_SMS * H + h);
             s_beta = s_beta + __ldg(row + MT_INV_BETA * H + h);
             s_pw = s_pw + __ldg(row + MT_INV_PW * H + h);
@@ -268,6 +271,9 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
     double s_hl1 = 0.0, s_k0 = 0.0, s_k1 = 0.0, s_alpha = 0.0, s_kp = 0.0, s_k2 = 0.0, s_asp = 0.0;
     for (int j = 0; j < ns; ++j) {
         const uint32_t c = __ldg(code + (size_t)j * N);
+        if (!bc_ok(BC_MPR_KEY, c & kMprKeyMask, a.n_keys) ||
+            !bc_ok(BC_MPR_GEO, (long long)(c >> 24), (long long)a.n_gamma - a.off.geo))
+            continue;
         const double *row = tab + (size_t)(c & kMprKeyMask) * ts;
         const double sej = __ldg(se + (size_t)j * N);
         s_hl1 = s_hl1 + __ldg(row + 5 * H + 0);
@@ -326,6 +332,7 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
         double s_int = 0.0, s_pet = 0.0, s_pt = 0.0, s_ra = 0.0, s_rs = 0.0;
         for (int j = 0; j < ns; ++j) {
             const uint32_t c = __ldg(code + (size_t)j * N);
+            if (!a.lai && !bc_ok(BC_MPR_LAI, (c >> 16) & 0xFFu, a.n_lai_classes)) continue;
             double lai;
             if (a.lai) {
                 lai = __ldg(a.lai + mo * slots + (size_t)j * N + k);
@@ -392,3 +399,5 @@ cudaError_t launch_mpr(const MprArgs &a, cudaStream_t s)
 }
 
 } // namespace mhm
+
+MHM_BC_ACCESSOR(bc_take_mpr)

@@ -12,6 +12,7 @@
 #include <atomic>
 #include <cstdint>
 
+#include "bounds.cuh"
 #include "calendar.h"
 #include "mhm_kernels.cuh"
 
@@ -48,11 +49,13 @@ __global__ void __launch_bounds__(256) runoff_acc_kernel(const AccArgs a)
         const int b = __ldg(a.node_cell_ptr + pos), e = __ldg(a.node_cell_ptr + pos + 1);
         for (int j = b; j < e; ++j) {
             const int k = __ldg(a.node_cells + j);
+            if (!bc_ok(BC_ACC_CELL, k, a.n_cells)) continue;
             acc = acc + run(k) * __ldg(a.l1_area + k);
         }
         q = acc * 1000.0 / a.TST;
     } else {
-        q = run(__ldg(a.pos_l11_l1 + pos)) * __ldg(a.pos_area + pos) * 1000.0 / a.TST;
+        const int k = __ldg(a.pos_l11_l1 + pos);
+        q = bc_ok(BC_ACC_L1, k, a.n_cells) ? run(k) * __ldg(a.pos_area + pos) * 1000.0 / a.TST : 0.0;
     }
     a.qout[((size_t)m * a.n_steps + t) * L + pos] = q;
 }
@@ -93,12 +96,14 @@ __device__ __forceinline__ void route_item(const RouteArgs &a, const int m, cons
 #pragma unroll
     for (int t = 0; t < SUB; ++t) qtin[t] = 0.0; // netNode_qTIN(:, IT) = 0
     for (int j = ub; j < ue; ++j) {
-        const double *up = a.qtr + base + __ldg(a.up_pos + j);
+        const int up_pos = __ldg(a.up_pos + j);
+        if (!bc_ok(BC_ROUTE_UP, up_pos, L)) continue;
+        const double *up = a.qtr + base + up_pos;
 #pragma unroll
         for (int t = 0; t < SUB; ++t)
             if (t < nt) qtin[t] = qtin[t] + __ldcg(up + (size_t)t * L);
     }
-    if (add_qout) {
+    if (add_qout && bc_ok(BC_ROUTE_QOUT, (t0 + nt - 1) / a.rdiv, a.n_qsteps)) {
         const double *qo = a.qout + (size_t)m * a.n_qsteps * L + pos;
 #pragma unroll
         for (int t = 0; t < SUB; ++t)
@@ -212,6 +217,10 @@ __global__ void inflow_kernel(const InflowArgs a)
     }
     tt0 += (int64_t)s * a.win; // first model step of routing step s
     double *row = a.qout + ((size_t)m * a.n_qsteps + s) * a.n_nodes;
+    // the days of this routing step (the host checks that the series covers the run)
+    const int64_t d_first = (tt0 + a.steps_day - 1) / a.steps_day - a.day0;
+    const int64_t d_last = (tt0 + (a.mean ? a.win - 1 : 0) + a.steps_day - 1) / a.steps_day - a.day0;
+    if (!bc_ok(BC_INFLOW_DAY, d_first, a.n_days) || !bc_ok(BC_INFLOW_DAY, d_last, a.n_days)) return;
     for (int g = 0; g < a.n_inflow; ++g) {
         double Q;
         if (a.mean) {
@@ -225,9 +234,21 @@ __global__ void inflow_kernel(const InflowArgs a)
             const int64_t day = (tt0 + a.steps_day - 1) / a.steps_day;
             Q = __ldg(a.q + (size_t)(day - a.day0) * a.n_inflow + g);
         }
-        double *v = row + __ldg(a.pos + g);
+        const int p = __ldg(a.pos + g);
+        if (!bc_ok(BC_INFLOW_POS, p, a.n_nodes)) continue;
+        double *v = row + p;
         *v = a.headwater[g] ? *v + Q : Q;
     }
+}
+
+// mhm_bounds_selftest: one failing test (index == extent) with no access
+// behind it, so that the status path can be checked without any bad access
+__global__ void bc_selftest_kernel(int n) { bc_ok(BC_SELFTEST, n, n); }
+
+cudaError_t launch_bc_selftest(cudaStream_t s)
+{
+    bc_selftest_kernel<<<1, 1, 0, s>>>(7);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_inflow(const InflowArgs &a, cudaStream_t s)
@@ -304,9 +325,10 @@ __global__ void gauge_gather_kernel(const GaugeArgs a)
     const int64_t mg = gid / a.n_steps;
     const int g = (int)(mg % a.n_gauges);
     const int m = (int)(mg / a.n_gauges);
-    const double v = (a.member_step0 && a.member_step0[m] < 0)
+    const int gp = __ldg(a.gauge_pos + g);
+    const double v = (a.member_step0 && a.member_step0[m] < 0) || !bc_ok(BC_GAUGE_POS, gp, a.n_nodes)
                          ? 0.0
-                         : a.qmod[((size_t)m * a.n_steps + t) * a.n_nodes + __ldg(a.gauge_pos + g)];
+                         : a.qmod[((size_t)m * a.n_steps + t) * a.n_nodes + gp];
     a.q_gauge[((size_t)m * a.n_gauges + g) * a.total_steps + a.step_offset + t] = v;
 }
 
@@ -442,3 +464,5 @@ cudaError_t launch_reg_rout(int n_links, const double *p5, double ss_max, double
 }
 
 } // namespace mhm
+
+MHM_BC_ACCESSOR(bc_take_routing)

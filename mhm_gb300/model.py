@@ -429,6 +429,20 @@ class MhmGpu:
     def sync(self):
         self._check(self.L.mhm_sync(self.ctx), "mhm_sync")
 
+    def device_status(self):
+        """None, or (site, index) of the first failed index test of the
+        bounds-checked build (mhm_device_status; clears it)."""
+        site = C.c_int32()
+        idx = C.c_int64()
+        rc = self.L.mhm_device_status(self.ctx, C.byref(site), C.byref(idx))
+        if rc == _lib.MHM_ERR_BOUNDS:
+            return int(site.value), int(idx.value)
+        self._check(rc, "mhm_device_status")
+        return None
+
+    def bounds_selftest(self):
+        self._check(self.L.mhm_bounds_selftest(self.ctx), "mhm_bounds_selftest")
+
     def poll(self) -> bool:
         """True if all enqueued work has completed (sync() then returns at once)."""
         d = C.c_int32()
