@@ -141,6 +141,29 @@ def measured_peaks() -> dict:
     return {}
 
 
+def run_manifest(device, lib) -> dict:
+    """What the numbers were measured on: the GPU, its driver, the CUDA and
+    PyTorch runtimes, the library variant loaded and the host."""
+    import platform
+    import subprocess
+
+    import torch
+    props = torch.cuda.get_device_properties(device)
+    driver = None
+    try:
+        r = subprocess.run(["nvidia-smi", "-i", str(device.index or 0), "--query-gpu=driver_version",
+                            "--format=csv,noheader"], capture_output=True, text=True, timeout=20)
+        driver = r.stdout.strip() or None
+    except (OSError, subprocess.SubprocessError):
+        pass
+    from mhm_gb300 import _lib
+    return {"gpu": props.name, "sm_count": props.multi_processor_count, "compute_capability": f"{props.major}.{props.minor}",
+            "hbm_gib": round(props.total_memory / 2**30, 1), "driver": driver, "cuda_runtime": torch.version.cuda,
+            "torch": torch.__version__, "library": _lib.lib_path().name,
+            "bounds_checked": bool(lib.mhm_bounds_checked()), "host": platform.machine(),
+            "python": platform.python_version()}
+
+
 def profile_figure(key: str, name: str = "cell_chain_kernel_H6_hourly.md"):
     """A per-cell-step figure ("<key>: <value>") of the cell-chain kernel from
     the committed ncu summary."""
@@ -358,6 +381,7 @@ def run_gpu(args) -> dict:
                            "timed_region": ms},
         "clocks": clk.summary(),
         "autotune": tune,
+        "manifest": run_manifest(device, lib),
     }
     g.close()
     del pre, temp, pet

@@ -143,6 +143,11 @@ class Server:
         self.autotune = autotune
         self.tuned: dict[str, dict] = {}
         self.failed: list[Request] = []      # failed, rejected or cancelled
+        # admission statistics: contexts opened and retired to make room,
+        # admissions deferred by the HBM budget, peak device footprint and
+        # peak number of running requests
+        self.stats = {"contexts_opened": 0, "contexts_retired_for_room": 0, "budget_deferrals": 0,
+                      "peak_hbm_bytes": 0, "peak_running": 0}
         self._cancel: set[int] = set()       # request ids to cancel (filled from any thread)
         self.pool = ThreadPoolExecutor(max_workers=workers)
         for b in basins:
@@ -195,6 +200,8 @@ class Server:
         self.ctx[bi] = {"g": g, "bi": bi, "slots": [None] * members, "tt0": np.zeros(members, np.int32), "bytes": need,
                         "q": np.zeros((members, len(b.dom.gauge_node), self.chunk)), "busy": False}
         self.used += need
+        self.stats["contexts_opened"] += 1
+        self.stats["peak_hbm_bytes"] = max(self.stats["peak_hbm_bytes"], self.used)
         return True
 
     def _close(self, bi: int):
@@ -287,7 +294,9 @@ class Server:
                     # make room: retire contexts without active slots
                     for bi in [k for k, v in self.ctx.items() if all(s is None for s in v["slots"])]:
                         self._close(bi)
+                        self.stats["contexts_retired_for_room"] += 1
                     if not self._open(r.basin, want):
+                        self.stats["budget_deferrals"] += 1
                         still.append(r)
                         continue
                 c = self.ctx[r.basin]
@@ -308,6 +317,8 @@ class Server:
             r.admitted = now
             r.status = "running"
         self.waiting = still
+        running = sum(1 for c in self.ctx.values() for sl in c["slots"] if sl is not None)
+        self.stats["peak_running"] = max(self.stats["peak_running"], running)
 
     def step(self, now: float) -> bool:
         """One pass of the loop; returns False when there is nothing to do.
@@ -397,6 +408,11 @@ class Server:
                 self.failed.append(r)
         out = summarize(self.finished, wall, self.cell_steps)
         out["failed"] = len(self.failed)
+        waits = np.array([r.admitted - r.arrival for r in self.finished if r.admitted is not None])
+        out["admission"] = dict(self.stats, queue_wait_p50_s=float(np.percentile(waits, 50)) if waits.size else None,
+                                queue_wait_p99_s=float(np.percentile(waits, 99)) if waits.size else None,
+                                rejected=sum(1 for r in self.failed if r.status == "rejected"),
+                                cancelled=sum(1 for r in self.failed if r.status == "cancelled"))
         return out
 
     def close(self):

@@ -175,6 +175,32 @@ def test_over_budget_basin_is_rejected_and_others_run():
         srv.close()
     assert reqs[0].status == "done" and res["requests"] == 1
     assert reqs[1].status == "rejected" and "budget" in reqs[1].error
+    adm = res["admission"]
+    assert adm["rejected"] == 1 and adm["contexts_opened"] == 1 and adm["peak_running"] == 1
+    assert 0 < adm["peak_hbm_bytes"] <= small_budget and adm["queue_wait_p50_s"] >= 0.0
+
+
+def test_budget_defers_admission_until_a_context_retires():
+    """Two basins that fit the budget only one at a time: the second request
+    waits (a budget deferral) until the first basin's context is idle and is
+    retired to make room, then runs; both give their stand-alone results."""
+    basins = _basins()
+    b0, b1 = (serve.context_bytes(basins[i], 1, CHUNK) for i in (0, 1))
+    srv = _server(basins, budget=max(b0, b1) * 1.01)
+    gam = params.random_gammas(2, 1, 0, 1, basins[0].l0.n_geo, seed=8)
+    reqs = [serve.Request(rid=0, basin=0, gamma=gam[0], horizon=2 * CHUNK),
+            serve.Request(rid=1, basin=1, gamma=gam[1], horizon=CHUNK)]
+    try:
+        res = srv.serve(reqs, timeout_s=60)
+    finally:
+        srv.close()
+    assert [r.status for r in reqs] == ["done", "done"]
+    adm = res["admission"]
+    assert adm["budget_deferrals"] >= 1 and adm["contexts_retired_for_room"] >= 1
+    assert adm["contexts_opened"] == 2 and adm["peak_hbm_bytes"] <= max(b0, b1) * 1.01
+    for r in reqs:
+        alone = serve.run_alone(basins[r.basin], r, CHUNK, g=FakeCtx(basins[r.basin].dom))
+        assert np.array_equal(r.discharge(), alone)
 
 
 def test_cancel_while_waiting():
