@@ -146,6 +146,19 @@ int mhm_set_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
  * the reference's L1_* arrays. */
 int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
 
+/* Gridded LAI series (timeStep_LAI_input, src/common/mo_common_datetime_type.f90:
+ * 138-155): mode 0 (or 1) keeps the 12 monthly LAI slots of the effective
+ * parameters (iLAI = month); -1 / -2 / -3 read the LAI-indexed parameters --
+ * maxInter, the petLAIcorFactor / PrieTayAlpha / aeroResist group and
+ * surfResist -- from a series of n_lai entries, iLAI counting the days /
+ * months / years from the run's first step (tt = 1 is entry 1).  The series
+ * starts zeroed; mhm_set_lai_params fills a member's entries, each array
+ * [n_lai][n_cells] or NULL (zeros).  A run whose last step lies beyond the
+ * series fails with MHM_ERR_INVALID. */
+int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai);
+int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, const double *pet_lai,
+                       const double *surf_resist);
+
 /* Floodplain impervious fraction of the links [nLinks] for the land-cover
  * scene that starts (L11_nLinkFracFPimp(:, iLC) of src/mRM/mo_mrm_routing.f90
  * follows the scene of the current year); the next mhm_set_routing_params /
@@ -312,7 +325,7 @@ int mhm_member_status(mhm_ctx *ctx, int32_t *status);
  * the site (1 forcing row, 2 member step row, 3 L1 cell of a node, 4 L1 cell
  * of an L11 cell, 5 upstream position, 6 qOUT row, 7 gauge position,
  * 8 inflow gauge position, 9 inflow day, 10 soil key, 11 LAI class,
- * 12 geology unit, 99 self-test) and index; both may be NULL.
+ * 12 geology unit, 13 gridded-LAI entry, 99 self-test) and index; both may be NULL.
  * mhm_bounds_selftest runs one failing test with no access behind it (site
  * 99, index 7) so a caller can check the reporting path; MHM_ERR_UNSUPPORTED
  * in other builds.  (No reference counterpart: the reference's debug builds
@@ -508,6 +521,10 @@ int mhm_routing_order(int32_t n_nodes, int32_t n_outlets, const int32_t *from_n,
  * mo_common_datetime_type.f90:71-125).  Any output pointer may be NULL. */
 int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t n, int32_t *month,
                       int32_t *hour, int32_t *doy);
+/* iLAI of steps tt0 .. tt0+n-1 for timeStep_LAI_input lai_mode (the month
+ * for 0 / 1; the day / month / year count from the run's first step for
+ * -1 / -2 / -3), as the cell chain reads its LAI-indexed parameters. */
+int mhm_step_lai(int32_t jul_start, int32_t timestep, int32_t lai_mode, int32_t tt0, int32_t n, int32_t *lai);
 
 /* ---- multiscale parameter regionalisation (MPR) ---- */
 

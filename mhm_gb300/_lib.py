@@ -124,7 +124,8 @@ EXPORTS = [
     "mhm_member_status", "mhm_set_launch_config", "mhm_get_launch_config", "mhm_autotune_ex",
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
     "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping", "mhm_autotune_route",
-    "mhm_bounds_checked", "mhm_device_status", "mhm_bounds_selftest",
+    "mhm_bounds_checked", "mhm_device_status", "mhm_bounds_selftest", "mhm_set_lai_series", "mhm_set_lai_params",
+    "mhm_step_lai",
 ]
 
 _LIB = None
@@ -216,6 +217,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_bounds_checked.argtypes = []
     L.mhm_device_status.argtypes = [vp, _ip, C.POINTER(C.c_int64)]
     L.mhm_bounds_selftest.argtypes = [vp]
+    L.mhm_set_lai_series.argtypes = [vp, C.c_int32, C.c_int32]
+    L.mhm_set_lai_params.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
+    L.mhm_step_lai.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip]
     L.mhm_batch_create.argtypes = [C.c_int32, C.POINTER(vp)]
     L.mhm_batch_destroy.argtypes = [vp]
     L.mhm_batch_last_error.argtypes = [vp]

@@ -2,8 +2,9 @@
 //
 // Every index a kernel takes from data rather than from its thread index --
 // forcing rows of the calendar, the member step table, network tables, L1
-// <-> L11 mappings, gauge and inflow positions, inflow days, soil keys, LAI
-// classes and geology units of the L0 codes -- is tested before the access.
+// <-> L11 mappings, gauge and inflow positions, inflow days, entries of a
+// gridded LAI series, soil keys, LAI classes and geology units of the L0
+// codes -- is tested before the access.
 // A failed test records (site, index) in the translation unit's device status
 // word (the first failure wins, atomicCAS) and the access is skipped; nothing
 // traps, so the context stays usable and the host reports the failure
@@ -28,6 +29,7 @@ enum BoundsSite : int {
     BC_MPR_KEY = 10,     // MPR: soil key of an L0 cell
     BC_MPR_LAI = 11,     // MPR: LAI class of an L0 cell
     BC_MPR_GEO = 12,     // MPR: geology unit of an L0 cell
+    BC_LAI_STEP = 13,    // cell chain: entry of a gridded LAI series
     BC_SELFTEST = 99,    // mhm_bounds_selftest
 };
 

@@ -65,4 +65,21 @@ MHM_HD int32_t step_dflags(int32_t jul_start, int32_t timestep, int64_t tt)
     return fl;
 }
 
+// iLAI of step tt (datetimeinfo_update_LAI_timestep,
+// src/common/mo_common_datetime_type.f90:138-155): the month for monthly LAI
+// slots (timeStep_LAI_input 0, 1); for a gridded series (-1 daily, -2
+// monthly, -3 yearly) the count of days / months / years from the run's first
+// step through tt, i.e. the reference's counter raised at every new day /
+// month / year with the first step counting as new.
+MHM_HD int32_t step_lai(int32_t jul_start, int32_t timestep, int64_t tt, int32_t mode)
+{
+    const StepDate sd = step_date(jul_start, timestep, tt);
+    if (mode >= 0) return sd.month;
+    if (mode == -1) return (int32_t)(((tt - 1) * (int64_t)timestep) / 24 + 1);
+    int32_t y0, m0, d0;
+    jdn_to_gregorian(jul_start, &y0, &m0, &d0);
+    if (mode == -2) return (sd.year - y0) * 12 + (sd.month - m0) + 1;
+    return sd.year - y0 + 1;
+}
+
 } // namespace mhm

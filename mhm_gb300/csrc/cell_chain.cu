@@ -10,7 +10,7 @@ cudaError_t launch_cell_chain_o8(const CellArgs &a, int H, cudaStream_t s);
 
 // Calendar of steps tt0 .. tt0+n-1: forcing row, month, day flags, day of year.
 __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
-                                  int32_t stride)
+                                  int32_t stride, int32_t lai_mode)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -22,14 +22,15 @@ __global__ void steps_fill_kernel(StepInfo *steps, int64_t tt0, int32_t n, int32
     si.dflags = (int8_t)step_dflags(jul_start, timestep, tt);
     si.doy = (int16_t)sd.doy;
     si.hour = (int8_t)sd.hour;
+    si.lai = (int16_t)step_lai(jul_start, timestep, tt, lai_mode);
     steps[i] = si;
 }
 
 cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
-                              int32_t stride, cudaStream_t s)
+                              int32_t stride, int32_t lai_mode, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    steps_fill_kernel<<<(n + 255) / 256, 256, 0, s>>>(steps, tt0, n, jul_start, timestep, stride);
+    steps_fill_kernel<<<(n + 255) / 256, 256, 0, s>>>(steps, tt0, n, jul_start, timestep, stride, lai_mode);
     return cudaGetLastError();
 }
 

@@ -207,7 +207,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
     const bool sealed = c.fsealed > 0.0;           // frac_sealed > 0 (parameter only)
     const bool sthresh_pos = c.sthresh > kEps;     // water_thresh_sealed > eps (parameter only)
     const bool dd_thr_ok = !hm_isnan_i(c.dd_thr);  // prec <= NaN is false
-    int cur_month = -1;
+    int cur_key = -1;
     double imax = 0.0, petlai = 0.0, petsurf = 0.0, evap = 0.0;
     uint64_t r_imax = 0, r_evap = 0;
     int cur_doy = -1;
@@ -241,15 +241,28 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
     for (int t = 0; t < a.n_steps; ++t) {
         const StepInfo si = steps[t];
         const int month = si.month;
-        if (month != cur_month) { // iLAI = month (LUT-based LAI)
-            cur_month = month;
-            imax = par(P_MAXINTER + month - 1);
-            r_imax = hm_recip_of(imax);
-            evap = a.tab.evap[month - 1];
+        // the month (evap_coeff) and the LAI entry (iLAI: the month, or the
+        // step's entry of a gridded LAI series) as one key: their parameters
+        // are reloaded together when either changes
+        const int key = ((int)si.lai << 4) | month;
+        if (key != cur_key) {
+            cur_key = key;
+            evap = a.tab.evap[month - 1]; // evap_coeff of the calendar month
             r_evap = hm_recip_of(evap);
-            // petLAIcorFactor (proc_pet -1) or PrieTayAlpha (proc_pet 2) of the LAI month
-            if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = par(P_PETLAI + month - 1);
-            if (!LEAN && a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
+            if (!a.lai_series) { // iLAI = month: the monthly LAI slots
+                imax = par(P_MAXINTER + month - 1);
+                // petLAIcorFactor (proc_pet -1) or PrieTayAlpha (proc_pet 2) of the LAI month
+                if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = par(P_PETLAI + month - 1);
+                if (!LEAN && a.proc_pet == 3) petsurf = par(P_PET2 + month - 1); // surfResist of the LAI month
+            } else {             // a gridded LAI series: its entry iLAI
+                if (!bc_ok(BC_LAI_STEP, si.lai - 1, a.n_lai)) break;
+                const size_t NL = (size_t)a.n_lai * N;
+                const double *ls = a.lai_series + (size_t)m * 3 * NL + (size_t)(si.lai - 1) * N + k;
+                imax = __ldg(ls);
+                if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = __ldg(ls + NL);
+                if (!LEAN && a.proc_pet == 3) petsurf = __ldg(ls + 2 * NL);
+            }
+            r_imax = hm_recip_of(imax);
         }
         if (kBoundsChecked && !bc_ok(BC_FORCING_ROW, a.member_step0 ? a.step_shift + t : si.row - a.row_base,
                                      a.n_forc_rows))

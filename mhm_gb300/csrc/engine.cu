@@ -27,7 +27,7 @@
 namespace mhm {
 cudaError_t launch_cell_chain(const CellArgs &a, int H, int occ, cudaStream_t s);
 cudaError_t launch_steps_fill(StepInfo *steps, int64_t tt0, int32_t n, int32_t jul_start, int32_t timestep,
-                              int32_t stride, cudaStream_t s);
+                              int32_t stride, int32_t lai_mode, cudaStream_t s);
 cudaError_t launch_runoff_acc(const AccArgs &a, cudaStream_t s);
 cudaError_t launch_route_tick(const RouteArgs &a, cudaStream_t s);
 cudaError_t launch_route_walk(const RouteArgs &a, const RouteWalk &w, int cs, cudaStream_t s);
@@ -203,6 +203,10 @@ struct mhm_ctx {
     // the whole wavefront of a chunk in one launch of clusters of that many CTAs
     int32_t route_cluster = 0;
     DevBuf<int32_t> level_ptr_d;
+    // timeStep_LAI_input: 0 monthly LAI slots; -1 / -2 / -3 a gridded LAI series
+    // of n_lai entries, its parameters in lai_series [M][3][n_lai][N]
+    int32_t lai_mode = 0, n_lai = 0;
+    DevBuf<double> lai_series;
     int32_t cell_occ = 4;  // cell-chain register variant: resident blocks per SM (4, 6, 8)
     int32_t chunk_cap = 0; // most time steps per chunk (0: the device-memory budget decides)
     // routing case 2: per-member routing time step [s] and the link lengths
@@ -917,6 +921,52 @@ int mhm_set_inflow_discharge(mhm_ctx *ctx, int32_t day0, int32_t n_days, const d
     return MHM_OK;
 }
 
+int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (mode < -3 || mode > 1) return fail(ctx, MHM_ERR_INVALID, "timeStep_LAI_input must be 1, 0, -1, -2 or -3");
+    if (mode < 0 && (n_lai < 1 || n_lai > INT16_MAX))
+        return fail(ctx, MHM_ERR_INVALID, "a gridded LAI series needs 1 .. 32767 entries");
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc; // no enqueued step may still read the old series
+    if (mode >= 0) {
+        ctx->lai_series.release();
+        ctx->lai_mode = 0;
+        ctx->n_lai = 0;
+    } else {
+        const size_t n = (size_t)ctx->M * 3 * n_lai * ctx->N;
+        ctx->lai_series.release();
+        CK(ctx->lai_series.ensure(n), "LAI series");
+        CK(cudaMemsetAsync(ctx->lai_series.p, 0, n * sizeof(double), ctx->stream), "LAI series");
+        CK(cudaStreamSynchronize(ctx->stream), "LAI series");
+        ctx->lai_mode = mode;
+        ctx->n_lai = n_lai;
+    }
+    ctx->steps_all_filled = 0; // the member step table carries the LAI index
+    return MHM_OK;
+}
+
+int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, const double *pet_lai,
+                       const double *surf_resist)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (ctx->lai_mode >= 0) return fail(ctx, MHM_ERR_INVALID, "no gridded LAI series: mhm_set_lai_series first");
+    if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc;
+    const size_t NL = (size_t)ctx->n_lai * ctx->N;
+    const double *src[3] = {max_inter, pet_lai, surf_resist};
+    for (int g = 0; g < 3; ++g) {
+        double *dst = ctx->lai_series.p + ((size_t)member * 3 + g) * NL;
+        if (src[g])
+            CK(cudaMemcpyAsync(dst, src[g], NL * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "LAI params");
+        else
+            CK(cudaMemsetAsync(dst, 0, NL * sizeof(double), ctx->stream), "LAI params");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "LAI params");
+    return MHM_OK;
+}
+
 int mhm_set_link_fpimp(mhm_ctx *ctx, const double *ffp_imp)
 {
     if (!ctx || !ffp_imp) return MHM_ERR_INVALID;
@@ -1129,6 +1179,17 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
                          (hi + sd - 1) / sd > (int64_t)ctx->inflow_day0 + ctx->inflow_ndays - 1))
             return fail(ctx, MHM_ERR_INVALID, "inflow discharge does not cover the days of the run");
     }
+    if (ctx->lai_mode < 0) {
+        // the run's last step must lie in the gridded LAI series (iLAI grows with tt)
+        int64_t hi = (int64_t)tt0 + n_steps - 1;
+        if (members) {
+            hi = 0;
+            for (size_t m = 0; m < M; ++m)
+                if (member_tt0[m] > 0) hi = std::max<int64_t>(hi, (int64_t)member_tt0[m] + n_steps - 1);
+        }
+        if (hi >= 1 && step_lai(ctx->jul_start, ctx->timestep, hi, ctx->lai_mode) > ctx->n_lai)
+            return fail(ctx, MHM_ERR_INVALID, "the gridded LAI series does not cover the run");
+    }
     // member mode reads the first n_steps rows of the device forcing window
     const int32_t first_row = members ? ctx->forc[0].row0 : (tt0 + stride - 1) / stride;
     const int32_t last_row = members ? ctx->forc[0].row0 + n_steps - 1 : (tt0 + n_steps - 1 + stride - 1) / stride;
@@ -1260,7 +1321,8 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
             const int64_t cap = ((need_steps + 8759) / 8760) * 8760;
             CK(cudaStreamSynchronize(ctx->stream), "sync");
             CK(ctx->steps_all.ensure((size_t)cap), "member steps");
-            CK(launch_steps_fill(ctx->steps_all.p, 1, (int32_t)cap, ctx->jul_start, ctx->timestep, 1, ctx->stream),
+            CK(launch_steps_fill(ctx->steps_all.p, 1, (int32_t)cap, ctx->jul_start, ctx->timestep, 1, ctx->lai_mode,
+                                 ctx->stream),
                "steps fill");
             g_launches++;
             ctx->steps_all_filled = cap;
@@ -1292,7 +1354,8 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         // this chunk's calendar, computed on the device (stream-ordered before the cell chain)
         if (!members) {
             CK(ctx->steps.ensure((size_t)ctx->tc_cap), "steps");
-            CK(launch_steps_fill(ctx->steps.p, tt0 + s0, nT, ctx->jul_start, ctx->timestep, stride, ctx->stream),
+            CK(launch_steps_fill(ctx->steps.p, tt0 + s0, nT, ctx->jul_start, ctx->timestep, stride, ctx->lai_mode,
+                                 ctx->stream),
                "steps fill");
             g_launches++;
         }
@@ -1356,6 +1419,10 @@ static int run_enqueue(mhm_ctx *ctx, int32_t tt0, int32_t n_steps, double *q_gau
         a.tab = ctx->tab;
         a.nonfinite = ctx->nonfinite.p;
         a.n_horizons = H;
+        if (ctx->lai_mode < 0) {
+            a.lai_series = ctx->lai_series.p;
+            a.n_lai = ctx->n_lai;
+        }
         if (ctx->out_flux) {
             a.flux_aet = ctx->flux_d[0].p;
             a.flux_loss = ctx->flux_d[1].p;
@@ -2438,6 +2505,15 @@ int mhm_step_calendar(int32_t jul_start, int32_t timestep, int32_t tt0, int32_t 
         if (hour) hour[i] = sd.hour;
         if (doy) doy[i] = sd.doy;
     }
+    return MHM_OK;
+}
+
+int mhm_step_lai(int32_t jul_start, int32_t timestep, int32_t lai_mode, int32_t tt0, int32_t n, int32_t *lai)
+{
+    if (jul_start < 2299161 || timestep < 1 || 24 % timestep != 0 || tt0 < 1 || n < 0 || lai_mode < -3 ||
+        lai_mode > 1 || (n > 0 && !lai))
+        return MHM_ERR_INVALID;
+    for (int32_t i = 0; i < n; ++i) lai[i] = step_lai(jul_start, timestep, (int64_t)tt0 + i, lai_mode);
     return MHM_OK;
 }
 

@@ -47,6 +47,7 @@ struct StepInfo {
     int8_t dflags;  // SF_ISDAY: 6 < hour <= 18; SF_*_END: the next step starts a new day / month / year
     int16_t doy;
     int8_t hour;    // 0..23, the hour index of the meteo weights
+    int16_t lai;    // iLAI: the month, or the index in a gridded LAI series (1-based)
 };
 
 // Aggregated flux/state outputs (outputFlxState of mhm_outputs.nml), indexes
@@ -135,6 +136,12 @@ struct CellArgs {
     // forcing rows from row_base (or window rows in member mode) and, in member
     // mode, the rows of the member step table
     int32_t n_forc_rows, n_step_rows;
+    // gridded LAI series (timeStep_LAI_input -1 / -2 / -3): the LAI-indexed
+    // parameters as [M][3][n_lai][n_cells] -- maxInter, the petLAIcorFactor /
+    // PrieTayAlpha / aeroResist group, surfResist -- read at step.lai instead
+    // of the monthly planes; nullptr: monthly slots
+    const double *lai_series;
+    int32_t n_lai;
 };
 
 // One persistent launch of the cell chain over several contexts (with the

@@ -160,6 +160,18 @@ class MhmGpu:
         a = np.ascontiguousarray(q, np.float64)
         self._check(self.L.mhm_set_inflow_discharge(self.ctx, day0, a.shape[0], _d(a)), "mhm_set_inflow_discharge")
 
+    def set_lai_series(self, mode: int, n_lai: int = 0):
+        """timeStep_LAI_input: 0 monthly LAI slots (default); -1 / -2 / -3 a
+        gridded LAI series of n_lai daily / monthly / yearly entries
+        (mhm_set_lai_series)."""
+        self._check(self.L.mhm_set_lai_series(self.ctx, int(mode), int(n_lai)), "mhm_set_lai_series")
+
+    def set_lai_params(self, max_inter, pet_lai=None, surf_resist=None, member: int = 0):
+        """The member's LAI-indexed parameters of the series, each [n_lai][n_cells]."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (max_inter, pet_lai, surf_resist)]
+        self._check(self.L.mhm_set_lai_params(self.ctx, member, *[_d(a) if a is not None else None for a in arrs]),
+                    "mhm_set_lai_params")
+
     def set_link_fpimp(self, ffp):
         """Floodplain impervious fraction of the links for a new land-cover scene."""
         a = np.ascontiguousarray(ffp, np.float64)

@@ -511,6 +511,32 @@ void ora_step_calendar_ex(int32_t jul_start, int32_t timestep, int32_t nSteps, i
     }
 }
 
+/* iLAI of steps 1 .. nSteps by datetimeinfo_update_LAI_timestep
+ * (src/common/mo_common_datetime_type.f90:138-155) on the flags of the
+ * increment: month for timeStep_LAI_input 0 / 1, else a counter raised at
+ * every new day (-1), month (-2) or year (-3), all flags true at the first
+ * step (datetimeinfo_init, :88-91). */
+void ora_step_lai(int32_t jul_start, int32_t timestep, int32_t lai_mode, int32_t nSteps, int32_t *lai)
+{
+    int32_t *month = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)(nSteps > 0 ? nSteps : 1));
+    if (!month)
+        return;
+    int32_t *flags = month + (nSteps > 0 ? nSteps : 1);
+    ora_step_calendar_ex(jul_start, timestep, nSteps, month, NULL, NULL, NULL, NULL, flags);
+    int32_t ilai = 0;
+    for (int32_t t = 0; t < nSteps; ++t) {
+        const int32_t fl = t == 0 ? 14 : flags[t - 1];
+        switch (lai_mode) {
+        case -1: ilai += (fl & 2) ? 1 : 0; break;
+        case -2: ilai += (fl & 4) ? 1 : 0; break;
+        case -3: ilai += (fl & 8) ? 1 : 0; break;
+        default: ilai = month[t]; break;
+        }
+        lai[t] = ilai;
+    }
+    free(month);
+}
+
 /* ---- routing ---- */
 
 /* src/mRM/mo_mrm_mpr.f90:61-119 */
@@ -951,13 +977,34 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
     const double nTstepDay_dp = 24.0 / (double)d->timestep;   /* nTstepDay = 24/timestep */
     if (tt0 < 1 || nT < 0 || H < 1 || H > 16)
         return -1;
-    int32_t *cal = (int32_t *)malloc(sizeof(int32_t) * 4 * (size_t)(tt0 + nT));
+    int32_t *cal = (int32_t *)malloc(sizeof(int32_t) * 5 * (size_t)(tt0 + nT));
     if (!cal)
         return -2;
     int32_t *cal_month = cal, *cal_hour = cal + (tt0 + nT), *cal_doy = cal + 2 * (tt0 + nT);
-    int32_t *cal_new = cal + 3 * (tt0 + nT);
+    int32_t *cal_new = cal + 3 * (tt0 + nT), *cal_lai = cal + 4 * (tt0 + nT);
     ora_step_calendar_ex(d->jul_start, d->timestep, tt0 - 1 + nT, cal_month, cal_hour, cal_doy, NULL, NULL,
                          cal_new);
+    /* iLAI of every step from the run's first (datetimeinfo_update_LAI_timestep,
+     * src/common/mo_common_datetime_type.f90:138-155): the month for LAI slots;
+     * for a series a counter raised when the step starts a new day / month /
+     * year, is_new_* being true at the first step (:88-91) */
+    {
+        int32_t ilai = 0;
+        for (int32_t t = 0; t < tt0 - 1 + nT; ++t) {
+            const int32_t fl = t == 0 ? 14 : cal_new[t - 1];
+            switch (d->lai_mode) {
+            case -1: ilai += (fl & 2) ? 1 : 0; break;
+            case -2: ilai += (fl & 4) ? 1 : 0; break;
+            case -3: ilai += (fl & 8) ? 1 : 0; break;
+            default: ilai = cal_month[t]; break;
+            }
+            cal_lai[t] = ilai;
+        }
+        if (d->lai_mode < 0 && (tt0 - 1 + nT) > 0 && cal_lai[tt0 - 2 + nT] > d->n_lai) {
+            free(cal);
+            return -6; /* the LAI series does not cover the run */
+        }
+    }
     double *pet_calc = (double *)malloc(sizeof(double) * (size_t)N);
     double *temp_calc = (double *)malloc(sizeof(double) * (size_t)N);
     double *prec_calc = (double *)malloc(sizeof(double) * (size_t)N);
@@ -1048,7 +1095,7 @@ int ora_run_ex(const ora_domain *d, const ora_params *p, ora_state *s, const ora
         const double *eabs = f->eabs ? f->eabs + (size_t)row * N : NULL;
         const double *wind = f->windspeed ? f->windspeed + (size_t)row * N : NULL;
         const double evap_coeff = d->evap_coeff[month - 1];
-        const int iLAI = month; /* timeStep_LAI_input = 0 (mo_common_datetime_type.f90:135-155) */
+        const int iLAI = cal_lai[tt - 1];
         /* this step's outputs (write_output after do_time_step) */
         const int out_on = out && out->n_planes > 0 && tt > out->warm_steps;
         int out_write = 0, out_slot = 0;

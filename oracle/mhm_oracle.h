@@ -76,6 +76,7 @@ void ora_dec2date(double julian, int32_t *dd, int32_t *mm, int32_t *yy, int32_t 
  * month[tt-1], hour, doy, day, year. */
 void ora_step_calendar(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
                        int32_t *hour, int32_t *doy, int32_t *day, int32_t *year);
+void ora_step_lai(int32_t jul_start, int32_t timestep, int32_t lai_mode, int32_t nSteps, int32_t *lai);
 void ora_step_calendar_ex(int32_t jul_start, int32_t timestep, int32_t nSteps, int32_t *month,
                           int32_t *hour, int32_t *doy, int32_t *day, int32_t *year, int32_t *new_flags);
 
@@ -153,6 +154,12 @@ typedef struct {
     int32_t nInflow, inflow_day0, inflow_ndays, pad2_;
     const int32_t *inflow_node, *inflow_headwater;
     const double *inflow_q;
+    /* timeStep_LAI_input: 0 (or 1) monthly LAI slots indexed by the calendar
+     * month; -1 / -2 / -3 a gridded LAI series, its index raised at every new
+     * day / month / year of the run (the first step counts as new).  n_lai:
+     * the series' length (the LAI-indexed parameters then hold n_lai entries
+     * per cell). */
+    int32_t lai_mode, n_lai;
 } ora_domain;
 
 typedef struct {

@@ -39,6 +39,7 @@ class OraDomain(C.Structure):
         ("pre_w", _dp), ("pet_w", _dp), ("temp_w", _dp),
         ("nInflow", C.c_int32), ("inflow_day0", C.c_int32), ("inflow_ndays", C.c_int32), ("pad2_", C.c_int32),
         ("inflow_node", _ip), ("inflow_headwater", _ip), ("inflow_q", _dp),
+        ("lai_mode", C.c_int32), ("n_lai", C.c_int32),
     ]
 
 
@@ -177,6 +178,7 @@ def load(kind: str = "hmath") -> C.CDLL:
     L.ora_output_planes.argtypes = [C.POINTER(OraOutput), C.c_int]
     L.ora_output_planes.restype = C.c_int
     L.ora_step_calendar_ex.argtypes = [C.c_int32, C.c_int32, C.c_int32, _ip, _ip, _ip, _ip, _ip, _ip]
+    L.ora_step_lai.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip]
     L.ora_default_states.argtypes = [C.POINTER(OraDomain), _dp, C.POINTER(OraState)]
     L.ora_math_kind.restype = C.c_int
     L.ora_mpr.argtypes = [C.POINTER(OraMprDomain), C.POINTER(OraGamma), C.POINTER(OraMprOut)]
@@ -216,7 +218,7 @@ class OracleRun:
 
     def __init__(self, dom, params: dict, rout_param=None, proc_sm=1, proc_pet=0, proc_rout=1,
                  hourly=True, read_states=False, kind="hmath", link_celerity=None, meteo_weights=None,
-                 inflow=None):
+                 inflow=None, lai_mode: int = 0, n_lai: int = 12):
         self.L = load(kind)
         self.dom = dom
         self.keep = []
@@ -251,6 +253,10 @@ class OracleRun:
             d.inflow_day0 = int(inflow.get("day0", 1))
             d.inflow_ndays = q.shape[0]
             d.inflow_q = _d(q)
+        # timeStep_LAI_input: 0 = monthly slots; -1 / -2 / -3 = a gridded LAI series of
+        # n_lai daily / monthly / yearly entries (the LAI-indexed parameters then have
+        # n_lai entries per cell)
+        d.lai_mode, d.n_lai = int(lai_mode), int(n_lai)
         if meteo_weights is not None:   # {"pre", "pet", "temp"}: [24][12][n_cells] each
             for n in ("pre", "pet", "temp"):
                 setattr(d, n + "_w", _d(k(meteo_weights[n])))

@@ -8,11 +8,10 @@ the node are cut, src/mRM/mo_mrm_pre_routing.f90:179-214 and
 src/mRM/mo_mrm_routing.f90:447-452), a headwater in domain 2 (added to the
 node's runoff), absent in domain 3.  case_05 reads a monthly gridded LAI
 series (timeStep_LAI_input = -2, src/common/mo_common_datetime_type.f90:
-138-155), which is not in the reference tree, so the time loop here runs
+138-155) whose file is not in the reference tree, so the time loop here runs
 with the effective parameters of the reference's own restart files (the
-regionalisation is pinned by the other cases): maxInter of LAI step
-iLAI = months since the run start, i.e. the 1990 entries with the 1990
-land-cover scene and the 1991 entries (January-June) with the 1991 scene.
+regionalisation is pinned by the other cases), the 18 monthly maxInter
+entries of the run (1990-01 .. 1991-06) as the context's gridded LAI series.
 
 Checked for every domain, on the oracle (libm and hmath builds) and on the
 device: the 365 daily discharges of both gauges equal b<d>_daily_discharge.out
@@ -34,6 +33,7 @@ import test_case00_mpr as mpr_case
 from test_case00_run import HMATH_RTOL, Q_DECIMALS, check_states, daily_means, load_run
 
 GOLD = Path(__file__).resolve().parent / "golden" / "case05_gold.npz"
+N_LAI = 18       # monthly LAI entries of the run, 1990-01 .. 1991-06
 H = 2
 KEYS = {"fSealed": "fSealed", "alpha": "alpha", "degDayInc": "degDayInc", "degDayMax": "degDayMax",
         "degDayNoPre": "degDayNoPre", "fAsp": "fAsp", "karstLoss": "karstLoss", "kfastFlow": "kFastFlow",
@@ -59,9 +59,7 @@ def case05(d: int):
             if a.ndim >= 2:                        # [scene][...]: scene-dependent parameter
                 a = a[scene]
             p[key] = np.ascontiguousarray(a, np.float64).reshape(-1)
-        lai = z[pre + "p_maxInter"]                # [18 LAI months from 1990-01][cell]
-        tab = np.array(lai[0:12]) if scene == 0 else np.concatenate([lai[12:18], lai[6:12]])
-        p["maxInter"] = np.ascontiguousarray(tab).reshape(-1)   # by calendar month of its year
+        p["maxInter"] = np.ascontiguousarray(z[pre + "p_maxInter"]).reshape(-1)  # [18 LAI months][cell]
         ps.append(p)
     gamma = mpr_case.load_case()[2]
     off = params.layout(1, 0, 1, 10)
@@ -76,6 +74,14 @@ def case05(d: int):
     return z0, doms, forcing, ps, rp, inflow, gold
 
 
+def monthly(p):
+    """the parameters with 12 monthly maxInter slots (the first 12 series entries;
+    the series replaces them in the run)"""
+    q = dict(p)
+    q["maxInter"] = p["maxInter"][: 12 * (p["maxInter"].size // N_LAI)]
+    return q
+
+
 def check_discharge(z0, gold, q_steps, warm_days):
     qd = np.stack([daily_means(q_steps[:, i], warm_days) for i in range(q_steps.shape[1])], axis=1)
     assert np.array_equal(np.round(qd, Q_DECIMALS), gold["q"]), np.abs(qd - gold["q"]).max()
@@ -84,7 +90,8 @@ def check_discharge(z0, gold, q_steps, warm_days):
 
 
 def oracle_run(doms, ps, rp, inflow, forcing, s2, n_steps, kind):
-    kw = dict(rout_param=rp, proc_sm=1, proc_pet=0, proc_rout=1, hourly=False, kind=kind, inflow=inflow)
+    kw = dict(rout_param=rp, proc_sm=1, proc_pet=0, proc_rout=1, hourly=False, kind=kind, inflow=inflow,
+              lai_mode=-2, n_lai=N_LAI)
     r1 = oracle.OracleRun(doms[0], ps[0], **kw)
     q1, _, _ = r1.run(forcing, 1, 1, s2)
     r2 = oracle.OracleRun(doms[1], ps[1], **kw)
@@ -119,14 +126,16 @@ def test_gpu_reproduces_case05(domain):
     s2 = int(z0["scene2_from_day"]) * 24
     g = MhmGpu(doms[0], proc_soilmoist=1, proc_pet=0, proc_routing=1, hourly=False, n_members=1)
     try:
-        g.set_eff_params(ps[0])
+        g.set_eff_params(monthly(ps[0]))
         g.set_routing_params(rp)
         g.init_states(0)
+        g.set_lai_series(-2, N_LAI)
+        g.set_lai_params(ps[0]["maxInter"].reshape(N_LAI, -1))
         if inflow is not None:
             g.set_inflow_gauges(inflow["node"], inflow["headwater"], inflow["q"], day0=1)
         g.set_meteo(1, forcing["pre"], forcing["temp"], forcing["pet"])
         q1 = g.run(1, s2)[0].T
-        g.set_eff_params(ps[1])            # land-cover scene 1991: new parameters, states kept
+        g.set_eff_params(monthly(ps[1]))   # land-cover scene 1991: new parameters, states kept
         g.set_link_fpimp(doms[1].ffp_imp)
         g.set_routing_params(rp)
         q2 = g.run(s2 + 1, n_steps - s2)[0].T
