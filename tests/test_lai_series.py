@@ -23,7 +23,7 @@ _ip = C.POINTER(C.c_int32)
 @pytest.mark.parametrize("timestep", [1, 6, 24])
 @pytest.mark.parametrize("mode", [0, -1, -2, -3])
 def test_lai_index_equals_the_reference_counter(jul_start, timestep, mode, lib, ora_hmath):
-    n = (24 // timestep) * 500
+    n = max((24 // timestep) * 500, 600)
     got = np.zeros(n, np.int32)
     assert lib.mhm_step_lai(jul_start, timestep, mode, 1, n, got.ctypes.data_as(_ip)) == 0
     want = np.zeros(n, np.int32)
