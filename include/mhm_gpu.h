@@ -158,6 +158,12 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
 int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai);
 int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, const double *pet_lai,
                        const double *surf_resist);
+/* The member's series entries read back (each pointer may be NULL); mhm_mpr
+ * with gridded L0 LAI of the series' length writes them (the reference's
+ * L1_maxInter, L1_petLAIcorFactor / L1_PrieTayAlpha / L1_aeroResist and
+ * L1_surfResist over size(LAI0, 2) entries, src/MPR/mo_multi_param_reg.f90:
+ * 1142, 1266-1281). */
+int mhm_get_lai_params(mhm_ctx *ctx, int32_t member, double *max_inter, double *pet_lai, double *surf_resist);
 
 /* Floodplain impervious fraction of the links [nLinks] for the land-cover
  * scene that starts (L11_nLinkFracFPimp(:, iLC) of src/mRM/mo_mrm_routing.f90
@@ -544,8 +550,12 @@ typedef struct {
     int32_t max_soil_hor;      /* row stride of the per-soil horizon arrays      */
     int32_t n_geo_units;       /* nGeoUnits                                      */
     int32_t n_lai_classes;     /* > 0: LAI from a look-up table by class;
-                                  0: gridded LAI0 [12][n_cells0]                 */
-    int32_t pad_;
+                                  0: gridded LAI0 [n_lai_steps][n_cells0]        */
+    int32_t n_lai_steps;       /* entries of gridded LAI0 (0: 12 monthly slots);
+                                  a context with a gridded LAI series
+                                  (mhm_set_lai_series) needs its n_lai entries,
+                                  and mhm_mpr then writes the LAI-indexed
+                                  parameters into the series                     */
     double frac_sealed_city;   /* fracSealed_cityArea (mhm.nml)                  */
     const double *horizon_depth;  /* [n_horizons] HorizonDepth_mHM [mm]; the last
                                      entry is replaced per soil type by RZdepth  */
@@ -561,7 +571,7 @@ typedef struct {
     const double *y0;          /* [n_cells0] L0 latitude (sign: hemisphere)      */
     const int32_t *lai_class0; /* [n_cells0] LAI class, n_lai_classes > 0        */
     const double *lai_lut;     /* [n_lai_classes][12] monthly LAI by class       */
-    const double *lai0;        /* [12][n_cells0] gridded LAI, n_lai_classes == 0 */
+    const double *lai0;        /* [n_lai_steps][n_cells0] gridded LAI, n_lai_classes == 0 */
     const int32_t *soil_n_hor;   /* [n_soil_types] soilDB%nHorizons              */
     const int32_t *soil_n_till;  /* [n_soil_types] soilDB%nTillHorizons          */
     const double *soil_ud, *soil_ld;   /* [n_soil_types][max_soil_hor] [mm]      */

@@ -67,7 +67,7 @@ class L0Desc(C.Structure):
     """mhm_l0_desc: level-0 inputs of the parameter regionalisation."""
     _fields_ = [
         ("n_cells0", C.c_int32), ("nrows0", C.c_int32), ("ncols0", C.c_int32), ("n_soil_types", C.c_int32),
-        ("max_soil_hor", C.c_int32), ("n_geo_units", C.c_int32), ("n_lai_classes", C.c_int32), ("pad_", C.c_int32),
+        ("max_soil_hor", C.c_int32), ("n_geo_units", C.c_int32), ("n_lai_classes", C.c_int32), ("n_lai_steps", C.c_int32),
         ("frac_sealed_city", C.c_double), ("horizon_depth", _dp), ("mask0", C.POINTER(C.c_uint8)),
         ("l1_up", _ip), ("l1_down", _ip), ("l1_left", _ip), ("l1_right", _ip), ("l1_nsub", _ip),
         ("soil_id0", _ip), ("lcover0", _ip), ("geo_unit0", _ip), ("slope0", _dp), ("aspect0", _dp), ("y0", _dp),
@@ -125,7 +125,7 @@ EXPORTS = [
     "mhm_batch_create", "mhm_batch_destroy", "mhm_batch_last_error", "mhm_batch_run_members",
     "mhm_l11_network_size", "mhm_l11_network", "mhm_l1_l11_mapping", "mhm_autotune_route",
     "mhm_bounds_checked", "mhm_device_status", "mhm_bounds_selftest", "mhm_set_lai_series", "mhm_set_lai_params",
-    "mhm_step_lai",
+    "mhm_step_lai", "mhm_get_lai_params",
 ]
 
 _LIB = None
@@ -220,6 +220,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.mhm_set_lai_series.argtypes = [vp, C.c_int32, C.c_int32]
     L.mhm_set_lai_params.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
     L.mhm_step_lai.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _ip]
+    L.mhm_get_lai_params.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
     L.mhm_batch_create.argtypes = [C.c_int32, C.POINTER(vp)]
     L.mhm_batch_destroy.argtypes = [vp]
     L.mhm_batch_last_error.argtypes = [vp]

@@ -921,6 +921,25 @@ int mhm_set_inflow_discharge(mhm_ctx *ctx, int32_t day0, int32_t n_days, const d
     return MHM_OK;
 }
 
+// Where mpr() puts the LAI-indexed parameters: the monthly planes (12 LAI
+// entries), or the context's gridded LAI series (as many gridded entries as
+// the series has).  Sets a.n_lai_steps / a.lai_out for members member0.. .
+static int mpr_lai_target(mhm_ctx *ctx, const MprSetup &m, int32_t member0, MprArgs &a)
+{
+    a.n_lai_steps = m.n_lai_steps;
+    a.lai_out = nullptr;
+    if (ctx->lai_mode < 0) {
+        if (m.n_lai_classes > 0 || m.n_lai_steps != ctx->n_lai)
+            return fail(ctx, MHM_ERR_INVALID, "a gridded LAI series of " + std::to_string(ctx->n_lai) +
+                                                  " entries needs gridded L0 LAI with as many entries");
+        a.lai_out = ctx->lai_series.p + (size_t)member0 * 3 * ctx->n_lai * ctx->N;
+    } else if (m.n_lai_steps != 12) {
+        return fail(ctx, MHM_ERR_INVALID, "L0 LAI with " + std::to_string(m.n_lai_steps) +
+                                              " entries needs a gridded LAI series (mhm_set_lai_series)");
+    }
+    return MHM_OK;
+}
+
 int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai)
 {
     if (!ctx) return MHM_ERR_INVALID;
@@ -964,6 +983,23 @@ int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, co
             CK(cudaMemsetAsync(dst, 0, NL * sizeof(double), ctx->stream), "LAI params");
     }
     CK(cudaStreamSynchronize(ctx->stream), "LAI params");
+    return MHM_OK;
+}
+
+int mhm_get_lai_params(mhm_ctx *ctx, int32_t member, double *max_inter, double *pet_lai, double *surf_resist)
+{
+    if (!ctx) return MHM_ERR_INVALID;
+    if (ctx->lai_mode >= 0) return fail(ctx, MHM_ERR_INVALID, "no gridded LAI series");
+    if (member < 0 || member >= ctx->M) return fail(ctx, MHM_ERR_INVALID, "member out of range");
+    ON_CTX_DEVICE(ctx);
+    if (int rc = mhm_sync(ctx)) return rc;
+    const size_t NL = (size_t)ctx->n_lai * ctx->N;
+    double *dst[3] = {max_inter, pet_lai, surf_resist};
+    for (int g = 0; g < 3; ++g)
+        if (dst[g])
+            CK(cudaMemcpy(dst[g], ctx->lai_series.p + ((size_t)member * 3 + g) * NL, NL * sizeof(double),
+                          cudaMemcpyDeviceToHost),
+               "LAI params");
     return MHM_OK;
 }
 
@@ -2637,6 +2673,7 @@ int mhm_mpr(mhm_ctx *ctx, int32_t member0, int32_t n, const double *gammas, int3
     a.member_stride = np * ctx->N;
     a.params = ctx->params.p + (size_t)member0 * a.member_stride;
     (void)slots;
+    if (int rc = mpr_lai_target(ctx, m, member0, a)) return rc;
     CK(launch_mpr(a, s), "mpr");
     g_launches += 2;
     if (ctx->proc_rout == 1 && ctx->n_links > 0) {
@@ -2761,6 +2798,7 @@ int mhm_mpr_noalloc(mhm_ctx *ctx, int32_t member, const double *gamma, int32_t n
     a.petlai = d_petlai;
     a.member_stride = (int64_t)n_param_planes(ctx->H) * ctx->N;
     a.params = ctx->params.p + (size_t)member * a.member_stride;
+    if (int rc = mpr_lai_target(ctx, m, member, a)) return rc;
     CK(launch_mpr(a, s), "mpr");
     g_launches += 2;
     if (ctx->proc_rout == 1 && ctx->n_links > 0) {

@@ -292,6 +292,13 @@ struct MprArgs {
     double *petlai;                // [n_members][3][n_lai][12] reciprocal factors
     double *params;                // effective parameters of the first member
     int64_t member_stride;         // doubles between members' parameter blocks
+    // LAI entries (12 monthly slots, or a gridded series) and, for a series,
+    // where its LAI-indexed parameters go: [member][3][n_lai_steps][n1] from
+    // the first member's block (maxInter, petLAIcorFactor / PrieTayAlpha /
+    // aeroResist, surfResist); nullptr: the monthly parameter planes
+    int32_t n_lai_steps;
+    double *lai_out;
 };
+
 
 } // namespace mhm

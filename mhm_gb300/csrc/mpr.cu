@@ -324,11 +324,13 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
         (a.proc_sm == 2 || a.proc_sm == 3) ? g[a.off.soil + a.off.n_soil_params - 1] : 0.0;
 
     // canopy_intercept_param (src/MPR/mo_multi_param_reg.f90:1132-1152) and
-    // pet_correctbyLAI, per LAI month
+    // pet_correctbyLAI, per LAI entry (12 monthly slots or a gridded series:
+    // the reference loops over size(LAI0, 2), :1142)
     const double gi = g[a.off.interc];
     const size_t slots = (size_t)a.max_sub * N;
     const double *plai = a.petlai + (size_t)m * 3 * a.n_lai_classes * 12;
-    for (int mo = 0; mo < 12; ++mo) {
+    const int n_lai = a.n_lai_steps;
+    for (int mo = 0; mo < n_lai; ++mo) {
         double s_int = 0.0, s_pet = 0.0, s_pt = 0.0, s_ra = 0.0, s_rs = 0.0;
         for (int j = 0; j < ns; ++j) {
             const uint32_t c = __ldg(code + (size_t)j * N);
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
                 double hc = (l == 0) ? pp[0] : pp[1];
                 if (l == 2) {
                     double mx = -1.0e300;
-                    for (int t = 0; t < 12; ++t) {
+                    for (int t = 0; t < n_lai; ++t) { // MAXVAL(LAI0, dim=2) over every entry
                         const double x = a.lai ? __ldg(a.lai + t * slots + (size_t)j * N + k)
                                                : __ldg(a.lai_lut + ((c >> 16) & 0xFFu) * 12 + t);
                         mx = (t == 0 || x > mx) ? x : mx;
@@ -377,11 +379,21 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
                 s_pet = s_pet + inv;
             }
         }
-        out[(size_t)(P_MAXINTER + mo) * N + k] = s_int / dn;
-        out[(size_t)(P_PETLAI + mo) * N + k] = (a.proc_pet == -1) ? dn / s_pet
-                                               : (a.proc_pet == 2) ? s_pt / dn
-                                               : (a.proc_pet == 3) ? s_ra / dn : 0.0;
-        out[(size_t)(P_PET2 + mo) * N + k] = (a.proc_pet == 3) ? s_rs / dn : 0.0;
+        const double v_int = s_int / dn;
+        const double v_pet = (a.proc_pet == -1) ? dn / s_pet
+                             : (a.proc_pet == 2) ? s_pt / dn
+                             : (a.proc_pet == 3) ? s_ra / dn : 0.0;
+        const double v_pet2 = (a.proc_pet == 3) ? s_rs / dn : 0.0;
+        if (a.lai_out) { // a gridded LAI series: [member][3][n_lai][N]
+            double *lo = a.lai_out + (size_t)m * 3 * n_lai * N + (size_t)mo * N + k;
+            lo[0] = v_int;
+            lo[(size_t)n_lai * N] = v_pet;
+            lo[(size_t)2 * n_lai * N] = v_pet2;
+        } else {
+            out[(size_t)(P_MAXINTER + mo) * N + k] = v_int;
+            out[(size_t)(P_PETLAI + mo) * N + k] = v_pet;
+            out[(size_t)(P_PET2 + mo) * N + k] = v_pet2;
+        }
     }
 }
 

@@ -113,6 +113,11 @@ bool mpr_prepare(const mhm_l0_desc &l0, int32_t n1, int32_t H, MprSetup &o, std:
         err = "LAI input missing";
         return false;
     }
+    if (l0.n_lai_steps < 0 || l0.n_lai_steps > 32767 || (l0.n_lai_classes > 0 && l0.n_lai_steps != 0 &&
+                                                        l0.n_lai_steps != 12)) {
+        err = "LAI entries out of range (a look-up table has 12 monthly entries)";
+        return false;
+    }
     o.n1 = n1;
     o.n0 = n0;
     o.H = H;
@@ -120,6 +125,7 @@ bool mpr_prepare(const mhm_l0_desc &l0, int32_t n1, int32_t H, MprSetup &o, std:
     o.max_hor = l0.max_soil_hor;
     o.n_keys = 3 * o.n_soil;
     o.n_lai_classes = l0.n_lai_classes;
+    o.n_lai_steps = (l0.n_lai_classes > 0 || l0.n_lai_steps == 0) ? 12 : l0.n_lai_steps;
     o.n_geo = l0.n_geo_units;
     const size_t nsh = (size_t)o.n_soil * o.max_hor;
     o.n_hor.assign(l0.soil_n_hor, l0.soil_n_hor + o.n_soil);
@@ -216,7 +222,7 @@ bool mpr_prepare(const mhm_l0_desc &l0, int32_t n1, int32_t H, MprSetup &o, std:
     o.sub_code.assign(slots, 0u);
     o.sub_se.assign(slots, 0.0);
     o.sub_asp.assign(slots, 0.0);
-    if (o.n_lai_classes == 0) o.sub_lai.assign(12 * slots, 0.0);
+    if (o.n_lai_classes == 0) o.sub_lai.assign((size_t)o.n_lai_steps * slots, 0.0);
     for (int32_t k = 0; k < n1; ++k) {
         const int32_t iu = l0.l1_up[k], id = l0.l1_down[k], jl = l0.l1_left[k], jr = l0.l1_right[k];
         int32_t slot = 0, c_forest = 0, c_sealed = 0;
@@ -229,7 +235,8 @@ bool mpr_prepare(const mhm_l0_desc &l0, int32_t n1, int32_t H, MprSetup &o, std:
                 o.sub_se[p] = o.slope_emp[c];
                 o.sub_asp[p] = l0.aspect0[c];
                 if (o.n_lai_classes == 0)
-                    for (int m = 0; m < 12; ++m) o.sub_lai[(size_t)m * slots + p] = l0.lai0[(size_t)m * n0 + c];
+                    for (int m = 0; m < o.n_lai_steps; ++m)
+                        o.sub_lai[(size_t)m * slots + p] = l0.lai0[(size_t)m * n0 + c];
                 c_forest += (l0.lcover0[c] == 1);
                 c_sealed += (l0.lcover0[c] == 2);
                 ++slot;

@@ -24,6 +24,7 @@ constexpr uint32_t kMprForest = 1u << 15;
 struct MprSetup {
     int32_t n1 = 0, n0 = 0, max_sub = 0, H = 0;
     int32_t n_soil = 0, max_hor = 0, n_keys = 0, n_lai_classes = 0, n_geo = 0;
+    int32_t n_lai_steps = 12;              // entries of the LAI input (12 for the look-up table)
     double dpth_t_last = 0.0;              // RZdepth of the soil of the last L0 cell
     std::vector<double> horizon_depth;     // [H], last entry = last soil type's RZdepth
     std::vector<double> Wd;                // [n_soil][H][max_hor]
@@ -31,7 +32,7 @@ struct MprSetup {
     std::vector<int32_t> nsub;             // [n1]
     std::vector<uint32_t> sub_code;        // [max_sub][n1]
     std::vector<double> sub_se, sub_asp;   // [max_sub][n1]
-    std::vector<double> sub_lai;           // [12][max_sub][n1], gridded LAI only
+    std::vector<double> sub_lai;           // [n_lai_steps][max_sub][n1], gridded LAI only
     std::vector<double> f_forest, f_sealed, f_perm, f_kar; // [n1]
     std::vector<int32_t> n_hor, n_till, present; // [n_soil]
     std::vector<double> sand, clay, dbm;   // [n_soil][max_hor]

@@ -172,6 +172,12 @@ class MhmGpu:
         self._check(self.L.mhm_set_lai_params(self.ctx, member, *[_d(a) if a is not None else None for a in arrs]),
                     "mhm_set_lai_params")
 
+    def get_lai_params(self, n_lai: int, member: int = 0) -> tuple:
+        """(maxInter, pet group, surfResist) of the member's series, each [n_lai][n_cells]."""
+        out = tuple(np.zeros((n_lai, self.dom.n_cells)) for _ in range(3))
+        self._check(self.L.mhm_get_lai_params(self.ctx, member, *[_d(a) for a in out]), "mhm_get_lai_params")
+        return out
+
     def set_link_fpimp(self, ffp):
         """Floodplain impervious fraction of the links for a new land-cover scene."""
         a = np.ascontiguousarray(ffp, np.float64)
@@ -230,7 +236,9 @@ class MhmGpu:
                   "soil_rz_depth"):
             setattr(d, n, _d(k(getattr(l0, n))))
         if gridded:
-            d.lai0 = _d(k(l0.lai0()))
+            lai0 = k(l0.lai0())
+            d.lai0 = _d(lai0)
+            d.n_lai_steps = int(lai0.shape[0])
         else:
             d.lai_class0 = _i(k(l0.lai_class0, np.int32))
             d.lai_lut = _d(k(l0.lai_lut))

@@ -459,6 +459,7 @@ class L0Maps:
     geo_unit_kar: np.ndarray   # [n_geo] int32
     horizon_depth: np.ndarray  # [H]
     frac_sealed_city: float = 0.6
+    lai_series: np.ndarray | None = None   # [n][N0] a gridded LAI series (replaces the table's 12 months)
 
     @property
     def n_cells0(self) -> int:
@@ -477,7 +478,10 @@ class L0Maps:
         return int(self.geo_unit_list.size)
 
     def lai0(self) -> np.ndarray:
-        """Gridded LAI [12][N0] (the look-up table expanded)."""
+        """Gridded LAI [entries][N0]: the series if set, else the look-up
+        table expanded to [12][N0]."""
+        if self.lai_series is not None:
+            return np.ascontiguousarray(self.lai_series, np.float64)
         return np.ascontiguousarray(self.lai_lut[self.lai_class0 - 1].T)
 
 

@@ -254,13 +254,13 @@ typedef struct {
     int32_t proc_sm;   /* processMatrix(3,1): 1..4 */
     int32_t proc_pet;  /* processMatrix(5,1): -1, 0, 1, 2 */
     int32_t n_soil_params; /* processMatrix(3,2): 17, 18, 22 or 21 */
-    int32_t pad_;
+    int32_t nLAI;      /* entries of LAI0 (size(LAI0, 2)); 0 means 12 */
     double fracSealed_cityArea;
     const int32_t *id0_2d;                        /* [ncols0 * nrows0] */
     const int32_t *up1, *down1, *left1, *right1, *nsub1; /* [nCells1] */
     const int32_t *LCover0, *soilId0, *geoUnit0;  /* [nCells0], 1-based class ids */
     const double *slope_emp0, *Asp0, *y0;         /* [nCells0] */
-    const double *LAI0;                           /* [12][nCells0] */
+    const double *LAI0;                           /* [nLAI][nCells0] */
     const int32_t *present, *nHor, *nTill;        /* [nSoil] */
     const double *sand, *clay, *DbM;              /* [nSoil][maxHor] */
     const double *RZdepth;                        /* [nSoil] */

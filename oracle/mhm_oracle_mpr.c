@@ -133,6 +133,7 @@ static double fraction_cover(const ora_mpr_domain *d, int k1, const int32_t *cls
 int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
 {
     const int N0 = d->nCells0, N1 = d->nCells1, H = d->nH, nS = d->nSoil, mH = d->maxHor;
+    const int nLAI = d->nLAI > 0 ? d->nLAI : 12; /* size(LAI0, 2): monthly slots or a gridded series */
     if (H < 2 || d->proc_sm < 1 || d->proc_sm > 4)
         return -1;
     double *KsVar_H0 = (double *)calloc((size_t)N0, sizeof(double));
@@ -362,7 +363,7 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
     /* ---- PET correction by LAI, src/MPR/mo_mpr_pet.f90:60-140 (harmonic mean) ---- */
     if (d->proc_pet == -1) {
         const double *p = g->pet;
-        for (int m = 0; m < 12; ++m) {
+        for (int m = 0; m < nLAI; ++m) {
             for (int k = 0; k < N0; ++k) {
                 int L = d->LCover0[k];
                 double base = (L == 1) ? p[0] : (L == 2) ? p[1] : p[2];
@@ -395,11 +396,11 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             const int lc = d->LCover0[k];
             hc0[k] = lc == 1 ? p[0] : (lc == 2 ? p[1] : nodata); /* forest, impervious */
             double mx = d->LAI0[k];                                  /* MAXVAL(LAI0, dim=2) */
-            for (int m = 1; m < 12; ++m)
+            for (int m = 1; m < nLAI; ++m)
                 if (d->LAI0[(size_t)m * N0 + k] > mx) mx = d->LAI0[(size_t)m * N0 + k];
             maxlai[k] = mx;
         }
-        for (int m = 0; m < 12; ++m) {
+        for (int m = 0; m < nLAI; ++m) {
             for (int k = 0; k < N0; ++k) {
                 const double lai = d->LAI0[(size_t)m * N0 + k];
                 if (d->LCover0[k] == 3) hc0[k] = p[2] * lai / maxlai[k]; /* pervious: the month's LAI */
@@ -428,13 +429,13 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->HarSamCoeff[k] = 0.0;
         }
         if (o->petLAIcorFactor)
-            for (size_t i = 0; i < (size_t)12 * N1; ++i)
+            for (size_t i = 0; i < (size_t)nLAI * N1; ++i)
                 o->petLAIcorFactor[i] = 0.0;
     } else if (d->proc_pet == 2) {
         /* ---- Priestley-Taylor alpha, src/MPR/mo_mpr_pet.f90:311-369: arithmetic
          * block mean of alpha0 = p1 + p2 * LAI0 per LAI month ---- */
         const double *p = g->pet;
-        for (int m = 0; m < 12; ++m) {
+        for (int m = 0; m < nLAI; ++m) {
             for (int k = 0; k < N0; ++k)
                 tmp0[k] = p[0] + p[1] * d->LAI0[(size_t)m * N0 + k];
             for (int k = 0; k < N1; ++k)
@@ -445,7 +446,7 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->HarSamCoeff[k] = 0.0;
         }
         if (o->petLAIcorFactor)
-            for (size_t i = 0; i < (size_t)12 * N1; ++i)
+            for (size_t i = 0; i < (size_t)nLAI * N1; ++i)
                 o->petLAIcorFactor[i] = 0.0;
     } else {
         /* ---- PET correction by aspect, src/MPR/mo_mpr_pet.f90:214-272 ---- */
@@ -464,7 +465,7 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->HarSamCoeff[k] = (d->proc_pet == 1) ? p[3] : 0.0;
         }
         if (o->petLAIcorFactor)
-            for (size_t i = 0; i < (size_t)12 * N1; ++i)
+            for (size_t i = 0; i < (size_t)nLAI * N1; ++i)
                 o->petLAIcorFactor[i] = 0.0;
     }
     /* ---- mpr_runoff, src/MPR/mo_mpr_runoff.f90:74-194 ---- */
@@ -536,7 +537,7 @@ int ora_mpr(const ora_mpr_domain *d, const ora_gamma *g, ora_mpr_out *o)
             o->kBaseFlow[k] = o->kSlowFlow[k];
     }
     /* ---- canopy_intercept_param (:1076-1159) ---- */
-    for (int m = 0; m < 12; ++m) {
+    for (int m = 0; m < nLAI; ++m) {
         for (int k = 0; k < N0; ++k)
             tmp0[k] = d->LAI0[(size_t)m * N0 + k] * g->interc[0];
         for (int k = 0; k < N1; ++k)

@@ -85,7 +85,7 @@ class OraMprDomain(C.Structure):
     _fields_ = [
         ("nCells0", C.c_int32), ("nrows0", C.c_int32), ("ncols0", C.c_int32), ("nCells1", C.c_int32),
         ("nH", C.c_int32), ("nSoil", C.c_int32), ("maxHor", C.c_int32), ("nGeo", C.c_int32),
-        ("proc_sm", C.c_int32), ("proc_pet", C.c_int32), ("n_soil_params", C.c_int32), ("pad_", C.c_int32),
+        ("proc_sm", C.c_int32), ("proc_pet", C.c_int32), ("n_soil_params", C.c_int32), ("nLAI", C.c_int32),
         ("fracSealed_cityArea", C.c_double), ("id0_2d", _ip),
         ("up1", _ip), ("down1", _ip), ("left1", _ip), ("right1", _ip), ("nsub1", _ip),
         ("LCover0", _ip), ("soilId0", _ip), ("geoUnit0", _ip), ("slope_emp0", _dp), ("Asp0", _dp), ("y0", _dp),
@@ -399,9 +399,11 @@ def oracle_mpr(n1: int, H: int, l0, gamma: np.ndarray, offsets, proc_sm: int = 1
     for i, n in enumerate(("interc", "snow", "soil", "runoff", "pet", "interflow", "perc")):
         setattr(gm, n, C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[i])), _dp))
     gm.geo = C.cast(C.byref(g.ctypes.data_as(C.POINTER(C.c_double)).contents, 8 * int(offsets[8])), _dp)
-    sizes = {"maxInter": 12 * n1, "petLAIcorFactor": 12 * n1, "fRoots": H * n1, "SMs": H * n1, "FC": H * n1,
-             "PW": H * n1, "beta": H * n1, "PrieTayAlpha": 12 * n1, "aeroResist": 12 * n1,
-             "surfResist": 12 * n1}
+    nl = int(l0.lai0().shape[0])       # LAI entries: 12 monthly slots or a gridded series
+    d.nLAI = nl
+    sizes = {"maxInter": nl * n1, "petLAIcorFactor": nl * n1, "fRoots": H * n1, "SMs": H * n1, "FC": H * n1,
+             "PW": H * n1, "beta": H * n1, "PrieTayAlpha": nl * n1, "aeroResist": nl * n1,
+             "surfResist": nl * n1}
     out = {n: np.zeros(sizes.get(n, n1)) for n in MPR_OUT_FIELDS}
     o = OraMprOut(**{n: _d(out[n]) for n in MPR_OUT_FIELDS})
     rc = L.ora_mpr(C.byref(d), C.byref(gm), C.byref(o))

@@ -131,3 +131,48 @@ def test_gpu_series_in_member_mode():
                                n_lai=n_lai)
         qo = run.run(f, t0, t0, C_)[0][:, 0]       # the window's rows from the member's own step
         assert np.array_equal(q[m, 0].view(np.uint64), qo.view(np.uint64)), m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("proc_pet", [0, -1])
+def test_gpu_mpr_of_a_gridded_series_and_its_run(proc_pet):
+    """mpr() over a gridded L0 LAI series of 15 monthly entries writes the
+    series' maxInter (and LAI correction factors) equal to the oracle's mpr()
+    over the same entries, and the run with them equals the oracle's"""
+    from mhm_gb300 import params
+    from mhm_gb300.model import MhmGpu
+    from oracle import oracle
+    dom = synth.make_domain(16, 14, 3, l11_factor=2, seed=51, jul_start=2447893)     # 1990-01-01
+    l0 = synth.make_l0(dom, 2, seed=52)
+    n_lai = 15
+    l0.lai_series = np.random.default_rng(53).uniform(0.2, 6.0, (n_lai, l0.n_cells0))
+    l0.gridded_lai = True
+    gam = params.random_gammas(2, 1, proc_pet, 1, l0.n_geo, seed=54)
+    off = params.offsets(1, proc_pet, 1, l0.n_geo)
+    T = 24 * 45
+    f = synth.make_forcing(dom, T, seed=55)
+    g = MhmGpu(dom, proc_pet=proc_pet, n_members=2)
+    try:
+        g.set_lai_series(-2, n_lai)
+        g.mpr_setup(l0)
+        g.mpr(gam)
+        series = [g.get_lai_params(n_lai, m) for m in range(2)]
+        p_dev = [g.get_eff_params(m) for m in range(2)]
+        for m in range(2):
+            g.init_states(m)
+        g.set_meteo(1, **f)
+        q = g.run(1, T)
+    finally:
+        g.close()
+    for m in range(2):
+        po = oracle.oracle_mpr(dom.n_cells, 3, l0, gam[m], off, 1, proc_pet, "hmath")
+        assert np.array_equal(series[m][0].reshape(-1), po["maxInter"]), m
+        if proc_pet == -1:
+            assert np.array_equal(series[m][1].reshape(-1), po["petLAIcorFactor"]), m
+        p = {k: v for k, v in p_dev[m].items()}
+        p["maxInter"] = series[m][0].reshape(-1)
+        p["petLAIcorFactor"] = series[m][1].reshape(-1)
+        run = oracle.OracleRun(dom, p, rout_param=gam[m][off[7]:off[7] + 5], proc_pet=proc_pet, kind="hmath",
+                               lai_mode=-2, n_lai=n_lai)
+        qo = run.run(f, 1, 1, T)[0][:, 0]
+        assert np.array_equal(q[m, 0].view(np.uint64), qo.view(np.uint64)), m
