@@ -48,6 +48,7 @@ class MhmGpu:
         self.L = _lib.load()
         self.dom = dom
         self.n_members = n_members
+        self._lai = (0, 12)      # (timeStep_LAI_input, LAI entries) of the context
         self._keep: list = []
 
         def keep(a, dt=np.float64):
@@ -165,6 +166,7 @@ class MhmGpu:
         gridded LAI series of n_lai daily / monthly / yearly entries
         (mhm_set_lai_series)."""
         self._check(self.L.mhm_set_lai_series(self.ctx, int(mode), int(n_lai)), "mhm_set_lai_series")
+        self._lai = (int(mode), int(n_lai)) if mode < 0 else (0, 12)
 
     def set_lai_params(self, max_inter, pet_lai=None, surf_resist=None, member: int = 0):
         """The member's LAI-indexed parameters of the series, each [n_lai][n_cells]."""
@@ -500,7 +502,20 @@ class MhmGpu:
         Create the context with read_states=True so that step 1 keeps them."""
         if int(mhm.mask.sum()) != self.dom.n_cells:
             raise MhmError(f"restart has {int(mhm.mask.sum())} L1 cells, the domain {self.dom.n_cells}")
-        self.set_eff_params(mhm.eff_params(scene), member)
+        p = mhm.eff_params(scene)
+        n_lai = mhm.n_lai
+        if self._lai[0] < 0 or n_lai != 12:
+            # a gridded LAI series: its entries go to the context's series
+            if self._lai[0] >= 0 or self._lai[1] != n_lai:
+                raise MhmError(f"the restart holds {n_lai} LAI entries: set_lai_series(mode, {n_lai}) first")
+            lp = mhm.lai_params(scene)
+            pet = {-1: "petLAIcorFactor", 2: "PrieTayAlpha", 3: "aeroResist"}.get(self.proc_pet)
+            self.set_lai_params(lp["maxInter"], lp.get(pet) if pet else None, lp.get("surfResist"), member)
+            N = self.dom.n_cells
+            for k in ("maxInter", "petLAIcorFactor", "PrieTayAlpha", "aeroResist", "surfResist"):
+                if k in p:
+                    p[k] = np.resize(p[k], 12 * N)   # the monthly slots are not read with a series
+        self.set_eff_params(p, member)
         st = dict(mhm.states)
         if mrm is not None:
             if int(mrm.mask.sum()) != self.dom.n_nodes:

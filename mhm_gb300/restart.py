@@ -113,6 +113,25 @@ class MhmRestart:
     n_scenes: int = 1
     extra: dict[str, np.ndarray] = field(default_factory=dict)
 
+    @property
+    def n_lai(self) -> int:
+        """LAI entries of the LAI-indexed parameters (L1_LAITimesteps): 12
+        monthly slots, or the length of a gridded LAI series."""
+        a = self.params.get("maxInter")
+        return int(a.shape[0]) if a is not None and a.ndim == 2 else 12
+
+    def lai_params(self, scene: int = 0) -> dict[str, np.ndarray]:
+        """The scene's LAI-indexed parameters, each [n_lai][n_cells]."""
+        out = {}
+        for var, (name, dims) in EFF_PARAMS.items():
+            if "lai" not in dims or name not in self.params:
+                continue
+            a = self.params[name]
+            if dims[0] == "scene":
+                a = a[min(scene, a.shape[0] - 1)]
+            out[name] = np.ascontiguousarray(a, np.float64)
+        return out
+
     def eff_params(self, scene: int = 0) -> dict[str, np.ndarray]:
         """The scene's parameters as mhm_set_eff_params takes them (flattened)."""
         out = {}
@@ -220,12 +239,15 @@ def write_mhm_restart(path, mask: np.ndarray, states: dict[str, np.ndarray], par
     hd = np.asarray(horizon_depth, np.float64)
     H = hd.size
     S = len(params_by_scene)
+    # LAI entries: 12 monthly slots, or the length of a gridded LAI series
+    mi = params_by_scene[-1].get("maxInter")
+    n_lai = int(np.asarray(mi).size // n) if mi is not None else 12
     with netcdf_file(str(path), "w", version=2) as f:
         f.createDimension("ncols1", mask.shape[0])
         f.createDimension("nrows1", mask.shape[1])
         f.createDimension("L1_SoilHorizons", H)
         f.createDimension("L1_LandCoverPeriods", S)
-        f.createDimension("L1_LAITimesteps", 12)
+        f.createDimension("L1_LAITimesteps", n_lai)
         f.createDimension("bnds", 2)
         v = f.createVariable("L1_domain_mask", "i4", ("ncols1", "nrows1"))
         v[:] = mask.astype(np.int32)

@@ -66,6 +66,62 @@ def test_mhm_restart_round_trip(tmp_path):
         assert np.array_equal(grid[:, mask].reshape(-1), states["soilMoist"])
 
 
+def test_mhm_restart_with_a_gridded_lai_series(tmp_path):
+    """18 LAI entries (a monthly series): L1_LAITimesteps has 18 entries and
+    they come back as the series (n_lai, lai_params)"""
+    mask = _grid_mask()
+    n, H = int(mask.sum()), 2
+    rng = np.random.default_rng(2)
+    states = {k: rng.uniform(0, 100, n) for k in ("interc", "snowpack", "sealSTW", "unsatSTW", "satSTW")}
+    states["soilMoist"] = rng.uniform(0, 100, H * n)
+    p = {name: rng.uniform(0.1, 1.0, n) for name in ("fSealed", "karstLoss", "fAsp")}
+    p["maxInter"] = rng.uniform(0.1, 1.0, 18 * n)
+    path = tmp_path / "series_restart.nc"
+    restart.write_mhm_restart(path, mask, states, [p], np.array([200.0, 1000.0]))
+    r = restart.read_mhm_restart(path)
+    assert r.n_lai == 18
+    assert np.array_equal(r.lai_params(0)["maxInter"].reshape(-1), p["maxInter"])
+    from scipy.io import netcdf_file
+    with netcdf_file(str(path), "r", mmap=False) as f:
+        assert f.dimensions["L1_LAITimesteps"] == 18
+
+
+@pytest.mark.gpu
+def test_gpu_restart_with_a_gridded_lai_series(tmp_path):
+    """a run with a monthly LAI series, written as restart files and resumed
+    in a new context, continues bit for bit as the first context does"""
+    from mhm_gb300 import synth
+    from mhm_gb300.model import MhmGpu
+    dom = synth.make_domain(12, 10, 2, l11_factor=2, seed=8, jul_start=2447893)
+    p = synth.make_eff_params(dom, seed=9)
+    n_lai = 4
+    series = np.random.default_rng(10).uniform(0.1, 3.0, (n_lai, dom.n_cells))
+    f = synth.make_forcing(dom, 24 * 60, seed=11)
+    a = MhmGpu(dom)
+    try:
+        a.prepare(p, synth.ROUTING_PARAMS_DEFAULT)
+        a.set_lai_series(-2, n_lai)
+        a.set_lai_params(series)
+        a.set_meteo(1, **f)
+        a.run(1, 24 * 20)
+        pw = dict(a.get_eff_params(0))
+        pw["maxInter"] = series.reshape(-1)
+        a.write_restart(tmp_path / "m.nc", [pw], mrm_path=tmp_path / "r.nc")
+        q_cont = a.run(24 * 20 + 1, 24 * 40)
+    finally:
+        a.close()
+    b = MhmGpu(dom, read_states=True)
+    try:
+        b.set_routing_params(synth.ROUTING_PARAMS_DEFAULT)
+        b.set_lai_series(-2, n_lai)
+        b.load_restart(restart.read_mhm_restart(tmp_path / "m.nc"), mrm=restart.read_mrm_restart(tmp_path / "r.nc"))
+        b.set_meteo(1, **f)
+        q_res = b.run(24 * 20 + 1, 24 * 40)
+    finally:
+        b.close()
+    assert np.array_equal(q_cont, q_res)
+
+
 def test_mrm_restart_round_trip(tmp_path):
     z = np.load(run_case.FIX)
     mask = np.ones((6, 1), bool)
