@@ -176,3 +176,48 @@ def test_gpu_mpr_of_a_gridded_series_and_its_run(proc_pet):
                                lai_mode=-2, n_lai=n_lai)
         qo = run.run(f, 1, 1, T)[0][:, 0]
         assert np.array_equal(q[m, 0].view(np.uint64), qo.view(np.uint64)), m
+
+
+@pytest.mark.gpu
+def test_gpu_series_in_a_fused_launch():
+    """a context with a gridded LAI series and one with monthly slots, their
+    cell chains in one fused launch, equal the same calls made one context at
+    a time"""
+    import torch
+    from mhm_gb300.model import MhmBatch, MhmGpu
+    C_ = 48
+
+    def contexts():
+        out = []
+        for i, series in enumerate((True, False)):
+            dom = synth.make_domain(14 + 2 * i, 12, 2 + i, l11_factor=2, seed=61 + i, jul_start=2447950)
+            p = synth.make_eff_params(dom, seed=62 + i)
+            g = MhmGpu(dom, n_members=2)
+            g.prepare([p, p], synth.ROUTING_PARAMS_DEFAULT)
+            if series:
+                g.set_lai_series(-1, 4)                      # daily entries
+                for m in range(2):
+                    g.set_lai_params(_series(dom, 4, 63 + m)[0], member=m)
+            f = synth.make_forcing(dom, C_, seed=64 + i)
+            g.set_meteo(1, *[torch.from_numpy(f[k]).cuda() for k in ("pre", "temp", "pet")], on_device=True)
+            out.append(g)
+        return out
+
+    ref, fused = contexts(), contexts()
+    batch = MhmBatch()
+    try:
+        t0 = [np.array([1, 25], np.int32), np.array([1, 0], np.int32)]
+        qa = [np.zeros((2, 1, C_)) for _ in ref]
+        qb = [np.zeros((2, 1, C_)) for _ in fused]
+        for g, t, q in zip(ref, t0, qa):
+            g.run_members_async(t, C_, q)
+            g.sync()
+        batch.run_members(fused, t0, C_, qb)
+        for g in fused:
+            g.sync()
+        for x, y in zip(qa, qb):
+            assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
+    finally:
+        batch.close()
+        for g in ref + fused:
+            g.close()
