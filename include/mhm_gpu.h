@@ -153,8 +153,10 @@ int mhm_get_eff_params(mhm_ctx *ctx, int32_t member, const mhm_eff_params *p);
  * surfResist -- from a series of n_lai entries, iLAI counting the days /
  * months / years from the run's first step (tt = 1 is entry 1).  The series
  * starts zeroed; mhm_set_lai_params fills a member's entries, each array
- * [n_lai][n_cells] or NULL (zeros).  A run whose last step lies beyond the
- * series fails with MHM_ERR_INVALID. */
+ * [n_lai][n_cells] or NULL (zeros).  Only the groups the context's PET case
+ * reads are stored (maxInter always; the second group for PET -1, 2, 3; the
+ * third for 3): the others are ignored and read back as zeros.  A run whose
+ * last step lies beyond the series fails with MHM_ERR_INVALID. */
 int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai);
 int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, const double *pet_lai,
                        const double *surf_resist);

@@ -257,7 +257,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
             } else {             // a gridded LAI series: its entry iLAI
                 if (!bc_ok(BC_LAI_STEP, si.lai - 1, a.n_lai)) break;
                 const size_t NL = (size_t)a.n_lai * N;
-                const double *ls = a.lai_series + (size_t)m * 3 * NL + (size_t)(si.lai - 1) * N + k;
+                const double *ls = a.lai_series + (size_t)m * lai_groups(a.proc_pet) * NL + (size_t)(si.lai - 1) * N + k;
                 imax = __ldg(ls);
                 if (a.proc_pet == -1 || a.proc_pet >= 2) petlai = __ldg(ls + NL);
                 if (!LEAN && a.proc_pet == 3) petsurf = __ldg(ls + 2 * NL);

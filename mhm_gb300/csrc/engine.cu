@@ -932,7 +932,7 @@ static int mpr_lai_target(mhm_ctx *ctx, const MprSetup &m, int32_t member0, MprA
         if (m.n_lai_classes > 0 || m.n_lai_steps != ctx->n_lai)
             return fail(ctx, MHM_ERR_INVALID, "a gridded LAI series of " + std::to_string(ctx->n_lai) +
                                                   " entries needs gridded L0 LAI with as many entries");
-        a.lai_out = ctx->lai_series.p + (size_t)member0 * 3 * ctx->n_lai * ctx->N;
+        a.lai_out = ctx->lai_series.p + (size_t)member0 * lai_groups(ctx->proc_pet) * ctx->n_lai * ctx->N;
     } else if (m.n_lai_steps != 12) {
         return fail(ctx, MHM_ERR_INVALID, "L0 LAI with " + std::to_string(m.n_lai_steps) +
                                               " entries needs a gridded LAI series (mhm_set_lai_series)");
@@ -953,7 +953,7 @@ int mhm_set_lai_series(mhm_ctx *ctx, int32_t mode, int32_t n_lai)
         ctx->lai_mode = 0;
         ctx->n_lai = 0;
     } else {
-        const size_t n = (size_t)ctx->M * 3 * n_lai * ctx->N;
+        const size_t n = (size_t)ctx->M * lai_groups(ctx->proc_pet) * n_lai * ctx->N;
         ctx->lai_series.release();
         CK(ctx->lai_series.ensure(n), "LAI series");
         CK(cudaMemsetAsync(ctx->lai_series.p, 0, n * sizeof(double), ctx->stream), "LAI series");
@@ -974,9 +974,10 @@ int mhm_set_lai_params(mhm_ctx *ctx, int32_t member, const double *max_inter, co
     ON_CTX_DEVICE(ctx);
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t NL = (size_t)ctx->n_lai * ctx->N;
+    const int ng = lai_groups(ctx->proc_pet);
     const double *src[3] = {max_inter, pet_lai, surf_resist};
-    for (int g = 0; g < 3; ++g) {
-        double *dst = ctx->lai_series.p + ((size_t)member * 3 + g) * NL;
+    for (int g = 0; g < ng; ++g) {
+        double *dst = ctx->lai_series.p + ((size_t)member * ng + g) * NL;
         if (src[g])
             CK(cudaMemcpyAsync(dst, src[g], NL * sizeof(double), cudaMemcpyHostToDevice, ctx->stream), "LAI params");
         else
@@ -995,9 +996,12 @@ int mhm_get_lai_params(mhm_ctx *ctx, int32_t member, double *max_inter, double *
     if (int rc = mhm_sync(ctx)) return rc;
     const size_t NL = (size_t)ctx->n_lai * ctx->N;
     double *dst[3] = {max_inter, pet_lai, surf_resist};
+    const int ng = lai_groups(ctx->proc_pet);
     for (int g = 0; g < 3; ++g)
-        if (dst[g])
-            CK(cudaMemcpy(dst[g], ctx->lai_series.p + ((size_t)member * 3 + g) * NL, NL * sizeof(double),
+        if (dst[g] && g >= ng)
+            std::memset(dst[g], 0, NL * sizeof(double)); // a group this PET case does not read
+        else if (dst[g])
+            CK(cudaMemcpy(dst[g], ctx->lai_series.p + ((size_t)member * ng + g) * NL, NL * sizeof(double),
                           cudaMemcpyDeviceToHost),
                "LAI params");
     return MHM_OK;

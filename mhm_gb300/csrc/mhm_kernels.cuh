@@ -137,12 +137,21 @@ struct CellArgs {
     // mode, the rows of the member step table
     int32_t n_forc_rows, n_step_rows;
     // gridded LAI series (timeStep_LAI_input -1 / -2 / -3): the LAI-indexed
-    // parameters as [M][3][n_lai][n_cells] -- maxInter, the petLAIcorFactor /
-    // PrieTayAlpha / aeroResist group, surfResist -- read at step.lai instead
-    // of the monthly planes; nullptr: monthly slots
+    // parameters as [M][lai_groups(proc_pet)][n_lai][n_cells] -- maxInter,
+    // then the petLAIcorFactor / PrieTayAlpha / aeroResist group and
+    // surfResist where the PET case reads them -- read at step.lai instead of
+    // the monthly planes; nullptr: monthly slots
     const double *lai_series;
     int32_t n_lai;
 };
+
+// LAI-indexed parameter groups a gridded LAI series holds for a PET case:
+// maxInter always; the LAI correction factor (-1), Priestley-Taylor alpha (2)
+// or aerodynamic resistance (3); the bulk surface resistance (3)
+__host__ __device__ constexpr int lai_groups(int proc_pet)
+{
+    return 1 + ((proc_pet == -1 || proc_pet >= 2) ? 1 : 0) + (proc_pet == 3 ? 1 : 0);
+}
 
 // One persistent launch of the cell chain over several contexts (with the
 // same process cases' code path): tile t covers work items

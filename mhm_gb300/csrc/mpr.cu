@@ -384,11 +384,12 @@ __global__ void __launch_bounds__(128) mpr_upscale_kernel(MprArgs a)
                              : (a.proc_pet == 2) ? s_pt / dn
                              : (a.proc_pet == 3) ? s_ra / dn : 0.0;
         const double v_pet2 = (a.proc_pet == 3) ? s_rs / dn : 0.0;
-        if (a.lai_out) { // a gridded LAI series: [member][3][n_lai][N]
-            double *lo = a.lai_out + (size_t)m * 3 * n_lai * N + (size_t)mo * N + k;
+        if (a.lai_out) { // a gridded LAI series: [member][lai_groups][n_lai][N]
+            const int ng = lai_groups(a.proc_pet);
+            double *lo = a.lai_out + (size_t)m * ng * n_lai * N + (size_t)mo * N + k;
             lo[0] = v_int;
-            lo[(size_t)n_lai * N] = v_pet;
-            lo[(size_t)2 * n_lai * N] = v_pet2;
+            if (ng > 1) lo[(size_t)n_lai * N] = v_pet;
+            if (ng > 2) lo[(size_t)2 * n_lai * N] = v_pet2;
         } else {
             out[(size_t)(P_MAXINTER + mo) * N + k] = v_int;
             out[(size_t)(P_PETLAI + mo) * N + k] = v_pet;
