@@ -7,6 +7,7 @@ Modules:
              and MhmBatch (the fused multi-context launch)
   serve      the continuous-batching serving loop and the uneven-basins rounds
   network    the L11 network start-up from L0 flow data (host C++)
+  routing    the link celerity of adaptive routing case 3 (L11_calc_celerity)
   restart    mHM / mRM restart files in the reference's layout
   outputs    aggregated flux/state outputs and the daily discharge file
   namelist   mhm.nml / mhm_parameter.nml reader and the run configuration
