@@ -52,6 +52,31 @@ def test_mpr_noalloc_matches_mpr_two_calls_in_a_row(proc_pet):
 
 
 @pytest.mark.gpu
+def test_mpr_noalloc_writes_a_gridded_lai_series():
+    """with a gridded LAI series the LAI-indexed parameters go to the series,
+    bit-identical to mhm_mpr's"""
+    from mhm_gb300.model import MhmGpu
+    dom = synth.make_domain(12, 10, 3, l11_factor=2, seed=1)
+    l0 = synth.make_l0(dom, 4, seed=4)
+    l0.lai_series = np.random.default_rng(5).uniform(0.2, 6.0, (7, l0.n_cells0))
+    l0.gridded_lai = True
+    gm = np.ascontiguousarray(params.random_gammas(1, 1, -1, 1, l0.n_geo, seed=22)[0])
+    g = MhmGpu(dom, proc_soilmoist=1, proc_pet=-1, n_members=2)
+    try:
+        g.set_lai_series(-3, 7)
+        g.mpr_setup(l0)
+        g.mpr(gm, member0=0)
+        rc = g.L.mhm_mpr_noalloc(g.ctx, 1, gm.ctypes.data_as(_dp), gm.size)
+        assert rc == 0, g.L.mhm_last_error(g.ctx)
+        want, got = g.get_lai_params(7, 0), g.get_lai_params(7, 1)
+        assert np.all(want[0] > 0) and np.all(want[1] > 0)
+        for a, b in zip(want[:2], got[:2]):
+            assert _bitwise(a, b)
+    finally:
+        g.close()
+
+
+@pytest.mark.gpu
 def test_mpr_noalloc_rejects_tables_beyond_the_scratch():
     from mhm_gb300.model import MhmGpu
     dom = synth.make_domain(4, 4, 6, l11_factor=2, seed=1)
