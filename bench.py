@@ -392,6 +392,10 @@ def run_gpu(args) -> dict:
         out["cpu_baseline"] = cpu_baseline(dom, l0, gamma, hf, chunk, args)
     if rank == 0 and not args.no_serving:
         out["serving"] = run_serving(args)
+    if rank == 0 and not args.no_uneven:
+        t0 = time.perf_counter()
+        out["uneven"] = run_uneven(args, side_by_side=False)   # fused rounds vs one basin at a time
+        out["uneven"]["wall_s"] = time.perf_counter() - t0
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
@@ -521,7 +525,7 @@ def run_serving(args) -> dict:
     return out
 
 
-def run_uneven(args) -> dict:
+def run_uneven(args, side_by_side: bool = True) -> dict:
     """Batched uneven basins: 64 basins with cell counts log-uniform in
     1e3..2.5e5, 2-6 soil horizons, 90..730-day hourly horizons, each with its
     own D8 network, all submitted at once.  Fused (the headline): rounds of
@@ -551,14 +555,17 @@ def run_uneven(args) -> dict:
     srv.close()
     fused = serve.run_batched(basins, reqs, 240)
     # side by side: the serving loop, one launch per basin context on its own streams
-    reqs_s = fresh()
-    srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=1, spinup_steps=0, autotune=True)
-    streams = srv.serve(reqs_s, timeout_s=3000)
-    tuned = srv.tuned
-    srv.close()
+    streams, tuned, reqs_s = None, None, None
+    if side_by_side:
+        reqs_s = fresh()
+        srv = serve.Server(basins, hbm_budget=150e9, chunk=240, max_slots=1, spinup_steps=0, autotune=True)
+        streams = srv.serve(reqs_s, timeout_s=3000)
+        tuned = srv.tuned
+        srv.close()
     plain = serve.serve_plain(basins, reqs_p, 240)
-    same = all(np.array_equal(a.discharge(), b.discharge()) and np.array_equal(a.discharge(), c.discharge())
-               for a, b, c in zip(reqs, reqs_p, reqs_s))
+    same = all(np.array_equal(a.discharge(), b.discharge()) and (c is None or np.array_equal(a.discharge(),
+                                                                                          c.discharge()))
+               for a, b, c in zip(reqs, reqs_p, reqs_s or [None] * len(reqs)))
     cells = [b.n_cells for b in basins]
     return {"metric": "batched uneven basins: cell-timesteps/s (mHM+mRM, FP64)", "unit": UNIT,
             "basins": len(basins), "cells_min": int(min(cells)), "cells_max": int(max(cells)),
@@ -566,8 +573,8 @@ def run_uneven(args) -> dict:
             "routing_levels": [b.dom.depth_stats()[0] for b in basins],
             "value": fused["throughput"], "plain_value": plain["throughput"],
             "speedup_vs_plain": fused["throughput"] / plain["throughput"],
-            "side_by_side_value": streams["throughput"],
-            "makespan_s": fused["wall_s"], "side_by_side_makespan_s": streams["wall_s"],
+            "side_by_side_value": streams["throughput"] if streams else None,
+            "makespan_s": fused["wall_s"], "side_by_side_makespan_s": streams["wall_s"] if streams else None,
             "plain_makespan_s": plain["wall_s"], "results_identical": bool(same), "autotune_side_by_side": tuned}
 
 
@@ -687,6 +694,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement of the default run")
     ap.add_argument("--uneven", action="store_true", help="measure the batched uneven-basins workload instead")
     ap.add_argument("--uneven-basins", type=int, default=64)
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-basins measurement of the default run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
