@@ -1775,7 +1775,7 @@ int mhm_poll(mhm_ctx *ctx, int32_t *done)
     return MHM_OK;
 }
 
-// The bounds-checked build's verdict on the work that has completed on the
+// The bounds-checked build's status for the work that has completed on the
 // context's device: MHM_OK, or MHM_ERR_BOUNDS with the site and index of the
 // first failed index test (status words read and cleared).
 static int take_bounds_status(mhm_ctx *ctx, int32_t *site, int64_t *index)

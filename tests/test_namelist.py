@@ -1,12 +1,13 @@
 """The namelist reader and the run configuration taken from it.
 
 The syntax cases are written here; the reader is also pinned to the
-reference's own check-case namelists when the reference tree is present
-(the CPU suite runs where it is): case_00's tables and parameter vector
+reference's own check-case namelists (the groups it reads, extracted by
+tests/golden/make_namelist_excerpts.py into namelist_excerpts.json):
+case_00's tables and parameter vector
 equal the ones the case_00 fixtures hold (built by a separate parser in
 tests/golden/make_case00_*.py), and case_04's and case_05's multi-domain
 periods, resolutions and (inflow) gauges are read as their namelists state."""
-import os
+import json
 from pathlib import Path
 
 import numpy as np
@@ -14,8 +15,8 @@ import pytest
 
 from mhm_gb300 import namelist as nl
 
-REF = Path(os.environ.get("MHM_REFERENCE_TREE", "/root/reference"))
 HERE = Path(__file__).resolve().parent
+EXCERPTS = json.loads((HERE / "golden" / "namelist_excerpts.json").read_text())
 
 TEXT = """
 ! a comment line
@@ -71,14 +72,9 @@ def test_unclosed_group_is_an_error():
         nl.read("&a\n x = 1\n")
 
 
-needs_ref = pytest.mark.skipif(not (REF / "check" / "case_00" / "mhm.nml").exists(),
-                               reason="the reference tree is not present")
-
-
-@needs_ref
 def test_case00_configuration_and_parameters():
     z = np.load(HERE / "golden" / "case00_run.npz")
-    cfg = nl.run_config(REF / "check" / "case_00" / "mhm.nml")
+    cfg = nl.run_config(EXCERPTS["case_00/mhm.nml"])
     assert cfg.process_case == [1, 1, 1, 1, 0, 1, 1, 1, 1, 0]
     assert (cfg.proc_sm, cfg.proc_pet, cfg.proc_rout) == (1, 0, 1)
     assert cfg.timestep == 1 and cfg.n_soil_horizons == 2 and cfg.soil_depth == [200.0]
@@ -90,19 +86,18 @@ def test_case00_configuration_and_parameters():
     assert cfg.gauges == [[398]] and cfg.inflow_gauges == [[]]
     assert cfg.lcover_years == [(1981, 1990), (1991, 2000)]
     import test_case00_mpr as mpr_case
-    gam = nl.gamma(REF / "check" / "case_00" / "mhm_parameter.nml", 1, 0, 1)
+    gam = nl.gamma(EXCERPTS["case_00/mhm_parameter.nml"], 1, 0, 1)
     assert np.array_equal(np.array(gam), np.asarray(mpr_case.load_case()[2]))
     # the JSON image gives the same configuration
-    g = nl.read(REF / "check" / "case_00" / "mhm.nml")
+    g = nl.read(EXCERPTS["case_00/mhm.nml"])
     assert nl.run_config(nl.from_json(nl.to_json(g))) == cfg
 
 
-@needs_ref
 def test_multi_domain_cases():
-    c5 = nl.run_config(REF / "check" / "case_05" / "mhm.nml")
+    c5 = nl.run_config(EXCERPTS["case_05/mhm.nml"])
     assert c5.n_domains == 3 and c5.gauges == [[398, 333]] * 3
     assert c5.inflow_gauges == [[(333, False)], [(333, True)], []]
-    c4 = nl.run_config(REF / "check" / "case_04" / "mhm.nml")
+    c4 = nl.run_config(EXCERPTS["case_04/mhm.nml"])
     assert c4.resolution_hydrology == [24000.0, 12000.0, 24000.0, 24000.0, 12000.0, 24000.0]
     assert c4.resolution_routing == [24000.0, 24000.0, 24000.0, 24000.0, 12000.0, 24000.0]
     assert c4.warming_days == [180, 180, 180, 360, 50, 0]
