@@ -101,7 +101,31 @@ def members_fused(status):
             g.close()
 
 
-SCENARIOS = [ensemble_chunks, inflow_window, members_fused]
+def lai_series_mpr(status):
+    """a monthly gridded LAI series regionalised on the device, PET case -1"""
+    from mhm_gb300.model import MhmGpu
+    dom = synth.make_domain(14, 12, 3, l11_factor=2, seed=51, jul_start=2447893)
+    l0 = synth.make_l0(dom, 2, seed=52)
+    l0.lai_series = np.random.default_rng(53).uniform(0.2, 6.0, (3, l0.n_cells0))
+    l0.gridded_lai = True
+    gam = params.random_gammas(2, 1, -1, 1, l0.n_geo, seed=54)
+    f = synth.make_forcing(dom, 24 * 70, seed=55)
+    g = MhmGpu(dom, proc_pet=-1, n_members=2)
+    try:
+        g.set_lai_series(-2, 3)
+        g.mpr_setup(l0)
+        g.mpr(gam)
+        for m in range(2):
+            g.init_states(m)
+        g.set_meteo(1, **f)
+        q = np.concatenate([g.run(1, 24 * 35), g.run(24 * 35 + 1, 24 * 35)], axis=2)
+        status.append(g.device_status())
+        return q.reshape(-1), _flat(g.get_state(1))
+    finally:
+        g.close()
+
+
+SCENARIOS = [ensemble_chunks, inflow_window, members_fused, lai_series_mpr]
 
 
 def run_all():

@@ -2,7 +2,8 @@
 child process on the scenarios of tests/bc_scenarios.py (member-tiled
 ensemble with device MPR, chunked calls and the cluster routing walk; inflow
 gauges with adaptive routing windows; members at their own steps in a fused
-launch), it reports no failed index test and gives results bit-identical to
+launch; a gridded LAI series regionalised on the device), it reports no
+failed index test and gives results bit-identical to
 the default build; its self-test (one failing test with no access behind it)
 comes back as site 99, index 7 and is cleared once read."""
 import os
