@@ -42,7 +42,7 @@ cudaError_t launch_cell_chain_fused(const FusedCellArgs &f, int hl, bool lean, i
 {
     if (f.n_tiles <= 0) return cudaSuccess;
     const int block = 128;
-    const size_t smem = (size_t)hs_planes(hl) * hl * block * sizeof(double);
+    const size_t smem = hs_bytes(hl, block);
     void (*k)(const FusedCellArgs) = nullptr;
     const bool o8 = occ >= 8;
     if (hl == 6)

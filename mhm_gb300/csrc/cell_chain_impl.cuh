@@ -118,9 +118,42 @@ struct CellRegs {
 // where 8 planes of 8 blocks fit the SM -- and are read from the parameter
 // planes in global memory (L1/L2-cached, coalesced) otherwise: with 6
 // horizons they would take 48 KB per block and cap the SM at 4 blocks.
-enum HorizonPlane : int { HS_SM = 0, HS_RSMS, HS_RDEN, HS_PAR0, HS_PLANES_ALL = HS_PAR0 + 5 };
+//
+// HS_FR holds the step's runoff fractions, which the warp evaluates packed
+// (runoff_fractions_packed); with the parameters in global memory a plane of
+// one pointer per thread (each thread's parameter planes) follows the horizon
+// planes, so that a lane can read another lane's SMs and beta.
+enum HorizonPlane : int { HS_SM = 0, HS_RSMS, HS_RDEN, HS_FR, HS_PAR0, HS_PLANES_ALL = HS_PAR0 + 5 };
 __host__ __device__ constexpr bool hs_params_shared(int HL) { return HL <= 3; }
 __host__ __device__ constexpr int hs_planes(int HL) { return hs_params_shared(HL) ? HS_PLANES_ALL : HS_PAR0; }
+// dynamic shared memory of a block of B threads
+__host__ __device__ constexpr size_t hs_bytes(int HL, int B)
+{
+    return (size_t)hs_planes(HL) * HL * B * sizeof(double) + (hs_params_shared(HL) ? 0 : (size_t)B * sizeof(void *));
+}
+
+// exp(beta * log(smh / SMs)) lies in [0, 1] for eps < smh <= SMs when SMs is
+// finite and beta is finite and > 0 (integer tests on the bits)
+__device__ __forceinline__ bool sm_frac_bounded(double sms, double beta)
+{
+    return hm_abs_bits(hm_d2b(sms)) < 0x7ff0000000000000ULL && hm_d2b(beta) - 1 < 0x7fefffffffffffffULL;
+}
+
+// position of the r-th (0-based) set bit of mask (r < popc(mask))
+__device__ __forceinline__ int nth_set_bit(unsigned mask, int r)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(mask & ((1u << w) - 1u));
+        if (r >= c) {
+            r -= c;
+            mask >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
 
 
 // LEAN: compiled for PET input (cases -1, 0) and the Feddes stress (soil-moisture
@@ -164,6 +197,8 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
         if constexpr (hs_params_shared(HL)) return hs(HS_PAR0 + g, h);
         else return __ldg(P + (size_t)(P_HORIZON + g * H + h) * N);
     };
+    const double **hptr = reinterpret_cast<const double **>(hsm + (size_t)hs_planes(HL) * HL * B);
+    if constexpr (!hs_params_shared(HL)) hptr[tb] = P;
     const bool feddes = LEAN || (a.proc_sm == 1 || a.proc_sm == 4);
     CellRegs c;
     const double c2 = a.c2TSTu;
@@ -188,6 +223,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
     c.lat_rad = (a.proc_pet == 1) ? kDeg2Rad * __ldg(a.latitude + k) : 0.0;
     c.r_sthresh = hm_recip_of(c.sthresh);
     c.r_jarvis = hm_recip_of(c.jarvis);
+    bool frac_bounded = true; // every horizon's runoff fraction is in [0, 1]
 #pragma unroll 1
     for (int h = 0; h < H; ++h) {
         if constexpr (hs_params_shared(HL)) {
@@ -197,6 +233,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
         hs(HS_RSMS, h) = hm_b2d(hm_recip_of(sms));
         hs(HS_RDEN, h) = hm_b2d(hm_recip_of(feddes ? fc - pw : sms - pw)); // mo_soil_moisture.f90:358, :435
         hs(HS_SM, h) = reset_sm ? 0.5 * fc : S[(size_t)(S_SM + h) * N];
+        frac_bounded = frac_bounded && sm_frac_bounded(sms, hp(4, h));
     }
     c.interc = S[(size_t)S_INTERC * N];
     c.snow = S[(size_t)S_SNOW * N];
@@ -371,6 +408,47 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
             }
             prec_effect = melt + rain;
         }
+        // ---- the horizons' runoff fractions exp(beta log(SM / SMs)),
+        // mo_soil_moisture.f90:230-234 ----
+        // Each depends on its horizon's start-of-step soil moisture and on
+        // parameters only, so the warp evaluates them ahead of the horizon
+        // loop, packed: the (lane, horizon) pairs of the lanes that need them
+        // are spread over all lanes of the warp, a pass of the warp per 32
+        // pairs instead of one per horizon.  A lane whose effective
+        // precipitation is +0 -- and whose fractions are known to lie in
+        // [0, 1] -- needs none: every horizon's input is then +0, and
+        // pin * (1 - frac) is +0 for every such fraction, so the loop takes 0.
+        // The same function of the same operands gives the same bits on any
+        // lane.
+        const bool need_frac = hm_d2b(prec_effect) != 0 || !frac_bounded;
+        {
+            const unsigned gm = __activemask();
+            __syncwarp(gm); // the soil moisture the lanes wrote last step is visible
+            const unsigned nm = __ballot_sync(gm, need_frac);
+            unsigned lt;
+            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+            const int G = __popc(gm), n_tasks = __popc(nm) * H, wb = tb & ~31;
+#pragma unroll 1
+            for (int t = __popc(gm & lt); t < n_tasks; t += G) {
+                const int r = t / H, h = t - r * H;
+                const int ol = wb + nth_set_bit(nm, r); // the lane the pair belongs to
+                const double smh = hsm[(HS_SM * HL + h) * B + ol];
+                double sms, beta;
+                if constexpr (hs_params_shared(HL)) {
+                    sms = hsm[((HS_PAR0 + 1) * HL + h) * B + ol];
+                    beta = hsm[((HS_PAR0 + 4) * HL + h) * B + ol];
+                } else {
+                    const double *Po = hptr[ol];
+                    sms = __ldg(Po + (size_t)(P_HORIZON + H + h) * N);
+                    beta = __ldg(Po + (size_t)(P_HORIZON + 4 * H + h) * N);
+                }
+                double fr = 0.0;
+                if (hm_gt(smh, kEps) && !hm_gt(smh, sms))
+                    fr = hm_exp(beta * hm_log(hm_div_r(smh, sms, hm_d2b(hsm[(HS_RSMS * HL + h) * B + ol]))));
+                hsm[(HS_FR * HL + h) * B + ol] = fr;
+            }
+            __syncwarp(gm); // the fractions are visible to their lanes
+        }
         // ---- soil_moisture, mo_soil_moisture.f90:176-286 ----
         double runoff_sealed = 0.0;
         double infil_last;
@@ -400,9 +478,8 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
                 const double sms = hp(1, h);
                 double smh = hs(HS_SM, h);
                 if (!hm_gt(smh, sms)) { // else the horizon passes its input on: infil stays pin
-                    double frac_runoff = 0.0;
-                    if (hm_gt(smh, kEps))
-                        frac_runoff = hm_exp(hp(4, h) * hm_log(hm_div_r(smh, sms, hm_d2b(hs(HS_RSMS, h)))));
+                    // evaluated above (0 when smh <= eps), or 0 for a lane that needs none
+                    const double frac_runoff = hm_sel(need_frac, hs(HS_FR, h), 0.0);
                     const double tmp = pin * (1.0 - frac_runoff);
                     const double filled = smh + tmp;
                     const bool over = hm_gt(filled, sms);
@@ -626,7 +703,7 @@ cudaError_t launch_cell_chain_h(const CellArgs &a, int H, cudaStream_t s)
     const unsigned grid = member_tiles(a.n_members)
                               ? (unsigned)(((int64_t)a.n_cells + 31) / 32 * (a.n_members / 4))
                               : (unsigned)((n + block - 1) / block);
-    const size_t smem = (size_t)hs_planes(H) * H * block * sizeof(double);
+    const size_t smem = hs_bytes(H, block);
     switch (H) {
 #define MHM_CASE(HH)                                                                                               \
     case HH:                                                                                                       \
