@@ -311,7 +311,7 @@ def run_gpu(args) -> dict:
     ms, value = replica_throughput(ms, float(N) * chunk * args.steps, world, device)
 
     # ---- e2e: host forcing (pinned), H2D + compute + D2H of the gauge series per step ----
-    e2e_steps = max(1, min(args.steps, 16))
+    e2e_steps = 16  # whole steps, so that filling and draining the copy / routing pipeline is amortised
     step(args.warmup + args.steps, on_device=False)  # warm the staging buffers
     g.sync()
     barrier()
@@ -340,10 +340,16 @@ def run_gpu(args) -> dict:
     fp64_line = {"peak": fp64_peak / 1e12 if fp64_peak else None, "unit": "TFLOP/s",
                  "peak_source": "measured live (DFMA probe, 2 FLOP per DFMA)"}
     ops = traffic_from_profiles_ops()
+    pipe_ops = profile_figure("fp64_pipe_ops_per_cell_step")
     if fp64_peak and ops:
         flops = ops * N * chunk / per_launch_s
         fp64_line.update({"achieved": flops / 1e12, "frac": flops / fp64_peak, "flop_per_cell_step": ops,
                           "kernel": "cell_chain_kernel<6>"})
+    if fp64_peak and pipe_ops:
+        # occupancy of the FP64 pipe: a DADD or DMUL takes a full slot, as a
+        # DFMA does, so the operations count against the DFMA issue rate
+        fp64_line.update({"pipe_ops_per_cell_step": pipe_ops,
+                          "pipe_frac": pipe_ops * N * chunk / per_launch_s / (fp64_peak / 2.0)})
     # the roof that binds the kernel: warp instructions issued (4 schedulers per SM,
     # one instruction each per cycle) at the SM clock sampled under load
     wi = profile_figure("warp_inst_per_cell_step")
@@ -367,14 +373,15 @@ def run_gpu(args) -> dict:
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * chunk * N * 8,
                 "d2h_bytes_per_step": chunk * len(dom.gauge_node) * 8, "steps": e2e_steps},
         "gpu_launches": int(launches),
-        # the contract's HBM view of the dominant kernel; the roof that binds it
-        # is the FP64 / integer issue rate (roofline_fp64)
+        # the contract's HBM view of the dominant kernel; the roofs that bind
+        # it are the FP64 pipe and the instruction issue rate
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": (tb * N * chunk) if tb else None,
                      "kernel": "cell_chain_kernel<6>", "alg_bytes_per_launch": alg_bytes,
                      "launch_ms": per_launch_s * 1e3, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"
                      if peaks else "of fallback",
-                     "binding_roof": "fp64+integer issue (roofline_fp64); HBM is not the limit"},
+                     "binding_roof": "the FP64 pipe (roofline_fp64.pipe_frac) and instruction issue "
+                                     "(roofline_issue); HBM is not the limit"},
         "roofline_fp64": fp64_line,
         "roofline_issue": issue_line,
         "kernel_time_ms": {"cell_chain": t_cell, "runoff_acc": t_acc, "routing": t_rt,

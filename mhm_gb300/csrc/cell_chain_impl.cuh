@@ -119,7 +119,7 @@ struct CellRegs {
 // planes in global memory (L1/L2-cached, coalesced) otherwise: with 6
 // horizons they would take 48 KB per block and cap the SM at 4 blocks.
 //
-// HS_FR holds the step's runoff fractions, which the warp evaluates packed
+// HS_FR holds 1 - the step's runoff fractions, which the warp evaluates packed
 // (runoff_fractions_packed); with the parameters in global memory a plane of
 // one pointer per thread (each thread's parameter planes) follows the horizon
 // planes, so that a lane can read another lane's SMs and beta.
@@ -445,7 +445,7 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
                 double fr = 0.0;
                 if (hm_gt(smh, kEps) && !hm_gt(smh, sms))
                     fr = hm_exp(beta * hm_log(hm_div_r(smh, sms, hm_d2b(hsm[(HS_RSMS * HL + h) * B + ol]))));
-                hsm[(HS_FR * HL + h) * B + ol] = fr;
+                hsm[(HS_FR * HL + h) * B + ol] = 1.0 - fr;
             }
             __syncwarp(gm); // the fractions are visible to their lanes
         }
@@ -478,9 +478,9 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
                 const double sms = hp(1, h);
                 double smh = hs(HS_SM, h);
                 if (!hm_gt(smh, sms)) { // else the horizon passes its input on: infil stays pin
-                    // evaluated above (0 when smh <= eps), or 0 for a lane that needs none
-                    const double frac_runoff = hm_sel(need_frac, hs(HS_FR, h), 0.0);
-                    const double tmp = pin * (1.0 - frac_runoff);
+                    // 1 - frac_runoff, evaluated above (frac_runoff = 0 when smh <= eps),
+                    // or 1 - 0 for a lane that needs none
+                    const double tmp = pin * hm_sel(need_frac, hs(HS_FR, h), 1.0);
                     const double filled = smh + tmp;
                     const bool over = hm_gt(filled, sms);
                     // pin + (smh - sms) or pin - tmp, as one addition: pin - tmp is
