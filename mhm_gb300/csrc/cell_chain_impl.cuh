@@ -115,9 +115,9 @@ struct CellRegs {
 //
 // The read-only per-horizon parameters (fRoots, SMs, FC, PW, beta) are copied
 // to shared memory too when that costs no occupancy -- up to 3 horizons,
-// where 8 planes of 8 blocks fit the SM -- and are read from the parameter
+// where 9 planes of 8 blocks fit the SM -- and are read from the parameter
 // planes in global memory (L1/L2-cached, coalesced) otherwise: with 6
-// horizons they would take 48 KB per block and cap the SM at 4 blocks.
+// horizons they would take 54 KB per block and cap the SM at 4 blocks.
 //
 // HS_FR holds 1 - the step's runoff fractions, which the warp evaluates packed
 // (runoff_fractions_packed); with the parameters in global memory a plane of
