@@ -248,3 +248,53 @@ def test_degenerate_parameters_bitwise(proc_sm):
     f = synth.make_forcing(dom, 24 * 20, seed=34, gamma_theta=4.0)
     gpu, ora = run_pair(dom, p, f, 24 * 20, proc_sm=proc_sm)
     _assert_all_bitwise(gpu, ora)
+
+
+@pytest.mark.parametrize("H", [3, 6])
+def test_unbounded_runoff_fraction_bitwise(H):
+    """The warp evaluates the horizons' runoff fractions exp(beta log(SM/SMs))
+    only for cells with effective precipitation other than +0, unless a
+    cell's fraction may leave [0, 1]: beta zero, negative or subnormal, SMs
+    infinite.  Cells with those parameters, mixed with ordinary ones in every
+    warp, under forcing with 70 % dry hours, equal the oracle bit for bit."""
+    dom = synth.make_domain(16, 20, H, 4, seed=41)
+    N = dom.n_cells
+    p = {k: np.array(v, np.float64, copy=True) for k, v in synth.make_eff_params(dom, seed=42).items()
+         if v is not None}
+    rng = np.random.default_rng(43)
+    cat = rng.integers(0, 5, N)          # 0 ordinary, 1 beta = 0, 2 beta < 0, 3 beta subnormal, 4 SMs = inf
+    beta = p["soilMoistExp"].reshape(H, N)
+    sms = p["soilMoistSat"].reshape(H, N)
+    for h in (0, H - 1):
+        beta[h, cat == 1] = 0.0
+        beta[h, cat == 2] = -0.4
+        beta[h, cat == 3] = 5e-324
+        sms[h, cat == 4] = np.inf
+    f = synth.make_forcing(dom, 24 * 20, seed=44)
+    gpu, ora = run_pair(dom, p, f, 24 * 20)
+    _assert_all_bitwise(gpu, ora)
+
+
+def test_members_across_warps_bitwise():
+    """Three parameter sets on 255 cells and 6 horizons: warps hold the last
+    cells of one member and the first of the next, and the packed runoff
+    fractions read the other lanes' parameter planes.  Each member equals
+    its own oracle run bit for bit."""
+    dom = synth.make_domain(15, 17, 6, 3, seed=51)
+    plist = [synth.make_eff_params(dom, seed=s) for s in (52, 53, 54)]
+    rlist = np.array([synth.ROUTING_PARAMS_DEFAULT,
+                      [0.33, 0.072, 2.05, 0.095, 0.2],
+                      [0.315, 0.078, 1.97, 0.105, 0.45]])
+    f = synth.make_forcing(dom, 24 * 12, seed=55)
+    n = 24 * 12
+    g = MhmGpu(dom, n_members=3)
+    g.prepare(plist, rlist)
+    g.set_meteo(1, **f)
+    q3 = g.run(1, n)
+    for m in range(3):
+        o = OracleRun(dom, plist[m], rlist[m])
+        q_o, _, _ = o.run(f, 1, 1, n)
+        assert bitwise(q3[m].T, q_o), f"member {m}: gauge Q max rel {max_rel(q3[m].T, q_o)}"
+        st = g.get_state(m)
+        for k, ko in STATE_MAP.items():
+            assert bitwise(st[k], o.state[ko]), f"member {m} state {k}: max rel {max_rel(st[k], o.state[ko])}"
