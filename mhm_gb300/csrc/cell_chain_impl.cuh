@@ -120,7 +120,7 @@ struct CellRegs {
 // horizons they would take 54 KB per block and cap the SM at 4 blocks.
 //
 // HS_FR holds 1 - the step's runoff fractions, which the warp evaluates packed
-// (runoff_fractions_packed); with the parameters in global memory a plane of
+// at the top of each step's soil moisture; with the parameters in global memory a plane of
 // one pointer per thread (each thread's parameter planes) follows the horizon
 // planes, so that a lane can read another lane's SMs and beta.
 enum HorizonPlane : int { HS_SM = 0, HS_RSMS, HS_RDEN, HS_FR, HS_PAR0, HS_PLANES_ALL = HS_PAR0 + 5 };
@@ -417,7 +417,8 @@ __device__ __forceinline__ void cell_chain_item(const CellArgs &a, const int m, 
         // pairs instead of one per horizon.  A lane whose effective
         // precipitation is +0 -- and whose fractions are known to lie in
         // [0, 1] -- needs none: every horizon's input is then +0, and
-        // pin * (1 - frac) is +0 for every such fraction, so the loop takes 0.
+        // pin * (1 - frac) is +0 for every such fraction, so the loop takes
+        // frac = 0.
         // The same function of the same operands gives the same bits on any
         // lane.
         const bool need_frac = hm_d2b(prec_effect) != 0 || !frac_bounded;
